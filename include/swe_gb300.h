@@ -1,0 +1,131 @@
+/* swe_gb300.h - C ABI of the GB300 (sm_103a) backend for the shallow-water hot path:
+ * MUSCL reconstruction with hydrostatic well-balanced bathymetry, HLL fluxes in x
+ * and y, the SSP-RK3 stage update, wall boundary conditions and the CFL
+ * max-wave-speed reduction.
+ *
+ * The reference has no C ABI: its backends are C++ classes that own host and device
+ * arrays and call kernels directly (include/backend/cuda/cuda_solver.hpp:107-597).
+ * This header is the thin layer a backend class calls instead; each entry point
+ * names the reference member it replaces.  Plain pointers and sizes only, no
+ * exceptions: every call returns an swe_status and the context keeps a message.
+ *
+ * Layout contract (include/backend/serial/HPC/HPC_kernels.hpp:18-31,
+ * include/core/array2D.hpp:33): host arrays are full ghosted double grids with
+ * nG = 2, Nx_total = Nx + 4, Ny_total = Ny + 4, row-major, index
+ * k = i * Ny_total + j, i = x (slow), j = y (contiguous).  The library owns all device
+ * memory; callers own host buffers, which are copied in and out.
+ *
+ * Threading: one context per host thread.  Each context owns one CUDA stream;
+ * calls are synchronous on return.
+ */
+#ifndef SWE_GB300_H
+#define SWE_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SWE_GB300_ABI_VERSION 1
+
+typedef enum swe_status {
+    SWE_OK = 0,
+    SWE_ERR_BAD_ARG = 1,     /* invalid argument or context */
+    SWE_ERR_CUDA = 2,        /* a CUDA runtime call failed (CUDA_SOLVER_CHECK, cuda_solver.hpp:36-44) */
+    SWE_ERR_NONFINITE = 3,   /* non-finite state after a stage (HPC_kernels.hpp:310-312) */
+    SWE_ERR_CFL = 4,         /* fixed dt above the CFL limit (HPC_solver.hpp:142-145) */
+    SWE_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+    SWE_ERR_NO_DEVICE = 6,   /* no usable CUDA device */
+    SWE_ERR_UNSUPPORTED = 7  /* option not available in this build */
+} swe_status;
+
+typedef enum swe_bc {
+    SWE_BC_REFLECTING = 0,   /* apply_reflecting_bc, HPC_solver.hpp:320-371 */
+    SWE_BC_TRANSMISSIVE = 1  /* zero-gradient ghost copies; no reference counterpart */
+} swe_bc;
+
+typedef enum swe_precision {
+    SWE_PRECISION_FP64 = 0,       /* the drop-in: bitwise equal to HPC_solver */
+    SWE_PRECISION_FP32_MIXED = 1  /* FP32 bulk, FP64 where balance/conservation need it */
+} swe_precision;
+
+typedef struct swe_params {
+    int Nx, Ny;       /* interior cells, each >= 2 (mesh.Nx/Ny, configs/config.hpp:21-30) */
+    int nG;           /* ghost layers; must be 2 (MUSCL, solver_assembly.hpp validate_config) */
+    double Lx, Ly;    /* domain size; dx = Lx / Nx, dy = Ly / Ny (include/core/grid.hpp:19-20) */
+    double g;         /* gravity; <= 0 selects the reference's 9.80665 (include/constants.hpp:4) */
+    double cfl;       /* CFL number (time.cfl) used by the max-wave-speed reduction */
+    int bc;           /* swe_bc */
+    int precision;    /* swe_precision */
+    int device;       /* CUDA device ordinal */
+    int reserved[5];  /* must be zero */
+} swe_params;
+
+typedef struct swe_ctx swe_ctx; /* opaque */
+
+/* Fills *p with defaults: nG = 2, L = 1, g = 9.80665, cfl = 0.45, reflecting, FP64,
+ * device 0.  Nx and Ny must still be set. */
+void swe_params_default(swe_params *p);
+
+/* Allocates the device state for one grid.  Replaces the backend constructors'
+ * allocation (cuda_solver.hpp:109-152, allocate_device :233-252). */
+int swe_create(const swe_params *p, swe_ctx **out);
+
+/* Releases device memory and the stream (cuda_solver.hpp:149). NULL is ignored. */
+void swe_destroy(swe_ctx *ctx);
+
+/* Copies a full ghosted state and bathymetry from host memory to the device
+ * (upload_initial_state_to_device, cuda_solver.hpp:277-286).  Ghost values of
+ * h, hu, hv are ignored (the boundary condition defines them); ghost values of B are
+ * used as given, as the reference does after apply_scalar_reflecting_bc
+ * (HPC_solver.hpp:112-117).  B may be NULL to keep the previous bathymetry. */
+int swe_upload(swe_ctx *ctx, const double *h, const double *hu, const double *hv,
+               const double *B);
+
+/* Copies the state back with ghosts refreshed by the boundary condition, i.e.
+ * exactly the arrays h_, hu_, hv_ of the reference after a step
+ * (download_state_from_device, cuda_solver.hpp:288-296). */
+int swe_download(swe_ctx *ctx, double *h, double *hu, double *hv);
+
+/* Advances n_steps SSP-RK3 steps (rk3_step, HPC_solver.hpp:233-318, inside the run
+ * loop :168-197).  dt > 0: every step uses dt (the reference's fixed
+ * end_time / time_steps, HPC_solver.hpp:94).  dt <= 0: adaptive, every step uses
+ * cfl * min(dx, dy) / max_wave_speed(U^n) (compute_stable_dt, HPC_kernels.hpp:281-298),
+ * reduced on the device inside the last stage of the previous step.  If t_inout is
+ * not NULL, *t_inout += dt for every step, in step order (HPC_solver.hpp:170).
+ * Returns SWE_ERR_NONFINITE if any stage produced a non-finite interior value (the
+ * state is then undefined), checked once per call. */
+int swe_step(swe_ctx *ctx, int n_steps, double dt, double *t_inout);
+
+/* Max over interior cells of max(|u| + c, |v| + c), c = sqrt(g max(0, h)), of the
+ * current state (the reduction inside compute_stable_dt). */
+int swe_max_wave_speed(swe_ctx *ctx, double *out);
+
+/* compute_stable_dt of the current state (HPC_kernels.hpp:281-298): 1e100 when the
+ * max wave speed is <= 1e-8.  The reference's CFL guard (HPC_solver.hpp:134-145) is
+ * this value compared with the fixed dt. */
+int swe_stable_dt(swe_ctx *ctx, double *out);
+
+/* Copies the dt of each step of the last swe_step call (up to n values) to out and
+ * returns how many were written in *written. */
+int swe_dt_log(swe_ctx *ctx, double *out, int n, int *written);
+
+/* Message of the last failed call on ctx ("" when none). */
+const char *swe_last_error(const swe_ctx *ctx);
+
+/* Static name of a status code. */
+const char *swe_status_string(int status);
+
+/* Number of kernels this library launched on ctx since creation (for accounting). */
+long long swe_kernel_launches(const swe_ctx *ctx);
+
+/* Device time in milliseconds of the stage kernels of the last swe_step call,
+ * measured with CUDA events on the context's stream (the reference's per-phase
+ * timers, HPC_solver.hpp:27-86, time the same loop on the host). */
+int swe_last_step_ms(const swe_ctx *ctx, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SWE_GB300_H */

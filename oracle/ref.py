@@ -1,0 +1,64 @@
+"""ctypes binding of the reference's own solver built by ``make ref`` (test infrastructure).
+
+Available only where the reference sources were present at build time; callers
+skip when :func:`available` is False.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBS = {
+    "g980665": os.path.join(HERE, "_ref", "libswe_ref.so"),
+    "g981": os.path.join(HERE, "_ref", "libswe_ref_g981.so"),
+}
+SOLVER_HPC = 0
+SOLVER_OMP = 1
+
+_libs = {}
+
+
+def available(variant="g980665") -> bool:
+    return os.path.exists(LIBS[variant])
+
+
+def lib(variant="g980665"):
+    if variant not in _libs:
+        L = ctypes.CDLL(LIBS[variant])
+        dp = ctypes.POINTER(ctypes.c_double)
+        i, d = ctypes.c_int, ctypes.c_double
+        L.ref_run.argtypes = [i, i, d, d, d, i, i, i, d, dp, dp, dp, dp, dp, dp]
+        L.ref_run.restype = ctypes.c_int
+        L.ref_stable_dt.argtypes = [i, i, d, d, d, dp, dp, dp]
+        L.ref_stable_dt.restype = ctypes.c_double
+        L.ref_gravity.argtypes = []
+        L.ref_gravity.restype = ctypes.c_double
+        _libs[variant] = L
+    return _libs[variant]
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def run(Nx, Ny, h, hu, hv, B, steps, dt_fixed=0.0, Lx=1.0, Ly=1.0, cfl=0.45, bc=0,
+        solver=SOLVER_HPC, variant="g980665"):
+    """Runs the reference; returns (h, hu, hv, dts, t, status) on copies."""
+    h, hu, hv = (np.array(a, dtype=np.float64, order="C", copy=True) for a in (h, hu, hv))
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    dts = np.zeros(max(steps, 1))
+    t = ctypes.c_double(0.0)
+    st = lib(variant).ref_run(Nx, Ny, Lx, Ly, cfl, bc, solver, steps, dt_fixed, _p(h), _p(hu),
+                              _p(hv), _p(B), _p(dts), ctypes.byref(t))
+    return h, hu, hv, dts[:steps], t.value, st
+
+
+def stable_dt(Nx, Ny, h, hu, hv, Lx=1.0, Ly=1.0, cfl=0.45, variant="g980665") -> float:
+    return lib(variant).ref_stable_dt(Nx, Ny, Lx, Ly, cfl, _p(h), _p(hu), _p(hv))
+
+
+def gravity(variant="g980665") -> float:
+    return lib(variant).ref_gravity()

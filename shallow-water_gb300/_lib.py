@@ -1,0 +1,94 @@
+"""ctypes binding of the C ABI in include/swe_gb300.h (libswe_gb300.so, built in-tree).
+
+Loading never falls back to anything: if the shared library is missing or does not
+export the ABI, :func:`lib` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libswe_gb300.so")
+
+SWE_OK = 0
+SWE_ERR_BAD_ARG = 1
+SWE_ERR_CUDA = 2
+SWE_ERR_NONFINITE = 3
+SWE_ERR_CFL = 4
+SWE_ERR_TIMEOUT = 5
+SWE_ERR_NO_DEVICE = 6
+SWE_ERR_UNSUPPORTED = 7
+
+SWE_BC_REFLECTING = 0
+SWE_BC_TRANSMISSIVE = 1
+SWE_PRECISION_FP64 = 0
+SWE_PRECISION_FP32_MIXED = 1
+
+# Every symbol include/swe_gb300.h declares.
+EXPORTS = (
+    "swe_params_default", "swe_create", "swe_destroy", "swe_upload", "swe_download",
+    "swe_step", "swe_max_wave_speed", "swe_stable_dt", "swe_dt_log", "swe_last_error",
+    "swe_status_string", "swe_kernel_launches", "swe_last_step_ms",
+)
+
+
+class SweParams(ctypes.Structure):
+    _fields_ = [
+        ("Nx", ctypes.c_int),
+        ("Ny", ctypes.c_int),
+        ("nG", ctypes.c_int),
+        ("Lx", ctypes.c_double),
+        ("Ly", ctypes.c_double),
+        ("g", ctypes.c_double),
+        ("cfl", ctypes.c_double),
+        ("bc", ctypes.c_int),
+        ("precision", ctypes.c_int),
+        ("device", ctypes.c_int),
+        ("reserved", ctypes.c_int * 5),
+    ]
+
+
+_lib = None
+
+
+def lib(path: str = LIB_PATH):
+    """Loads libswe_gb300.so and declares the ABI; raises if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} not found: build it first (python shallow-water_gb300/build.py); "
+            "there is no CPU fallback")
+    L = ctypes.CDLL(path)
+    dp = ctypes.POINTER(ctypes.c_double)
+    vp = ctypes.c_void_p
+    L.swe_params_default.argtypes = [ctypes.POINTER(SweParams)]
+    L.swe_params_default.restype = None
+    L.swe_create.argtypes = [ctypes.POINTER(SweParams), ctypes.POINTER(vp)]
+    L.swe_create.restype = ctypes.c_int
+    L.swe_destroy.argtypes = [vp]
+    L.swe_destroy.restype = None
+    L.swe_upload.argtypes = [vp, dp, dp, dp, dp]
+    L.swe_upload.restype = ctypes.c_int
+    L.swe_download.argtypes = [vp, dp, dp, dp]
+    L.swe_download.restype = ctypes.c_int
+    L.swe_step.argtypes = [vp, ctypes.c_int, ctypes.c_double, dp]
+    L.swe_step.restype = ctypes.c_int
+    L.swe_max_wave_speed.argtypes = [vp, dp]
+    L.swe_max_wave_speed.restype = ctypes.c_int
+    L.swe_stable_dt.argtypes = [vp, dp]
+    L.swe_stable_dt.restype = ctypes.c_int
+    L.swe_dt_log.argtypes = [vp, dp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    L.swe_dt_log.restype = ctypes.c_int
+    L.swe_last_error.argtypes = [vp]
+    L.swe_last_error.restype = ctypes.c_char_p
+    L.swe_status_string.argtypes = [ctypes.c_int]
+    L.swe_status_string.restype = ctypes.c_char_p
+    L.swe_kernel_launches.argtypes = [vp]
+    L.swe_kernel_launches.restype = ctypes.c_longlong
+    L.swe_last_step_ms.argtypes = [vp, dp]
+    L.swe_last_step_ms.restype = ctypes.c_int
+    _lib = L
+    return L

@@ -1,0 +1,356 @@
+// C ABI of the GB300 shallow-water backend (declared in include/swe_gb300.h).
+//
+// Owns the device state of one grid: U^n, U^(1), U^(2) (h, hu, hv each), the
+// bathymetry, two max-wave-speed slots, the time accumulator, a per-step dt record
+// and an error-flag word, all in one allocation.  Every call runs on the context's
+// own stream and synchronises before returning; no exception crosses the boundary.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/swe_gb300.h"
+#include "swe_launch.h"
+
+using namespace swe;
+
+struct swe_ctx {
+    swe_params p{};
+    cudaStream_t stream = nullptr;
+    int num_sms = 0;
+    long long pitch = 0;       // device row pitch, elements
+    size_t field_elems = 0;    // (Nx + 4) * pitch
+    void *base = nullptr;      // single device allocation
+    void *Un[3]{}, *U1[3]{}, *U2[3]{}, *B = nullptr;
+    unsigned long long *speed = nullptr;  // [2]
+    double *t_accum = nullptr;
+    int *flags = nullptr;
+    double *dt_log = nullptr;
+    int dt_log_cap = 0;
+    int last_steps = 0;
+    long long steps_done = 0;  // selects the speed slot parity
+    bool uploaded = false;
+    double dx = 0, dy = 0, inv_dx = 0, inv_dy = 0, cfl_min_dxdy = 0;
+    long long launches = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // bracket the stage launches of swe_step
+    double last_ms = 0.0;
+    std::string err;
+};
+
+namespace {
+
+int fail(swe_ctx *c, int status, const char *fmt, ...) {
+    if (c) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        c->err = buf;
+    }
+    return status;
+}
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess)                                                                \
+            return fail(c, SWE_ERR_CUDA, "%s failed: %s (%s:%d)", #call,                      \
+                        cudaGetErrorString(e_), __FILE__, __LINE__);                          \
+    } while (0)
+
+size_t elem_size(const swe_ctx *c) {
+    return c->p.precision == SWE_PRECISION_FP64 ? sizeof(double) : sizeof(float);
+}
+
+int set_device(swe_ctx *c) {
+    CK(cudaSetDevice(c->p.device));
+    return SWE_OK;
+}
+
+// Max wave speed of U^n into the slot the next step reads.
+int refresh_speed(swe_ctx *c) {
+    unsigned long long *slot = c->speed + (c->steps_done & 1);
+    CK(cudaMemsetAsync(slot, 0, sizeof(unsigned long long), c->stream));
+    CK(launch_max_speed_f64(c->Un[0], c->Un[1], c->Un[2], c->p.Nx, c->p.Ny, c->pitch, c->p.g,
+                            slot, c->num_sms, c->stream));
+    ++c->launches;
+    return SWE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void swe_params_default(swe_params *p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof *p);
+    p->nG = 2;
+    p->Lx = p->Ly = 1.0;
+    p->g = 9.80665;
+    p->cfl = 0.45;
+    p->bc = SWE_BC_REFLECTING;
+    p->precision = SWE_PRECISION_FP64;
+    p->device = 0;
+}
+
+const char *swe_status_string(int s) {
+    switch (s) {
+        case SWE_OK: return "ok";
+        case SWE_ERR_BAD_ARG: return "bad argument";
+        case SWE_ERR_CUDA: return "CUDA error";
+        case SWE_ERR_NONFINITE: return "non-finite state detected";
+        case SWE_ERR_CFL: return "time step above the CFL limit";
+        case SWE_ERR_TIMEOUT: return "device wait timed out";
+        case SWE_ERR_NO_DEVICE: return "no CUDA device";
+        case SWE_ERR_UNSUPPORTED: return "unsupported option";
+        default: return "unknown status";
+    }
+}
+
+const char *swe_last_error(const swe_ctx *c) { return c ? c->err.c_str() : "null context"; }
+
+long long swe_kernel_launches(const swe_ctx *c) { return c ? c->launches : 0; }
+
+int swe_create(const swe_params *pin, swe_ctx **out) {
+    if (!pin || !out) return SWE_ERR_BAD_ARG;
+    *out = nullptr;
+    swe_params p = *pin;
+    if (p.g <= 0.0) p.g = 9.80665;
+    if (p.nG != 2 || p.Nx < 2 || p.Ny < 2 || !(p.Lx > 0.0) || !(p.Ly > 0.0) ||
+        !(p.cfl > 0.0) || (p.bc != SWE_BC_REFLECTING && p.bc != SWE_BC_TRANSMISSIVE))
+        return SWE_ERR_BAD_ARG;
+    for (int r : p.reserved)
+        if (r != 0) return SWE_ERR_BAD_ARG;
+    // Device indices are int: keep (Nx + 4) * pitch below 2^31 per field.
+    if ((long long)(p.Nx + 4) * (long long)(p.Ny + 36) >= (1ll << 31)) return SWE_ERR_BAD_ARG;
+    if (p.precision != SWE_PRECISION_FP64) return SWE_ERR_UNSUPPORTED;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= p.device || p.device < 0) {
+        cudaGetLastError();
+        return SWE_ERR_NO_DEVICE;
+    }
+    swe_ctx *c = new (std::nothrow) swe_ctx();
+    if (!c) return SWE_ERR_BAD_ARG;
+    c->p = p;
+    int st = set_device(c);
+    if (st != SWE_OK) {
+        delete c;
+        return st;
+    }
+    // HPC_solver.hpp:91-93 and include/core/grid.hpp:19-20; 1.0 / dx as apply_divergence.
+    c->dx = p.Lx / p.Nx;
+    c->dy = p.Ly / p.Ny;
+    c->inv_dx = 1.0 / c->dx;
+    c->inv_dy = 1.0 / c->dy;
+    c->cfl_min_dxdy = p.cfl * std::min(c->dx, c->dy);
+    c->pitch = ((long long)(p.Ny + 4) + 31) / 32 * 32;
+    c->field_elems = (size_t)(p.Nx + 4) * (size_t)c->pitch;
+    const size_t fb = c->field_elems * elem_size(c);
+    const size_t aux = 256;  // speed slots, time, flags
+    auto cleanup = [&](int s) {
+        if (c->base) cudaFree(c->base);
+        if (c->ev0) cudaEventDestroy(c->ev0);
+        if (c->ev1) cudaEventDestroy(c->ev1);
+        if (c->stream) cudaStreamDestroy(c->stream);
+        cudaGetLastError();
+        delete c;
+        return s;
+    };
+    cudaError_t e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, p.device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+    if (e == cudaSuccess) e = cudaMalloc(&c->base, 10 * fb + aux);
+    if (e != cudaSuccess) {
+        const int s = (e == cudaErrorMemoryAllocation) ? SWE_ERR_BAD_ARG : SWE_ERR_CUDA;
+        return cleanup(s);
+    }
+    char *b = static_cast<char *>(c->base);
+    for (int f = 0; f < 3; ++f) {
+        c->Un[f] = b + (0 + f) * fb;
+        c->U1[f] = b + (3 + f) * fb;
+        c->U2[f] = b + (6 + f) * fb;
+    }
+    c->B = b + 9 * fb;
+    char *a = b + 10 * fb;
+    c->speed = reinterpret_cast<unsigned long long *>(a);
+    c->t_accum = reinterpret_cast<double *>(a + 16);
+    c->flags = reinterpret_cast<int *>(a + 24);
+    // Zero everything once so untouched ghosts and padding are defined.
+    e = cudaMemsetAsync(c->base, 0, 10 * fb + aux, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cleanup(SWE_ERR_CUDA);
+    *out = c;
+    return SWE_OK;
+}
+
+void swe_destroy(swe_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->p.device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->dt_log) cudaFree(c->dt_log);
+    if (c->base) cudaFree(c->base);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    cudaGetLastError();
+    delete c;
+}
+
+int swe_upload(swe_ctx *c, const double *h, const double *hu, const double *hv, const double *B) {
+    if (!c || !h || !hu || !hv) return fail(c, SWE_ERR_BAD_ARG, "swe_upload: null argument");
+    if (!c->uploaded && !B) return fail(c, SWE_ERR_BAD_ARG, "swe_upload: first upload needs B");
+    int st = set_device(c);
+    if (st) return st;
+    const size_t row = (size_t)(c->p.Ny + 4) * sizeof(double);
+    const size_t dpitch = (size_t)c->pitch * sizeof(double);
+    const double *src[4] = {h, hu, hv, B};
+    void *dst[4] = {c->Un[0], c->Un[1], c->Un[2], c->B};
+    for (int f = 0; f < 4; ++f) {
+        if (!src[f]) continue;
+        CK(cudaMemcpy2DAsync(dst[f], dpitch, src[f], row, row, (size_t)(c->p.Nx + 4),
+                             cudaMemcpyHostToDevice, c->stream));
+    }
+    c->steps_done = 0;
+    st = refresh_speed(c);
+    if (st) return st;
+    CK(cudaStreamSynchronize(c->stream));
+    c->uploaded = true;
+    return SWE_OK;
+}
+
+int swe_download(swe_ctx *c, double *h, double *hu, double *hv) {
+    if (!c || !h || !hu || !hv) return fail(c, SWE_ERR_BAD_ARG, "swe_download: null argument");
+    if (!c->uploaded) return fail(c, SWE_ERR_BAD_ARG, "swe_download: no state uploaded");
+    int st = set_device(c);
+    if (st) return st;
+    CK(launch_fill_ghosts_f64(c->Un[0], c->Un[1], c->Un[2], c->p.Nx, c->p.Ny, c->pitch, c->p.bc,
+                              c->stream));
+    ++c->launches;
+    const size_t row = (size_t)(c->p.Ny + 4) * sizeof(double);
+    const size_t spitch = (size_t)c->pitch * sizeof(double);
+    double *dst[3] = {h, hu, hv};
+    for (int f = 0; f < 3; ++f)
+        CK(cudaMemcpy2DAsync(dst[f], row, c->Un[f], spitch, row, (size_t)(c->p.Nx + 4),
+                             cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SWE_OK;
+}
+
+int swe_step(swe_ctx *c, int n_steps, double dt, double *t_inout) {
+    if (!c || n_steps < 0) return fail(c, SWE_ERR_BAD_ARG, "swe_step: bad argument");
+    if (!c->uploaded) return fail(c, SWE_ERR_BAD_ARG, "swe_step: no state uploaded");
+    if (!(dt == dt)) return fail(c, SWE_ERR_BAD_ARG, "swe_step: dt is NaN");
+    c->last_steps = 0;
+    if (n_steps == 0) return SWE_OK;
+    int st = set_device(c);
+    if (st) return st;
+    if (c->dt_log_cap < n_steps) {
+        if (c->dt_log) CK(cudaFree(c->dt_log));
+        c->dt_log = nullptr;
+        c->dt_log_cap = 0;
+        const int cap = std::max(n_steps, 1024);
+        CK(cudaMalloc(&c->dt_log, (size_t)cap * sizeof(double)));
+        c->dt_log_cap = cap;
+    }
+    const double t0 = t_inout ? *t_inout : 0.0;
+    CK(cudaMemcpyAsync(c->t_accum, &t0, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemsetAsync(c->flags, 0, sizeof(int), c->stream));
+
+    StageParams sp{};
+    sp.B = c->B;
+    sp.Nx = c->p.Nx;
+    sp.Ny = c->p.Ny;
+    sp.pitch = c->pitch;
+    sp.bc = c->p.bc;
+    sp.inv_dx = c->inv_dx;
+    sp.inv_dy = c->inv_dy;
+    sp.g = c->p.g;
+    sp.cfl_min_dxdy = c->cfl_min_dxdy;
+    sp.dt_fixed = dt > 0.0 ? dt : 0.0;
+    sp.speed = c->speed;
+    sp.t_accum = c->t_accum;
+    sp.dt_log = c->dt_log;
+    sp.flags = c->flags;
+    CK(cudaEventRecord(c->ev0, c->stream));
+    for (int s = 0; s < n_steps; ++s) {
+        sp.slot_read = (int)(c->steps_done & 1);
+        sp.slot_write = sp.slot_read ^ 1;
+        sp.log_index = s;
+        // Stage 1: U1 = Un + dt L(Un)
+        sp.hs = c->Un[0]; sp.hus = c->Un[1]; sp.hvs = c->Un[2];
+        sp.hn = c->Un[0]; sp.hun = c->Un[1]; sp.hvn = c->Un[2];
+        sp.ho = c->U1[0]; sp.huo = c->U1[1]; sp.hvo = c->U1[2];
+        CK(launch_stage_f64(1, sp, c->stream));
+        // Stage 2: U2 = 3/4 Un + 1/4 (U1 + dt L(U1))
+        sp.hs = c->U1[0]; sp.hus = c->U1[1]; sp.hvs = c->U1[2];
+        sp.ho = c->U2[0]; sp.huo = c->U2[1]; sp.hvo = c->U2[2];
+        CK(launch_stage_f64(2, sp, c->stream));
+        // Stage 3: Un = 1/3 Un + 2/3 (U2 + dt L(U2)), in place; max speed -> next slot
+        sp.hs = c->U2[0]; sp.hus = c->U2[1]; sp.hvs = c->U2[2];
+        sp.ho = c->Un[0]; sp.huo = c->Un[1]; sp.hvo = c->Un[2];
+        CK(launch_stage_f64(3, sp, c->stream));
+        c->launches += 3;
+        ++c->steps_done;
+    }
+    CK(cudaEventRecord(c->ev1, c->stream));
+    int flags = 0;
+    double t1 = 0.0;
+    CK(cudaMemcpyAsync(&flags, c->flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&t1, c->t_accum, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    c->last_ms = ms;
+    c->last_steps = n_steps;
+    if (t_inout) *t_inout = t1;
+    if (flags & FLAG_NONFINITE)
+        return fail(c, SWE_ERR_NONFINITE, "non-finite state detected in GB300 solver");
+    return SWE_OK;
+}
+
+int swe_max_wave_speed(swe_ctx *c, double *out) {
+    if (!c || !out) return fail(c, SWE_ERR_BAD_ARG, "swe_max_wave_speed: null argument");
+    if (!c->uploaded) return fail(c, SWE_ERR_BAD_ARG, "swe_max_wave_speed: no state uploaded");
+    int st = set_device(c);
+    if (st) return st;
+    unsigned long long bits = 0;
+    CK(cudaMemcpyAsync(&bits, c->speed + (c->steps_done & 1), sizeof bits,
+                       cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    std::memcpy(out, &bits, sizeof(double));
+    return SWE_OK;
+}
+
+int swe_stable_dt(swe_ctx *c, double *out) {
+    if (!out) return fail(c, SWE_ERR_BAD_ARG, "swe_stable_dt: null argument");
+    double ms = 0.0;
+    int st = swe_max_wave_speed(c, &ms);
+    if (st) return st;
+    *out = (ms <= 1.0e-8) ? 1.0e100 : c->cfl_min_dxdy / ms;  // HPC_kernels.hpp:296-297
+    return SWE_OK;
+}
+
+int swe_last_step_ms(const swe_ctx *c, double *ms) {
+    if (!c || !ms) return SWE_ERR_BAD_ARG;
+    *ms = c->last_ms;
+    return SWE_OK;
+}
+
+int swe_dt_log(swe_ctx *c, double *out, int n, int *written) {
+    if (!c || !out || n < 0) return fail(c, SWE_ERR_BAD_ARG, "swe_dt_log: bad argument");
+    const int m = std::min(n, c->last_steps);
+    if (written) *written = m;
+    if (m == 0) return SWE_OK;
+    CK(cudaMemcpyAsync(out, c->dt_log, (size_t)m * sizeof(double), cudaMemcpyDeviceToHost,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SWE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,358 @@
+// FP64 drop-in kernels: one fused kernel per SSP-RK3 stage.
+//
+// Bitwise parity with the reference's HPC_solver needs every floating-point
+// operation of include/backend/serial/HPC/HPC_kernels.hpp in the same order and
+// rounding: this translation unit is compiled with --fmad=false (no a*b+c fusion,
+// which the reference's x86-64 Release build never does), double division and sqrt
+// are IEEE round-to-nearest, and min/max are written as std::min/std::max.
+//
+// Stage kernel: a CTA owns a TI x TJ tile of interior cells.  It stages the tile plus
+// a 2-cell halo of h, hu, hv, B (and eta = h + B) in shared memory, with the wall
+// boundary condition applied through mirrored indices while loading, computes every
+// x- and y-interface of the tile once, then each thread forms its cell's divergence
+// (apply_divergence), the RK combine, positivity and the store.  Stage 3 also reduces
+// the max wave speed of the new state (compute_stable_dt) into a device slot with a
+// warp shuffle, a block reduction and one atomicMax per CTA.
+#include "swe_common.cuh"
+#include "swe_launch.h"
+
+namespace swe {
+namespace {
+
+constexpr int TI = 8;    // tile rows (x)
+constexpr int TJ = 32;   // tile columns (y, contiguous)
+constexpr int NT = TI * TJ;
+constexpr int RI = TI + 4;  // staged rows incl. halo
+constexpr int RJ = TJ + 4;  // staged columns incl. halo
+
+__device__ __forceinline__ double dmin(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double dmax(double a, double b) { return (a < b) ? b : a; }
+
+// HPC_kernels.hpp:33-35
+__device__ __forceinline__ double positive_height(double h) { return h > 0.0 ? h : 0.0; }
+
+// HPC_kernels.hpp:37-39
+__device__ __forceinline__ double safe_velocity(double q, double h) {
+    return (h > EPS) ? (q / h) : 0.0;
+}
+
+// HPC_kernels.hpp:41-44
+__device__ __forceinline__ double minmod(double a, double b) {
+    if (a * b <= 0.0) return 0.0;
+    return (a > 0.0 ? 1.0 : -1.0) * dmin(fabs(a), fabs(b));
+}
+
+// hll_x (HPC_kernels.hpp:46-82) in normal/tangential form; hll_y (:84-120) is the
+// same with hv normal and hu tangential.
+__device__ __forceinline__ void hll_normal(double g, double hL, double qnL, double qtL,
+                                           double hR, double qnR, double qtR, double &fh,
+                                           double &fqn, double &fqt) {
+    const double unL = safe_velocity(qnL, hL);
+    const double utL = safe_velocity(qtL, hL);
+    const double unR = safe_velocity(qnR, hR);
+    const double utR = safe_velocity(qtR, hR);
+    const double cL = sqrt(g * hL);
+    const double cR = sqrt(g * hR);
+    const double sL = dmin(unL - cL, unR - cR);
+    const double sR = dmax(unL + cL, unR + cR);
+    const double FL_h = qnL;
+    const double FL_n = qnL * unL + 0.5 * g * hL * hL;
+    const double FL_t = qnL * utL;
+    const double FR_h = qnR;
+    const double FR_n = qnR * unR + 0.5 * g * hR * hR;
+    const double FR_t = qnR * utR;
+    if (sL >= 0.0) {
+        fh = FL_h;
+        fqn = FL_n;
+        fqt = FL_t;
+    } else if (sR <= 0.0) {
+        fh = FR_h;
+        fqn = FR_n;
+        fqt = FR_t;
+    } else {
+        const double inv = 1.0 / (sR - sL);
+        fh = (sR * FL_h - sL * FR_h + sL * sR * (hR - hL)) * inv;
+        fqn = (sR * FL_n - sL * FR_n + sL * sR * (qnR - qnL)) * inv;
+        fqt = (sR * FL_t - sL * FR_t + sL * sR * (qtR - qtL)) * inv;
+    }
+}
+
+// One interface between stencil cells m1, c0 (minus side), p1 (plus side), p2, as
+// in compute_x_fluxes (HPC_kernels.hpp:136-184) / compute_y_fluxes (:203-251).
+// qn: normal momentum, qt: tangential.  eta values are h + B of the same cells.
+struct Face {
+    double fh, fqt, fqn_m, fqn_p;
+};
+
+__device__ __forceinline__ Face face_flux(double g, double eta_m1, double eta_0, double eta_p1,
+                                          double eta_p2, double qn_m1, double qn_0,
+                                          double qn_p1, double qn_p2, double qt_m1,
+                                          double qt_0, double qt_p1, double qt_p2,
+                                          double b_minus, double b_plus) {
+    const double eta_minus = eta_0 + 0.5 * minmod(eta_0 - eta_m1, eta_p1 - eta_0);
+    const double eta_plus = eta_p1 - 0.5 * minmod(eta_p1 - eta_0, eta_p2 - eta_p1);
+    const double qn_minus = qn_0 + 0.5 * minmod(qn_0 - qn_m1, qn_p1 - qn_0);
+    const double qt_minus = qt_0 + 0.5 * minmod(qt_0 - qt_m1, qt_p1 - qt_0);
+    const double qn_plus = qn_p1 - 0.5 * minmod(qn_p1 - qn_0, qn_p2 - qn_p1);
+    const double qt_plus = qt_p1 - 0.5 * minmod(qt_p1 - qt_0, qt_p2 - qt_p1);
+    const double b_star = dmax(b_minus, b_plus);
+    const double h_minus = positive_height(eta_minus - b_minus);
+    const double h_plus = positive_height(eta_plus - b_plus);
+    const double un_minus = safe_velocity(qn_minus, h_minus);
+    const double ut_minus = safe_velocity(qt_minus, h_minus);
+    const double un_plus = safe_velocity(qn_plus, h_plus);
+    const double ut_plus = safe_velocity(qt_plus, h_plus);
+    const double hs_minus = positive_height(eta_minus - b_star);
+    const double hs_plus = positive_height(eta_plus - b_star);
+    double f_h, f_n, f_t;
+    hll_normal(g, hs_minus, hs_minus * un_minus, hs_minus * ut_minus, hs_plus,
+               hs_plus * un_plus, hs_plus * ut_plus, f_h, f_n, f_t);
+    const double corr_minus = 0.5 * g * (h_minus * h_minus - hs_minus * hs_minus);
+    const double corr_plus = 0.5 * g * (h_plus * h_plus - hs_plus * hs_plus);
+    Face f;
+    f.fh = f_h;
+    f.fqt = f_t;
+    f.fqn_m = f_n + corr_minus;
+    f.fqn_p = f_n + corr_plus;
+    return f;
+}
+
+// Per-cell wave speed max(|u| + c, |v| + c) (compute_stable_dt body, :288-293).
+__device__ __forceinline__ double cell_speed(double g, double h, double hu, double hv) {
+    const double u = safe_velocity(hu, h);
+    const double v = safe_velocity(hv, h);
+    const double c = sqrt(g * dmax(0.0, h));
+    return dmax(fabs(u) + c, fabs(v) + c);
+}
+
+// Block max of per-thread non-negative speeds, then one atomicMax on the bit pattern
+// (order-preserving for non-negative doubles).
+__device__ __forceinline__ void block_max_to_slot(double v, unsigned long long *slot) {
+    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1) v = dmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        v = lane < nw ? red[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v = dmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0 && v > 0.0) atomicMax(slot, (unsigned long long)__double_as_longlong(v));
+    }
+}
+
+__device__ __forceinline__ double stage_dt(const StageParams &p) {
+    if (p.dt_fixed > 0.0) return p.dt_fixed;
+    const double ms = __longlong_as_double((long long)p.speed[p.slot_read]);
+    if (ms <= EPS) return 1.0e100;  // compute_stable_dt, HPC_kernels.hpp:296
+    return p.cfl_min_dxdy / ms;
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(NT) k_stage_f64(const StageParams p) {
+    __shared__ double s_h[RI][RJ], s_hu[RI][RJ], s_hv[RI][RJ], s_B[RI][RJ], s_eta[RI][RJ];
+    __shared__ double s_xf[4][TI + 1][TJ];  // fh, fhv, fhu_m, fhu_p
+    __shared__ double s_yf[4][TI][TJ + 1];  // gh, ghu, ghv_m, ghv_p
+
+    const int tid = threadIdx.x;
+    const int i0 = blockIdx.y * TI;  // interior coordinates of the tile origin
+    const int j0 = blockIdx.x * TJ;
+    const long long P = p.pitch;
+    const double *hs = static_cast<const double *>(p.hs);
+    const double *hus = static_cast<const double *>(p.hus);
+    const double *hvs = static_cast<const double *>(p.hvs);
+    const double *Bg = static_cast<const double *>(p.B);
+
+    // Stage the tile + halo; ghosts come from the wall boundary condition.
+    for (int t = tid; t < RI * RJ; t += NT) {
+        const int r = t / RJ, c = t - (t / RJ) * RJ;
+        const int ii = i0 - NG + r, jj = j0 - NG + c;
+        bool fx, fy;
+        const int mi = map_coord(ii, p.Nx, p.bc, fx);
+        const int mj = map_coord(jj, p.Ny, p.bc, fy);
+        const long long k = (long long)(mi + NG) * P + (mj + NG);
+        const double hv_ = hvs[k], hu_ = hus[k], h_ = hs[k];
+        // B is read where it lies, ghosts included (clamped in overhanging tiles).
+        const int bi = clamp_int(ii + NG, 0, p.Nx + 2 * NG - 1);
+        const int bj = clamp_int(jj + NG, 0, p.Ny + 2 * NG - 1);
+        const double b_ = Bg[(long long)bi * P + bj];
+        s_h[r][c] = h_;
+        s_hu[r][c] = fx ? -hu_ : hu_;
+        s_hv[r][c] = fy ? -hv_ : hv_;
+        s_B[r][c] = b_;
+        s_eta[r][c] = h_ + b_;
+    }
+    __syncthreads();
+
+    const double g = p.g;
+    // x-faces: between tile rows a = fr + 1 and a + 1, for fr in [0, TI].
+    for (int f = tid; f < (TI + 1) * TJ; f += NT) {
+        const int fr = f / TJ, fc = f - (f / TJ) * TJ;
+        const int a = fr + 1, c = fc + NG;
+        const Face F = face_flux(g, s_eta[a - 1][c], s_eta[a][c], s_eta[a + 1][c],
+                                 s_eta[a + 2][c], s_hu[a - 1][c], s_hu[a][c], s_hu[a + 1][c],
+                                 s_hu[a + 2][c], s_hv[a - 1][c], s_hv[a][c], s_hv[a + 1][c],
+                                 s_hv[a + 2][c], s_B[a][c], s_B[a + 1][c]);
+        s_xf[0][fr][fc] = F.fh;
+        s_xf[1][fr][fc] = F.fqt;
+        s_xf[2][fr][fc] = F.fqn_m;
+        s_xf[3][fr][fc] = F.fqn_p;
+    }
+    // y-faces: between tile columns a = fc + 1 and a + 1, for fc in [0, TJ].
+    for (int f = tid; f < TI * (TJ + 1); f += NT) {
+        const int fr = f / (TJ + 1), fc = f - (f / (TJ + 1)) * (TJ + 1);
+        const int r = fr + NG, a = fc + 1;
+        const Face F = face_flux(g, s_eta[r][a - 1], s_eta[r][a], s_eta[r][a + 1],
+                                 s_eta[r][a + 2], s_hv[r][a - 1], s_hv[r][a], s_hv[r][a + 1],
+                                 s_hv[r][a + 2], s_hu[r][a - 1], s_hu[r][a], s_hu[r][a + 1],
+                                 s_hu[r][a + 2], s_B[r][a], s_B[r][a + 1]);
+        s_yf[0][fr][fc] = F.fh;
+        s_yf[1][fr][fc] = F.fqt;
+        s_yf[2][fr][fc] = F.fqn_m;
+        s_yf[3][fr][fc] = F.fqn_p;
+    }
+    __syncthreads();
+
+    const int ty = tid / TJ, tx = tid - (tid / TJ) * TJ;
+    const int ii = i0 + ty, jj = j0 + tx;
+    const bool inside = (ii < p.Nx) && (jj < p.Ny);
+    const double dt = stage_dt(p);
+    double speed = 0.0;
+    if (inside) {
+        // apply_divergence (HPC_kernels.hpp:274-276): right/top face minus-side
+        // fluxes against left/bottom face plus-side fluxes.
+        const double rh = -p.inv_dx * (s_xf[0][ty + 1][tx] - s_xf[0][ty][tx]) -
+                          p.inv_dy * (s_yf[0][ty][tx + 1] - s_yf[0][ty][tx]);
+        const double rhu = -p.inv_dx * (s_xf[2][ty + 1][tx] - s_xf[3][ty][tx]) -
+                           p.inv_dy * (s_yf[1][ty][tx + 1] - s_yf[1][ty][tx]);
+        const double rhv = -p.inv_dx * (s_xf[1][ty + 1][tx] - s_xf[1][ty][tx]) -
+                           p.inv_dy * (s_yf[2][ty][tx + 1] - s_yf[3][ty][tx]);
+        const long long k = (long long)(ii + NG) * P + (jj + NG);
+        const double sh = s_h[ty + NG][tx + NG];
+        const double shu = s_hu[ty + NG][tx + NG];
+        const double shv = s_hv[ty + NG][tx + NG];
+        double oh, ohu, ohv;
+        if (STAGE == 1) {  // HPC_solver.hpp:246-248
+            oh = sh + dt * rh;
+            ohu = shu + dt * rhu;
+            ohv = shv + dt * rhv;
+        } else {
+            const double nh = static_cast<const double *>(p.hn)[k];
+            const double nhu = static_cast<const double *>(p.hun)[k];
+            const double nhv = static_cast<const double *>(p.hvn)[k];
+            if (STAGE == 2) {  // HPC_solver.hpp:271-273
+                oh = 0.75 * nh + 0.25 * (sh + dt * rh);
+                ohu = 0.75 * nhu + 0.25 * (shu + dt * rhu);
+                ohv = 0.75 * nhv + 0.25 * (shv + dt * rhv);
+            } else {  // HPC_solver.hpp:296-300
+                oh = (1.0 / 3.0) * nh + (2.0 / 3.0) * (sh + dt * rh);
+                ohu = (1.0 / 3.0) * nhu + (2.0 / 3.0) * (shu + dt * rhu);
+                ohv = (1.0 / 3.0) * nhv + (2.0 / 3.0) * (shv + dt * rhv);
+            }
+        }
+        // enforce_positivity (HPC_kernels.hpp:305-312)
+        if (oh < H_FLOOR) {
+            oh = H_FLOOR;
+            ohu = 0.0;
+            ohv = 0.0;
+        }
+        if (!isfinite(oh) || !isfinite(ohu) || !isfinite(ohv)) atomicOr(p.flags, FLAG_NONFINITE);
+        static_cast<double *>(p.ho)[k] = oh;
+        static_cast<double *>(p.huo)[k] = ohu;
+        static_cast<double *>(p.hvo)[k] = ohv;
+        if (STAGE == 3) speed = cell_speed(g, oh, ohu, ohv);
+    }
+    if (STAGE == 1 && blockIdx.x == 0 && blockIdx.y == 0 && tid == 0) {
+        p.speed[p.slot_write] = 0ull;  // read by nobody until stage 3 of this step
+        if (p.dt_log) p.dt_log[p.log_index] = dt;
+    }
+    if (STAGE == 3) {
+        block_max_to_slot(speed, p.speed + p.slot_write);
+        if (blockIdx.x == 0 && blockIdx.y == 0 && tid == 0 && p.t_accum) *p.t_accum += dt;
+    }
+}
+
+// Max wave speed of a state into one slot (used once after an upload).
+__global__ void __launch_bounds__(256) k_max_speed_f64(const double *h, const double *hu,
+                                                       const double *hv, int Nx, int Ny,
+                                                       long long P, double g,
+                                                       unsigned long long *slot) {
+    double v = 0.0;
+    const long long n = (long long)Nx * Ny;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t / Ny), j = (int)(t - (t / Ny) * Ny);
+        const long long k = (long long)(i + NG) * P + (j + NG);
+        v = dmax(v, cell_speed(g, h[k], hu[k], hv[k]));
+    }
+    block_max_to_slot(v, slot);
+}
+
+// Ghost refresh over the perimeter, reproducing apply_reflecting_bc's two sweeps
+// (HPC_solver.hpp:326-370): x-ghost rows take the mirrored row (hu negated), y-ghost
+// columns over all rows take the mirrored column (hv negated), so a corner holds the
+// doubly mirrored interior cell.  Transmissive walls copy the nearest interior cell.
+__global__ void k_fill_ghosts_f64(double *h, double *hu, double *hv, int Nx, int Ny,
+                                  long long P, int bc) {
+    const int NyT = Ny + 2 * NG;
+    const int n_rows = 4 * NyT;  // rows 0, 1, Nx+2, Nx+3, every column
+    const int n_cols = 4 * Nx;   // columns 0, 1, Ny+2, Ny+3 of interior rows
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_rows + n_cols) return;
+    int i, j;
+    if (t < n_rows) {
+        const int r = t / NyT;
+        j = t - r * NyT;
+        i = r < 2 ? r : Nx + r;  // 0, 1, Nx+2, Nx+3
+    } else {
+        const int u = t - n_rows;
+        const int c = u / Nx;
+        i = NG + (u - c * Nx);
+        j = c < 2 ? c : Ny + c;
+    }
+    bool fx, fy;
+    const int si = map_coord(i - NG, Nx, bc, fx) + NG;
+    const int sj = map_coord(j - NG, Ny, bc, fy) + NG;
+    const long long kd = (long long)i * P + j, ks = (long long)si * P + sj;
+    h[kd] = h[ks];
+    hu[kd] = fx ? -hu[ks] : hu[ks];
+    hv[kd] = fy ? -hv[ks] : hv[ks];
+}
+
+}  // namespace
+
+cudaError_t launch_stage_f64(int stage, const StageParams &p, cudaStream_t s) {
+    const dim3 grid((p.Ny + TJ - 1) / TJ, (p.Nx + TI - 1) / TI);
+    switch (stage) {
+        case 1: k_stage_f64<1><<<grid, NT, 0, s>>>(p); break;
+        case 2: k_stage_f64<2><<<grid, NT, 0, s>>>(p); break;
+        default: k_stage_f64<3><<<grid, NT, 0, s>>>(p); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_max_speed_f64(const void *h, const void *hu, const void *hv, int Nx, int Ny,
+                                 long long pitch, double g, unsigned long long *slot,
+                                 int num_sms, cudaStream_t s) {
+    const long long n = (long long)Nx * Ny;
+    long long blocks = (n + 255) / 256;
+    const long long cap = (long long)num_sms * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    k_max_speed_f64<<<(unsigned)blocks, 256, 0, s>>>(
+        static_cast<const double *>(h), static_cast<const double *>(hu),
+        static_cast<const double *>(hv), Nx, Ny, pitch, g, slot);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_ghosts_f64(void *h, void *hu, void *hv, int Nx, int Ny, long long pitch,
+                                   int bc, cudaStream_t s) {
+    const int n = 4 * (Ny + 2 * NG) + 4 * Nx;
+    k_fill_ghosts_f64<<<(n + 255) / 256, 256, 0, s>>>(static_cast<double *>(h),
+                                                       static_cast<double *>(hu),
+                                                       static_cast<double *>(hv), Nx, Ny, pitch,
+                                                       bc);
+    return cudaGetLastError();
+}
+
+}  // namespace swe

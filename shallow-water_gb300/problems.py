@@ -1,0 +1,102 @@
+"""Seeded synthetic inputs for the shallow-water hot path.
+
+The reference builds its inputs from TOML-selected initial conditions and
+bathymetries (include/initial_condition/*.hpp, include/bathymetry/*.hpp).  The
+workloads run here need a few it lacks (seeded multi-Gaussian bathymetry,
+free-surface based dam break / lake at rest), so every input is generated once on
+the host by this module and handed identically to the GPU path and to the CPU
+oracle; RNG or libm differences therefore cannot break parity.
+
+All arrays are full ghosted float64 ``(Nx + 4, Ny + 4)`` grids, row-major with
+i = x (slow) and j = y (contiguous), ghosts included (nG = 2).  Cell centres are
+``x = (i - nG + 0.5) * dx`` (include/core/grid.hpp:22-23), extended through the
+ghost cells.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+NG = 2
+
+
+def centres(N: int, L: float = 1.0) -> np.ndarray:
+    """Cell-centre coordinates of all N + 4 cells along one axis (ghosts included)."""
+    d = L / N
+    return (np.arange(N + 2 * NG, dtype=np.float64) - NG + 0.5) * d
+
+
+def gauss_hump(Nx, Ny, Lx=1.0, Ly=1.0, h0=1.0, amp=0.1, x0=0.5, y0=0.5, two_sigma2=0.01):
+    """h = h0 + amp * exp(-((x-x0)^2 + (y-y0)^2) / two_sigma2), hu = hv = 0, B = 0.
+
+    With the defaults this is the 256^2 parity case: GaussInitial with peak 0.1 and
+    2 sigma^2 = 0.01 (include/initial_condition/gauss_initial.hpp:13-28) over flat
+    bathymetry b0 = 0.
+    """
+    x = centres(Nx, Lx)[:, None]
+    y = centres(Ny, Ly)[None, :]
+    h = h0 + amp * np.exp(-((x - x0) ** 2 + (y - y0) ** 2) / two_sigma2)
+    z = np.zeros_like(h)
+    return np.ascontiguousarray(h), z.copy(), z.copy(), z.copy()
+
+
+def gaussian_sum_bathymetry(Nx, Ny, n=16, seed=0, Lx=1.0, Ly=1.0, width=(0.02, 0.1),
+                            amp=(-0.3, 0.3), rng=None):
+    """B = sum of n Gaussians with centres U[0,Lx]x[0,Ly], widths U[width], amplitudes U[amp].
+
+    Each bump is a * exp(-((x-cx)^2 + (y-cy)^2) / (2 w^2)), evaluated at every cell
+    centre including ghosts.  Separable, so it costs n outer products.
+    Returns (B, params) with params an (n, 4) array of (cx, cy, w, a).
+    """
+    rng = np.random.default_rng(seed) if rng is None else rng
+    cx = rng.uniform(0.0, Lx, n)
+    cy = rng.uniform(0.0, Ly, n)
+    w = rng.uniform(width[0], width[1], n)
+    a = rng.uniform(amp[0], amp[1], n)
+    x = centres(Nx, Lx)
+    y = centres(Ny, Ly)
+    B = np.zeros((Nx + 2 * NG, Ny + 2 * NG), dtype=np.float64)
+    for m in range(n):
+        gx = np.exp(-((x - cx[m]) ** 2) / (2.0 * w[m] ** 2))
+        gy = np.exp(-((y - cy[m]) ** 2) / (2.0 * w[m] ** 2))
+        B += a[m] * np.outer(gx, gy)
+    return B, np.stack([cx, cy, w, a], axis=1)
+
+
+def dam_break(B, Lx=1.0, eta_left=1.5, eta_right=1.0, x_dam=0.4):
+    """Free-surface dam break over B: eta = eta_left for x < x_dam else eta_right,
+    h = max(0, eta - B), hu = hv = 0."""
+    Nx = B.shape[0] - 2 * NG
+    x = centres(Nx, Lx)[:, None]
+    eta = np.where(x < x_dam, eta_left, eta_right)
+    h = np.maximum(0.0, eta - B)
+    z = np.zeros_like(h)
+    return np.ascontiguousarray(h), z.copy(), z.copy()
+
+
+def lake_at_rest(B, eta=1.0):
+    """Still water with a flat free surface: h = max(0, eta - B), hu = hv = 0.
+
+    (The reference's StillWater sets h = h0 instead, still_water.hpp:8-17, which is
+    only at rest over flat bathymetry.)"""
+    h = np.maximum(0.0, eta - B)
+    z = np.zeros_like(h)
+    return np.ascontiguousarray(h), z.copy(), z.copy()
+
+
+def random_state(Nx, Ny, seed=0, h_range=(0.5, 1.5), q_scale=0.3, b_scale=0.2, dry_frac=0.0):
+    """Rough random state for stress tests of every branch of the scheme.
+
+    Optionally sets a fraction of cells nearly dry (h below the 1e-8 floor or
+    exactly 0) so the dry-cell guards and positivity clamps are exercised."""
+    rng = np.random.default_rng(seed)
+    shape = (Nx + 2 * NG, Ny + 2 * NG)
+    h = rng.uniform(h_range[0], h_range[1], shape)
+    hu = rng.normal(0.0, q_scale, shape)
+    hv = rng.normal(0.0, q_scale, shape)
+    B = rng.normal(0.0, b_scale, shape)
+    if dry_frac > 0:
+        m = rng.random(shape) < dry_frac
+        h[m] = rng.choice(np.array([0.0, 1e-9, 5e-9, 2e-8]), size=int(m.sum()))
+        hu[m] *= 1e-8
+        hv[m] *= 1e-8
+    return h, hu, hv, B

@@ -1,0 +1,91 @@
+"""Generates the golden fixtures in this directory by running the reference itself.
+
+Requires oracle/_ref (``make -C oracle ref``, which compiles the reference's own
+HPC_solver / omp_solver from its sources).  Inputs come from
+shallow-water_gb300/problems.py; they are stored in the fixtures (small cases) or
+pinned by their SHA-256 (the full 256^2 parity case), so the fixtures do not depend
+on the platform's exp().
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import importlib
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+P = importlib.import_module("shallow-water_gb300.problems")
+from oracle import ref  # noqa: E402
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.float64).tobytes()).hexdigest()
+
+
+def case_config0(variant):
+    """256^2 Gaussian hump over flat B = 0, reflecting walls, CFL 0.45 fixed dt, 1000 steps."""
+    N = 256
+    h, hu, hv, B = P.gauss_hump(N, N)
+    dt = ref.stable_dt(N, N, h, hu, hv, cfl=0.45, variant=variant)
+    o = ref.run(N, N, h, hu, hv, B, 1000, dt_fixed=dt, cfl=0.45, bc=0, variant=variant)
+    assert o[5] == 0
+    return {
+        "N": N, "steps": 1000, "dt": dt, "g": ref.gravity(variant), "bc": 0, "cfl": 0.45,
+        "input_sha256": {"h": sha(h), "hu": sha(hu), "hv": sha(hv), "B": sha(B)},
+        "output_sha256": {"h": sha(o[0]), "hu": sha(o[1]), "hv": sha(o[2])},
+        "output_stats": {k: [float(a.sum()), float(np.abs(a).max())]
+                         for k, a in zip(("h", "hu", "hv"), o[:3])},
+        "t_end": o[4],
+    }
+
+
+def small_cases():
+    cases = {}
+    # rough random state with dry / sub-floor cells, reflecting walls, adaptive dt
+    h, hu, hv, B = P.random_state(40, 24, seed=7, dry_frac=0.08)
+    cases["random_dry_40x24"] = dict(Nx=40, Ny=24, Lx=1.0, Ly=0.75, cfl=0.3, bc=0, steps=30,
+                                     dt_fixed=0.0, h=h, hu=hu, hv=hv, B=B)
+    # dam break over seeded Gaussian bathymetry, transmissive walls, adaptive dt
+    B, _ = P.gaussian_sum_bathymetry(48, 40, n=16, seed=3)
+    h, hu, hv = P.dam_break(B)
+    cases["dambreak_trans_48x40"] = dict(Nx=48, Ny=40, Lx=1.0, Ly=1.0, cfl=0.45, bc=1, steps=40,
+                                         dt_fixed=0.0, h=h, hu=hu, hv=hv, B=B)
+    # lake at rest over emerged + submerged bumps, reflecting walls, fixed dt
+    B, _ = P.gaussian_sum_bathymetry(32, 32, n=6, seed=11, amp=(-0.4, 1.3))
+    h, hu, hv = P.lake_at_rest(B, 1.0)
+    cases["lake_island_32"] = dict(Nx=32, Ny=32, Lx=1.0, Ly=1.0, cfl=0.45, bc=0, steps=60,
+                                   dt_fixed=2.0e-3, h=h, hu=hu, hv=hv, B=B)
+    # odd sizes, fixed dt
+    h, hu, hv, B = P.random_state(17, 33, seed=5, q_scale=0.1, b_scale=0.05)
+    cases["odd_17x33"] = dict(Nx=17, Ny=33, Lx=0.5, Ly=1.0, cfl=0.45, bc=0, steps=25,
+                              dt_fixed=5.0e-4, h=h, hu=hu, hv=hv, B=B)
+    out = {}
+    for name, c in cases.items():
+        o = ref.run(c["Nx"], c["Ny"], c["h"], c["hu"], c["hv"], c["B"], c["steps"],
+                    dt_fixed=c["dt_fixed"], Lx=c["Lx"], Ly=c["Ly"], cfl=c["cfl"], bc=c["bc"])
+        assert o[5] == 0, name
+        out[name] = dict(c, h_out=o[0], hu_out=o[1], hv_out=o[2], dts=o[3], t_end=o[4])
+    return out
+
+
+def main():
+    assert ref.available() and ref.available("g981"), "build oracle/_ref first: make -C oracle ref"
+    meta = {"config0_g980665": case_config0("g980665"), "config0_g981": case_config0("g981")}
+    with open(os.path.join(HERE, "config0_256.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    for name, c in small_cases().items():
+        arrays = {k: v for k, v in c.items() if isinstance(v, np.ndarray)}
+        scalars = {k: v for k, v in c.items() if not isinstance(v, np.ndarray)}
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(scalars), **arrays)
+    print("wrote", sorted(os.listdir(HERE)))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,148 @@
+"""FP64 drop-in on the GPU, through the C ABI, against the CPU oracle: bitwise equal
+fields, dt sequences and times (max relative error 0 <= 1e-12)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import bitwise_equal, max_rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def run_both(sw, port, h, hu, hv, B, Nx, Ny, steps, dt=0.0, Lx=1.0, Ly=1.0, cfl=0.45, bc=0,
+             g=9.80665, chunks=1):
+    p = port.grid(Nx, Ny, Lx, Ly, g=g, cfl=cfl, bc=bc)
+    ref = port.run(p, h, hu, hv, B, steps, dt)
+    with sw.Solver(Nx, Ny, Lx, Ly, g=g, cfl=cfl, bc=bc) as s:
+        s.upload(h, hu, hv, B)
+        dts = []
+        per = steps // chunks
+        for c in range(chunks):
+            n = per if c < chunks - 1 else steps - per * (chunks - 1)
+            s.step(n, dt if dt > 0 else None)
+            dts.append(s.dt_log(n))
+        out = s.download()
+        return ref, out, np.concatenate(dts), s.time, s
+
+
+def assert_bitwise(ref, out, dts, t):
+    assert ref[5] == 0
+    for k, name in enumerate(("h", "hu", "hv")):
+        err = max_rel_err(out[k], ref[k])
+        assert err <= 1e-12, (name, err)
+        assert bitwise_equal(out[k], ref[k]), (name, err)
+    assert bitwise_equal(dts, ref[3])
+    assert t == ref[4]
+
+
+@pytest.mark.parametrize("g", [9.80665, 9.81])
+def test_config0_small_gauss_hump(gpu_lib, sw, port, problems, g):
+    h, hu, hv, B = problems.gauss_hump(64, 64)
+    p = port.grid(64, 64, g=g)
+    dt = port.stable_dt(p, h, hu, hv)
+    ref, out, dts, t, _ = run_both(sw, port, h, hu, hv, B, 64, 64, 200, dt=dt, g=g)
+    assert_bitwise(ref, out, dts, t)
+
+
+def test_config0_full_256_1000_steps(gpu_lib, sw, port, problems):
+    """The 256^2, 1000-step parity case (CFL 0.45 fixed dt)."""
+    h, hu, hv, B = problems.gauss_hump(256, 256)
+    dt = port.stable_dt(port.grid(256, 256), h, hu, hv)
+    ref, out, dts, t, _ = run_both(sw, port, h, hu, hv, B, 256, 256, 1000, dt=dt, chunks=4)
+    assert_bitwise(ref, out, dts, t)
+
+
+@pytest.mark.parametrize("bc", [0, 1], ids=["reflecting", "transmissive"])
+@pytest.mark.parametrize("shape", [(37, 29), (2, 2), (3, 130), (130, 3), (64, 96)])
+def test_random_states_adaptive(gpu_lib, sw, port, problems, bc, shape):
+    Nx, Ny = shape
+    h, hu, hv, B = problems.random_state(Nx, Ny, seed=Nx * 1000 + Ny, q_scale=0.1, b_scale=0.05)
+    ref, out, dts, t, _ = run_both(sw, port, h, hu, hv, B, Nx, Ny, 15, cfl=0.3, bc=bc,
+                                   Lx=1.0, Ly=1.7)
+    assert_bitwise(ref, out, dts, t)
+
+
+def test_dry_cells_and_positivity(gpu_lib, sw, port, problems):
+    h, hu, hv, B = problems.random_state(48, 40, seed=9, q_scale=0.1, b_scale=0.05, dry_frac=0.1)
+    ref, out, dts, t, _ = run_both(sw, port, h, hu, hv, B, 48, 40, 20, cfl=0.2)
+    assert_bitwise(ref, out, dts, t)
+
+
+def test_dambreak_transmissive(gpu_lib, sw, port, problems):
+    B, _ = problems.gaussian_sum_bathymetry(200, 136, n=16, seed=2)
+    h, hu, hv = problems.dam_break(B)
+    ref, out, dts, t, _ = run_both(sw, port, h, hu, hv, B, 200, 136, 60, bc=1, chunks=3)
+    assert_bitwise(ref, out, dts, t)
+
+
+def test_lake_at_rest_all_wet_is_exact(gpu_lib, sw, port, problems):
+    """Submerged bumps, eta = 1: momentum stays exactly zero (reference behaviour)."""
+    B, _ = problems.gaussian_sum_bathymetry(96, 96, n=8, seed=4, amp=(-0.3, 0.5))
+    h, hu, hv = problems.lake_at_rest(B, 1.0)
+    assert h[2:-2, 2:-2].min() > 0.1
+    ref, out, dts, t, _ = run_both(sw, port, h, hu, hv, B, 96, 96, 100, dt=1e-3)
+    assert_bitwise(ref, out, dts, t)
+    assert np.abs(out[1]).max() == 0.0 and np.abs(out[2]).max() == 0.0
+
+
+def test_golden_fixtures_on_gpu(gpu_lib, sw):
+    from test_golden import SMALL, load_case
+    for name in SMALL:
+        meta, a = load_case(name)
+        with sw.Solver(meta["Nx"], meta["Ny"], meta["Lx"], meta["Ly"], cfl=meta["cfl"],
+                       bc=meta["bc"]) as s:
+            s.upload(a["h"], a["hu"], a["hv"], a["B"])
+            s.step(meta["steps"], meta["dt_fixed"] or None)
+            out = s.download()
+            assert bitwise_equal(out[0], a["h_out"]), name
+            assert bitwise_equal(out[1], a["hu_out"]), name
+            assert bitwise_equal(out[2], a["hv_out"]), name
+            assert bitwise_equal(s.dt_log(meta["steps"]), a["dts"]), name
+            assert s.time == meta["t_end"], name
+
+
+def test_stable_dt_and_speed(gpu_lib, sw, port, problems):
+    h, hu, hv, B = problems.random_state(50, 70, seed=1)
+    p = port.grid(50, 70, 2.0, 1.0)
+    with sw.Solver(50, 70, 2.0, 1.0) as s:
+        s.upload(h, hu, hv, B)
+        assert s.max_wave_speed() == port.max_wave_speed(p, h, hu, hv)
+        assert s.stable_dt() == port.stable_dt(p, h, hu, hv)
+
+
+def test_nonfinite_reports_status(gpu_lib, sw, problems):
+    h, hu, hv, B = problems.random_state(16, 16, seed=1)
+    h[8, 8] = np.nan
+    with sw.Solver(16, 16) as s:
+        s.upload(h, hu, hv, B)
+        with pytest.raises(sw.SweError) as e:
+            s.step(1, 1e-4)
+        assert e.value.status == 3
+        # the context stays usable after the error
+        h2, hu2, hv2, B2 = problems.random_state(16, 16, seed=2)
+        s.upload(h2, hu2, hv2, B2)
+        s.step(2, None)
+
+
+def test_cfl_guard_in_run(gpu_lib, sw, problems):
+    h, hu, hv, B = problems.gauss_hump(32, 32)
+    with sw.Solver(32, 32) as s:
+        s.upload(h, hu, hv, B)
+        with pytest.raises(sw.SweError) as e:
+            s.run(end_time=1.0, time_steps=10)
+        assert e.value.status == 4 and "Time step too large" in str(e.value)
+
+
+def test_run_snapshots_match_oracle(gpu_lib, sw, port, problems):
+    h, hu, hv, B = problems.gauss_hump(40, 40)
+    p = port.grid(40, 40)
+    dt = port.stable_dt(p, h, hu, hv)
+    snaps = []
+    with sw.Solver(40, 40) as s:
+        s.upload(h, hu, hv, B)
+        s.run(end_time=dt * 30, time_steps=30, save_every=10,
+              on_snapshot=lambda n, t, a, b, c: snaps.append((n, a.copy())))
+    assert [n for n, _ in snaps] == [0, 10, 20, 30]
+    ref = port.run(p, h, hu, hv, B, 30, (dt * 30) / 30.0)
+    assert bitwise_equal(snaps[-1][1], ref[0])
