@@ -87,7 +87,7 @@ class Dist:
 
 def workload(n: int, seed: int):
     P = importlib.import_module("shallow-water_gb300.problems")
-    B, _ = P.gaussian_sum_bathymetry(n, n, n=16, seed=seed)
+    B, _ = P.gaussian_sum_bathymetry(n, n, n=16, seed=seed, bc="transmissive")
     h, hu, hv = P.dam_break(B)
     return h, hu, hv, B
 

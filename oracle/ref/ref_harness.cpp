@@ -27,19 +27,7 @@
 #undef private
 
 // ---- no-op I/O: the harness never writes NetCDF -------------------------------------
-NetCDFWriter::NetCDFWriter(const std::string &, const Grid &grid, const std::string &,
-                           const std::string &, const std::string &, const std::string &, int)
-    : grid_(grid), nx_(0), ny_(0) {}
-void NetCDFWriter::write_snapshot(const State &, double, double, const std::string &,
-                                  const std::string &, const std::string &, const std::string &,
-                                  const std::string &, const std::string &) {}
-void NetCDFWriter::write_bathymetry(const Array2D &) {}
-SanityCheckNetCDFWriter::SanityCheckNetCDFWriter(const std::string &, const std::string &,
-                                                 const std::string &, int, double,
-                                                 const std::string &, const std::string &,
-                                                 const std::string &, const std::string &,
-                                                 const std::string &, const std::string &) {}
-void SanityCheckNetCDFWriter::write(std::size_t, double, double, double) {}
+#include "netcdf_noop.cpp"
 
 namespace {
 

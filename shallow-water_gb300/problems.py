@@ -39,12 +39,36 @@ def gauss_hump(Nx, Ny, Lx=1.0, Ly=1.0, h0=1.0, amp=0.1, x0=0.5, y0=0.5, two_sigm
     return np.ascontiguousarray(h), z.copy(), z.copy(), z.copy()
 
 
+def fill_scalar_ghosts(a: np.ndarray, bc: str = "reflecting") -> np.ndarray:
+    """Fills the ghost cells of a ghosted scalar field in place from the interior, as the
+    reference does for the bathymetry after apply_bathymetry
+    (apply_scalar_reflecting_bc, HPC_solver.hpp:373-404: mirrored rows for interior
+    columns, then mirrored columns over all rows).  ``"transmissive"`` copies the
+    nearest interior row / column instead (zero gradient)."""
+    Nx, Ny = a.shape[0] - 2 * NG, a.shape[1] - 2 * NG
+    refl = bc == "reflecting"
+    for g in range(NG):
+        src_lo = NG + g if refl else NG
+        src_hi = NG + Nx - 1 - g if refl else NG + Nx - 1
+        a[NG - 1 - g, NG:NG + Ny] = a[src_lo, NG:NG + Ny]
+        a[NG + Nx + g, NG:NG + Ny] = a[src_hi, NG:NG + Ny]
+    for g in range(NG):
+        src_lo = NG + g if refl else NG
+        src_hi = NG + Ny - 1 - g if refl else NG + Ny - 1
+        a[:, NG - 1 - g] = a[:, src_lo]
+        a[:, NG + Ny + g] = a[:, src_hi]
+    return a
+
+
 def gaussian_sum_bathymetry(Nx, Ny, n=16, seed=0, Lx=1.0, Ly=1.0, width=(0.02, 0.1),
-                            amp=(-0.3, 0.3), rng=None):
+                            amp=(-0.3, 0.3), rng=None, bc="reflecting"):
     """B = sum of n Gaussians with centres U[0,Lx]x[0,Ly], widths U[width], amplitudes U[amp].
 
-    Each bump is a * exp(-((x-cx)^2 + (y-cy)^2) / (2 w^2)), evaluated at every cell
-    centre including ghosts.  Separable, so it costs n outer products.
+    Each bump is a * exp(-((x-cx)^2 + (y-cy)^2) / (2 w^2)), evaluated at the interior
+    cell centres; the ghosts are then filled for the wall type ``bc`` by
+    :func:`fill_scalar_ghosts`, as the reference does for its GaussHill bathymetry
+    (gaussian_hill.hpp:16-30 then HPC_solver.hpp:114), so a flat free surface is at rest
+    up to the walls.  Separable, so it costs n outer products.
     Returns (B, params) with params an (n, 4) array of (cx, cy, w, a).
     """
     rng = np.random.default_rng(seed) if rng is None else rng
@@ -59,6 +83,7 @@ def gaussian_sum_bathymetry(Nx, Ny, n=16, seed=0, Lx=1.0, Ly=1.0, width=(0.02, 0
         gx = np.exp(-((x - cx[m]) ** 2) / (2.0 * w[m] ** 2))
         gy = np.exp(-((y - cy[m]) ** 2) / (2.0 * w[m] ** 2))
         B += a[m] * np.outer(gx, gy)
+    fill_scalar_ghosts(B, bc)
     return B, np.stack([cx, cy, w, a], axis=1)
 
 

@@ -53,7 +53,7 @@ def small_cases():
     cases["random_dry_40x24"] = dict(Nx=40, Ny=24, Lx=1.0, Ly=0.75, cfl=0.3, bc=0, steps=30,
                                      dt_fixed=0.0, h=h, hu=hu, hv=hv, B=B)
     # dam break over seeded Gaussian bathymetry, transmissive walls, adaptive dt
-    B, _ = P.gaussian_sum_bathymetry(48, 40, n=16, seed=3)
+    B, _ = P.gaussian_sum_bathymetry(48, 40, n=16, seed=3, bc="transmissive")
     h, hu, hv = P.dam_break(B)
     cases["dambreak_trans_48x40"] = dict(Nx=48, Ny=40, Lx=1.0, Ly=1.0, cfl=0.45, bc=1, steps=40,
                                          dt_fixed=0.0, h=h, hu=hu, hv=hv, B=B)

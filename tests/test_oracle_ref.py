@@ -30,7 +30,7 @@ def _inputs(problems, gen, Nx, Ny, seed):
         return problems.random_state(Nx, Ny, seed=seed, q_scale=0.1, b_scale=0.05)
     if gen == "dry":
         return problems.random_state(Nx, Ny, seed=seed, q_scale=0.1, b_scale=0.05, dry_frac=0.1)
-    B, _ = problems.gaussian_sum_bathymetry(Nx, Ny, n=16, seed=seed)
+    B, _ = problems.gaussian_sum_bathymetry(Nx, Ny, n=16, seed=seed, bc="transmissive")
     h, hu, hv = problems.dam_break(B)
     return h, hu, hv, B
 
@@ -77,3 +77,17 @@ def test_nonfinite_status_matches(port, problems):
     p = port.grid(16, 16)
     assert port.run(p, h, hu, hv, B, 1, 1e-4)[5] == 1
     assert ref.run(16, 16, h, hu, hv, B, 1, 1e-4)[5] == 1
+
+
+@pytest.mark.parametrize("bc", [0, 1], ids=["reflecting", "transmissive"])
+def test_lake_at_rest_exact_in_reference_and_port(port, problems, bc):
+    """All-wet lake over bumps with wall-consistent bathymetry ghosts: the reference keeps
+    hu, hv at rounding level (eta = h + B is 1 only to rounding), and so does the port."""
+    B, _ = problems.gaussian_sum_bathymetry(48, 40, n=8, seed=4, amp=(-0.3, 0.5),
+                                            bc="reflecting" if bc == 0 else "transmissive")
+    h, hu, hv = problems.lake_at_rest(B, 1.0)
+    a = port.run(port.grid(48, 40, bc=bc), h, hu, hv, B, 50, 1e-3)
+    b = ref.run(48, 40, h, hu, hv, B, 50, 1e-3, bc=bc)
+    for k in range(3):
+        assert bitwise_equal(a[k], b[k])
+    assert np.abs(b[1]).max() < 1e-13 and np.abs(b[2]).max() < 1e-13

@@ -70,20 +70,22 @@ def test_dry_cells_and_positivity(gpu_lib, sw, port, problems):
 
 
 def test_dambreak_transmissive(gpu_lib, sw, port, problems):
-    B, _ = problems.gaussian_sum_bathymetry(200, 136, n=16, seed=2)
+    B, _ = problems.gaussian_sum_bathymetry(200, 136, n=16, seed=2, bc="transmissive")
     h, hu, hv = problems.dam_break(B)
     ref, out, dts, t, _ = run_both(sw, port, h, hu, hv, B, 200, 136, 60, bc=1, chunks=3)
     assert_bitwise(ref, out, dts, t)
 
 
-def test_lake_at_rest_all_wet_is_exact(gpu_lib, sw, port, problems):
-    """Submerged bumps, eta = 1: momentum stays exactly zero (reference behaviour)."""
-    B, _ = problems.gaussian_sum_bathymetry(96, 96, n=8, seed=4, amp=(-0.3, 0.5))
+@pytest.mark.parametrize("bc", ["reflecting", "transmissive"])
+def test_lake_at_rest_all_wet_is_exact(gpu_lib, sw, port, problems, bc):
+    """Submerged bumps, eta = 1: momentum stays at rounding level (reference behaviour)."""
+    B, _ = problems.gaussian_sum_bathymetry(96, 96, n=8, seed=4, amp=(-0.3, 0.5), bc=bc)
     h, hu, hv = problems.lake_at_rest(B, 1.0)
     assert h[2:-2, 2:-2].min() > 0.1
-    ref, out, dts, t, _ = run_both(sw, port, h, hu, hv, B, 96, 96, 100, dt=1e-3)
+    ref, out, dts, t, _ = run_both(sw, port, h, hu, hv, B, 96, 96, 100, dt=1e-3,
+                                   bc=0 if bc == "reflecting" else 1)
     assert_bitwise(ref, out, dts, t)
-    assert np.abs(out[1]).max() == 0.0 and np.abs(out[2]).max() == 0.0
+    assert np.abs(out[1]).max() < 1e-13 and np.abs(out[2]).max() < 1e-13
 
 
 def test_golden_fixtures_on_gpu(gpu_lib, sw):
