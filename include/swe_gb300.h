@@ -107,6 +107,12 @@ int swe_max_wave_speed(swe_ctx *ctx, double *out);
  * this value compared with the fixed dt. */
 int swe_stable_dt(swe_ctx *ctx, double *out);
 
+/* Totals of the current state over the interior, times dx * dy: mass = sum h,
+ * momentum_x = sum hu, momentum_y = sum hv.  Compensated FP64 summation, deterministic.
+ * The reference sums h * dx * dy naively on the host for its MassConservation check
+ * (tests/sanity_checks/mass_conservation.hpp:45-56); this is the device-side twin. */
+int swe_totals(swe_ctx *ctx, double *mass, double *momentum_x, double *momentum_y);
+
 /* Copies the dt of each step of the last swe_step call (up to n values) to out and
  * returns how many were written in *written. */
 int swe_dt_log(swe_ctx *ctx, double *out, int n, int *written);

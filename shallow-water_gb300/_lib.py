@@ -29,7 +29,7 @@ SWE_PRECISION_FP32_MIXED = 1
 EXPORTS = (
     "swe_params_default", "swe_create", "swe_destroy", "swe_upload", "swe_download",
     "swe_step", "swe_max_wave_speed", "swe_stable_dt", "swe_dt_log", "swe_last_error",
-    "swe_status_string", "swe_kernel_launches", "swe_last_step_ms",
+    "swe_status_string", "swe_kernel_launches", "swe_last_step_ms", "swe_totals",
 )
 
 
@@ -88,6 +88,8 @@ def lib(path: str = LIB_PATH):
     L.swe_status_string.restype = ctypes.c_char_p
     L.swe_kernel_launches.argtypes = [vp]
     L.swe_kernel_launches.restype = ctypes.c_longlong
+    L.swe_totals.argtypes = [vp, dp, dp, dp]
+    L.swe_totals.restype = ctypes.c_int
     L.swe_last_step_ms.argtypes = [vp, dp]
     L.swe_last_step_ms.restype = ctypes.c_int
     _lib = L

@@ -21,6 +21,8 @@ COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-
 # source -> extra flags
 UNITS = {
     "swe_fp64.cu": ["--fmad=false"],
+    "swe_fp32.cu": [],
+    "swe_reduce.cu": [],
     "swe_api.cu": [],
 }
 

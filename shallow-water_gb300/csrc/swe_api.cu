@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -26,6 +27,8 @@ struct swe_ctx {
     size_t field_elems = 0;    // (Nx + 4) * pitch
     void *base = nullptr;      // single device allocation
     void *Un[3]{}, *U1[3]{}, *U2[3]{}, *B = nullptr;
+    void *stage64[2]{};        // FP32 form: FP64 staging (B as given, scratch) in device layout
+    double *partial = nullptr; // totals: per-block compensated pairs, then the 3 results
     unsigned long long *speed = nullptr;  // [2]
     double *t_accum = nullptr;
     int *flags = nullptr;
@@ -72,14 +75,33 @@ int set_device(swe_ctx *c) {
     return SWE_OK;
 }
 
+// k with x == 2^k when x is a normal power of two with |k| <= 64, else 127.
+int pow2_exponent(double x) {
+    int k = 0;
+    const double m = std::frexp(x, &k);  // x = m * 2^k, m in [0.5, 1)
+    if (m != 0.5 || !(x > 0.0) || k - 1 < -64 || k - 1 > 64) return 127;
+    return k - 1;
+}
+
+bool fp32(const swe_ctx *c) { return c->p.precision == SWE_PRECISION_FP32_MIXED; }
+
 // Max wave speed of U^n into the slot the next step reads.
 int refresh_speed(swe_ctx *c) {
     unsigned long long *slot = c->speed + (c->steps_done & 1);
     CK(cudaMemsetAsync(slot, 0, sizeof(unsigned long long), c->stream));
-    CK(launch_max_speed_f64(c->Un[0], c->Un[1], c->Un[2], c->p.Nx, c->p.Ny, c->pitch, c->p.g,
-                            slot, c->num_sms, c->stream));
+    if (fp32(c)) {
+        CK(launch_max_speed_f32(c->Un[0], c->Un[1], c->Un[2], c->B, c->p.Nx, c->p.Ny, c->pitch,
+                                c->p.g, slot, c->num_sms, c->stream));
+    } else {
+        CK(launch_max_speed_f64(c->Un[0], c->Un[1], c->Un[2], c->p.Nx, c->p.Ny, c->pitch,
+                                c->p.g, slot, c->num_sms, c->stream));
+    }
     ++c->launches;
     return SWE_OK;
+}
+
+cudaError_t launch_stage(swe_ctx *c, int stage, const StageParams &sp) {
+    return fp32(c) ? launch_stage_f32(stage, sp, c->stream) : launch_stage_f64(stage, sp, c->stream);
 }
 
 }  // namespace
@@ -128,7 +150,8 @@ int swe_create(const swe_params *pin, swe_ctx **out) {
         if (r != 0) return SWE_ERR_BAD_ARG;
     // Device indices are int: keep (Nx + 4) * pitch below 2^31 per field.
     if ((long long)(p.Nx + 4) * (long long)(p.Ny + 36) >= (1ll << 31)) return SWE_ERR_BAD_ARG;
-    if (p.precision != SWE_PRECISION_FP64) return SWE_ERR_UNSUPPORTED;
+    if (p.precision != SWE_PRECISION_FP64 && p.precision != SWE_PRECISION_FP32_MIXED)
+        return SWE_ERR_UNSUPPORTED;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= p.device || p.device < 0) {
         cudaGetLastError();
@@ -152,6 +175,8 @@ int swe_create(const swe_params *pin, swe_ctx **out) {
     c->field_elems = (size_t)(p.Nx + 4) * (size_t)c->pitch;
     const size_t fb = c->field_elems * elem_size(c);
     const size_t aux = 256;  // speed slots, time, flags
+    const size_t staging = (p.precision == SWE_PRECISION_FP32_MIXED)
+                               ? 2 * c->field_elems * sizeof(double) : 0;
     auto cleanup = [&](int s) {
         if (c->base) cudaFree(c->base);
         if (c->ev0) cudaEventDestroy(c->ev0);
@@ -165,7 +190,7 @@ int swe_create(const swe_params *pin, swe_ctx **out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
-    if (e == cudaSuccess) e = cudaMalloc(&c->base, 10 * fb + aux);
+    if (e == cudaSuccess) e = cudaMalloc(&c->base, 10 * fb + aux + staging);
     if (e != cudaSuccess) {
         const int s = (e == cudaErrorMemoryAllocation) ? SWE_ERR_BAD_ARG : SWE_ERR_CUDA;
         return cleanup(s);
@@ -181,8 +206,12 @@ int swe_create(const swe_params *pin, swe_ctx **out) {
     c->speed = reinterpret_cast<unsigned long long *>(a);
     c->t_accum = reinterpret_cast<double *>(a + 16);
     c->flags = reinterpret_cast<int *>(a + 24);
+    if (staging) {
+        c->stage64[0] = a + aux;
+        c->stage64[1] = a + aux + c->field_elems * sizeof(double);
+    }
     // Zero everything once so untouched ghosts and padding are defined.
-    e = cudaMemsetAsync(c->base, 0, 10 * fb + aux, c->stream);
+    e = cudaMemsetAsync(c->base, 0, 10 * fb + aux + staging, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cleanup(SWE_ERR_CUDA);
     *out = c;
@@ -194,6 +223,7 @@ void swe_destroy(swe_ctx *c) {
     cudaSetDevice(c->p.device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->dt_log) cudaFree(c->dt_log);
+    if (c->partial) cudaFree(c->partial);
     if (c->base) cudaFree(c->base);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -209,12 +239,33 @@ int swe_upload(swe_ctx *c, const double *h, const double *hu, const double *hv, 
     if (st) return st;
     const size_t row = (size_t)(c->p.Ny + 4) * sizeof(double);
     const size_t dpitch = (size_t)c->pitch * sizeof(double);
-    const double *src[4] = {h, hu, hv, B};
-    void *dst[4] = {c->Un[0], c->Un[1], c->Un[2], c->B};
-    for (int f = 0; f < 4; ++f) {
-        if (!src[f]) continue;
-        CK(cudaMemcpy2DAsync(dst[f], dpitch, src[f], row, row, (size_t)(c->p.Nx + 4),
-                             cudaMemcpyHostToDevice, c->stream));
+    const size_t rows = (size_t)(c->p.Nx + 4);
+    if (fp32(c)) {
+        // B as given stays in stage64[0]; eta = RN32(h + B), the rest rounded to FP32.
+        const int R = c->p.Nx + 4, C = c->p.Ny + 4;
+        if (B) {
+            CK(cudaMemcpy2DAsync(c->stage64[0], dpitch, B, row, row, rows,
+                                 cudaMemcpyHostToDevice, c->stream));
+            CK(launch_f64_to_f32(c->stage64[0], nullptr, c->B, R, C, c->pitch, c->num_sms,
+                                 c->stream));
+            ++c->launches;
+        }
+        const double *src[3] = {h, hu, hv};
+        for (int f = 0; f < 3; ++f) {
+            CK(cudaMemcpy2DAsync(c->stage64[1], dpitch, src[f], row, row, rows,
+                                 cudaMemcpyHostToDevice, c->stream));
+            CK(launch_f64_to_f32(c->stage64[1], f == 0 ? c->stage64[0] : nullptr, c->Un[f], R,
+                                 C, c->pitch, c->num_sms, c->stream));
+            ++c->launches;
+        }
+    } else {
+        const double *src[4] = {h, hu, hv, B};
+        void *dst[4] = {c->Un[0], c->Un[1], c->Un[2], c->B};
+        for (int f = 0; f < 4; ++f) {
+            if (!src[f]) continue;
+            CK(cudaMemcpy2DAsync(dst[f], dpitch, src[f], row, row, rows,
+                                 cudaMemcpyHostToDevice, c->stream));
+        }
     }
     c->steps_done = 0;
     st = refresh_speed(c);
@@ -229,15 +280,30 @@ int swe_download(swe_ctx *c, double *h, double *hu, double *hv) {
     if (!c->uploaded) return fail(c, SWE_ERR_BAD_ARG, "swe_download: no state uploaded");
     int st = set_device(c);
     if (st) return st;
-    CK(launch_fill_ghosts_f64(c->Un[0], c->Un[1], c->Un[2], c->p.Nx, c->p.Ny, c->pitch, c->p.bc,
-                              c->stream));
-    ++c->launches;
     const size_t row = (size_t)(c->p.Ny + 4) * sizeof(double);
     const size_t spitch = (size_t)c->pitch * sizeof(double);
     double *dst[3] = {h, hu, hv};
-    for (int f = 0; f < 3; ++f)
-        CK(cudaMemcpy2DAsync(dst[f], row, c->Un[f], spitch, row, (size_t)(c->p.Nx + 4),
-                             cudaMemcpyDeviceToHost, c->stream));
+    if (fp32(c)) {
+        CK(launch_fill_ghosts_f32(c->Un[0], c->Un[1], c->Un[2], c->B, c->p.Nx, c->p.Ny,
+                                  c->pitch, c->p.bc, c->stream));
+        ++c->launches;
+        for (int f = 0; f < 3; ++f) {
+            // h = eta - B (exact in FP64); hu, hv widened.  The scratch staging buffer is
+            // reused, so each field's copy completes before the next conversion.
+            CK(launch_f32_to_f64(c->Un[f], f == 0 ? c->B : nullptr, c->stage64[1],
+                                 c->p.Nx + 4, c->p.Ny + 4, c->pitch, c->num_sms, c->stream));
+            ++c->launches;
+            CK(cudaMemcpy2DAsync(dst[f], row, c->stage64[1], spitch, row,
+                                 (size_t)(c->p.Nx + 4), cudaMemcpyDeviceToHost, c->stream));
+        }
+    } else {
+        CK(launch_fill_ghosts_f64(c->Un[0], c->Un[1], c->Un[2], c->p.Nx, c->p.Ny, c->pitch,
+                                  c->p.bc, c->stream));
+        ++c->launches;
+        for (int f = 0; f < 3; ++f)
+            CK(cudaMemcpy2DAsync(dst[f], row, c->Un[f], spitch, row, (size_t)(c->p.Nx + 4),
+                                 cudaMemcpyDeviceToHost, c->stream));
+    }
     CK(cudaStreamSynchronize(c->stream));
     return SWE_OK;
 }
@@ -270,7 +336,10 @@ int swe_step(swe_ctx *c, int n_steps, double dt, double *t_inout) {
     sp.bc = c->p.bc;
     sp.inv_dx = c->inv_dx;
     sp.inv_dy = c->inv_dy;
+    sp.kx = pow2_exponent(c->inv_dx);
+    sp.ky = pow2_exponent(c->inv_dy);
     sp.g = c->p.g;
+    sp.half_g = 0.5 * c->p.g;
     sp.cfl_min_dxdy = c->cfl_min_dxdy;
     sp.dt_fixed = dt > 0.0 ? dt : 0.0;
     sp.speed = c->speed;
@@ -286,15 +355,15 @@ int swe_step(swe_ctx *c, int n_steps, double dt, double *t_inout) {
         sp.hs = c->Un[0]; sp.hus = c->Un[1]; sp.hvs = c->Un[2];
         sp.hn = c->Un[0]; sp.hun = c->Un[1]; sp.hvn = c->Un[2];
         sp.ho = c->U1[0]; sp.huo = c->U1[1]; sp.hvo = c->U1[2];
-        CK(launch_stage_f64(1, sp, c->stream));
+        CK(launch_stage(c, 1, sp));
         // Stage 2: U2 = 3/4 Un + 1/4 (U1 + dt L(U1))
         sp.hs = c->U1[0]; sp.hus = c->U1[1]; sp.hvs = c->U1[2];
         sp.ho = c->U2[0]; sp.huo = c->U2[1]; sp.hvo = c->U2[2];
-        CK(launch_stage_f64(2, sp, c->stream));
+        CK(launch_stage(c, 2, sp));
         // Stage 3: Un = 1/3 Un + 2/3 (U2 + dt L(U2)), in place; max speed -> next slot
         sp.hs = c->U2[0]; sp.hus = c->U2[1]; sp.hvs = c->U2[2];
         sp.ho = c->Un[0]; sp.huo = c->Un[1]; sp.hvo = c->Un[2];
-        CK(launch_stage_f64(3, sp, c->stream));
+        CK(launch_stage(c, 3, sp));
         c->launches += 3;
         ++c->steps_done;
     }
@@ -333,6 +402,26 @@ int swe_stable_dt(swe_ctx *c, double *out) {
     int st = swe_max_wave_speed(c, &ms);
     if (st) return st;
     *out = (ms <= 1.0e-8) ? 1.0e100 : c->cfl_min_dxdy / ms;  // HPC_kernels.hpp:296-297
+    return SWE_OK;
+}
+
+int swe_totals(swe_ctx *c, double *mass, double *mx, double *my) {
+    if (!c || !mass || !mx || !my) return fail(c, SWE_ERR_BAD_ARG, "swe_totals: null argument");
+    if (!c->uploaded) return fail(c, SWE_ERR_BAD_ARG, "swe_totals: no state uploaded");
+    int st = set_device(c);
+    if (st) return st;
+    if (!c->partial)
+        CK(cudaMalloc(&c->partial, (6 * (size_t)totals_blocks(c->num_sms) + 4) * sizeof(double)));
+    double *out = c->partial + 6 * totals_blocks(c->num_sms);
+    CK(launch_totals(c->Un[0], c->Un[1], c->Un[2], c->B, fp32(c), c->p.Nx, c->p.Ny, c->pitch,
+                     c->dx * c->dy, c->partial, out, c->num_sms, c->stream));
+    c->launches += 2;
+    double r[3];
+    CK(cudaMemcpyAsync(r, out, sizeof r, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *mass = r[0];
+    *mx = r[1];
+    *my = r[2];
     return SWE_OK;
 }
 

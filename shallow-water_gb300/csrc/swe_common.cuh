@@ -28,7 +28,9 @@ struct StageParams {
     long long pitch;             // device row pitch in elements
     int bc;                      // BC_*
     double inv_dx, inv_dy;       // 1.0 / dx, 1.0 / dy (host-computed, as apply_divergence)
+    int kx, ky;                  // log2 of inv_dx / inv_dy when a power of two, else 127
     double g;                    // gravity
+    double half_g;               // 0.5 * g (exact)
     double cfl_min_dxdy;         // cfl * min(dx, dy) (compute_stable_dt numerator)
     double dt_fixed;             // > 0: fixed dt; otherwise adaptive from speed slot
     unsigned long long *speed;   // two max-wave-speed slots (double bit patterns)

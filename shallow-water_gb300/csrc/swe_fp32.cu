@@ -1,0 +1,387 @@
+// FP32-mixed form of the fused SSP-RK3 stage kernel.
+//
+// Same scheme as the FP64 drop-in (MUSCL on eta, hu, hv; hydrostatic reconstruction
+// with b* = max(b-, b+); HLL; SSP-RK3; positivity; walls; CFL reduction), with three
+// changes that make FP32 arithmetic safe:
+//
+//  * The stored state is (eta, hu, hv) with eta = h + B, not (h, hu, hv).  A lake at
+//    rest then has a bitwise-constant eta, the MUSCL slopes are exactly zero, and the
+//    interface depths eta - b are differences of two FP32 numbers that are exact
+//    (Sterbenz) wherever the water is shallow compared with b - the near-dry cells where
+//    the reference relies on FP64.
+//  * The HLL flux is evaluated as F* = F_L + D with
+//    D = s_L (s_R dU - dF) / (s_R - s_L) (or 0 / F_R - F_L in the supersonic cases), and
+//    the pressure of the interface depth hs, which the reference adds in the flux and
+//    removes in its hydrostatic correction (HPC_kernels.hpp:61-65, 174-183), is dropped
+//    from both: the momentum flux seen by the cell on side s is
+//    q_n u_n + D_n + g/2 h_s^2.  For equal left/right states D is exactly 0, so the
+//    wall pressures of a lake at rest cancel bitwise and hu = hv stay exactly 0.
+//  * Time and the CFL dt are FP64 (dt is reduced in FP32, divided in FP64, applied as
+//    the FP32 value whose FP64 image is accumulated).
+//
+// Layout: eta, hu, hv, B are FP32 ghosted arrays with the same pitch rule as the FP64
+// form.  The wall boundary condition is applied by mirrored indices while loading.
+#include "swe_common.cuh"
+#include "swe_launch.h"
+
+namespace swe {
+namespace {
+
+constexpr int TI = 8;
+constexpr int TJ = 32;
+constexpr int NT = (TI + 1) * TJ;
+constexpr int RI = TI + 4;
+constexpr int RJ = TJ + 4;
+constexpr float EPSF = 1.0e-8f;
+constexpr float H_FLOORF = 1.0e-8f;
+
+// Approximate reciprocal and square root (PTX rcp.approx / sqrt.approx, about 1 ulp);
+// their error is far below the form's stated L1 budget.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ float minmodf(float a, float b) {
+    if (a > 0.f && b > 0.f) return fminf(a, b);
+    if (a < 0.f && b < 0.f) return fmaxf(a, b);
+    return 0.f;
+}
+
+struct FaceF {
+    float fh, fqt, fqn_m, fqn_p;
+};
+
+// One interface from the 4-cell stencil (m1, c0 | p1, p2) of eta, qn (normal momentum),
+// qt (tangential momentum) and the bathymetry of the two adjacent cells.
+__device__ __forceinline__ FaceF face_flux_f32(float g, float half_g, float e_m1, float e_0,
+                                               float e_p1, float e_p2, float n_m1, float n_0,
+                                               float n_p1, float n_p2, float t_m1, float t_0,
+                                               float t_p1, float t_p2, float b_m, float b_p) {
+    const float eta_m = e_0 + 0.5f * minmodf(e_0 - e_m1, e_p1 - e_0);
+    const float eta_p = e_p1 - 0.5f * minmodf(e_p1 - e_0, e_p2 - e_p1);
+    const float qn_m = n_0 + 0.5f * minmodf(n_0 - n_m1, n_p1 - n_0);
+    const float qt_m = t_0 + 0.5f * minmodf(t_0 - t_m1, t_p1 - t_0);
+    const float qn_p = n_p1 - 0.5f * minmodf(n_p1 - n_0, n_p2 - n_p1);
+    const float qt_p = t_p1 - 0.5f * minmodf(t_p1 - t_0, t_p2 - t_p1);
+    const float b_star = fmaxf(b_m, b_p);
+    const float h_m = fmaxf(eta_m - b_m, 0.f);
+    const float h_p = fmaxf(eta_p - b_p, 0.f);
+    const float hs_m = fmaxf(eta_m - b_star, 0.f);
+    const float hs_p = fmaxf(eta_p - b_star, 0.f);
+    const float ih_m = h_m > EPSF ? rcp_approx(h_m) : 0.f;
+    const float ih_p = h_p > EPSF ? rcp_approx(h_p) : 0.f;
+    const float un_m = qn_m * ih_m, ut_m = qt_m * ih_m;
+    const float un_p = qn_p * ih_p, ut_p = qt_p * ih_p;
+    // left / right hydrostatic states and their advective fluxes
+    const float qnL = hs_m * un_m, qtL = hs_m * ut_m;
+    const float qnR = hs_p * un_p, qtR = hs_p * ut_p;
+    const float aLn = qnL * un_m, aLt = qnL * ut_m;
+    const float aRn = qnR * un_p, aRt = qnR * ut_p;
+    const float cL = sqrt_approx(g * hs_m), cR = sqrt_approx(g * hs_p);
+    const float sL = fminf(un_m - cL, un_p - cR);
+    const float sR = fmaxf(un_m + cL, un_p + cR);
+    float Dh = 0.f, Dn = 0.f, Dt = 0.f;
+    if (!(sL >= 0.f)) {
+        const float dFh = qnR - qnL;
+        const float dFn = (aRn - aLn) + half_g * (hs_p - hs_m) * (hs_p + hs_m);
+        const float dFt = aRt - aLt;
+        if (sR <= 0.f) {
+            Dh = dFh;
+            Dn = dFn;
+            Dt = dFt;
+        } else {
+            const float k = sL * rcp_approx(sR - sL);
+            Dh = k * (sR * (hs_p - hs_m) - dFh);
+            Dn = k * (sR * (qnR - qnL) - dFn);
+            Dt = k * (sR * (qtR - qtL) - dFt);
+        }
+    }
+    FaceF f;
+    f.fh = qnL + Dh;
+    f.fqt = aLt + Dt;
+    const float base = aLn + Dn;
+    f.fqn_m = base + half_g * h_m * h_m;
+    f.fqn_p = base + half_g * h_p * h_p;
+    return f;
+}
+
+__device__ __forceinline__ float cell_speed_f32(float g, float h, float hu, float hv) {
+    const float ih = h > EPSF ? rcp_approx(h) : 0.f;
+    const float c = sqrt_approx(g * fmaxf(h, 0.f));
+    return fmaxf(fabsf(hu * ih) + c, fabsf(hv * ih) + c);
+}
+
+__device__ __forceinline__ void block_max_to_slot_f(float v, unsigned long long *slot) {
+    __shared__ float red[32];
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        v = lane < nw ? red[lane] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0 && v > 0.f)
+            atomicMax(slot, (unsigned long long)__double_as_longlong((double)v));
+    }
+}
+
+__device__ __forceinline__ double stage_dt_f32(const StageParams &p) {
+    if (p.dt_fixed > 0.0) return p.dt_fixed;
+    const double ms = __longlong_as_double((long long)p.speed[p.slot_read]);
+    if (ms <= EPS) return 1.0e100;
+    return p.cfl_min_dxdy / ms;
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(NT) k_stage_f32(const StageParams p) {
+    __shared__ float s_e[RI][RJ], s_u[RI][RJ], s_v[RI][RJ], s_b[RI][RJ];
+    __shared__ float s_xf[4][TI + 1][TJ];
+    __shared__ float s_yf[4][TI][TJ + 1];
+
+    const int tid = threadIdx.x;
+    const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
+    const long long P = p.pitch;
+    const float *es = static_cast<const float *>(p.hs);
+    const float *us = static_cast<const float *>(p.hus);
+    const float *vs = static_cast<const float *>(p.hvs);
+    const float *Bg = static_cast<const float *>(p.B);
+
+    for (int t = tid; t < RI * RJ; t += NT) {
+        const int r = t / RJ, c = t - (t / RJ) * RJ;
+        const int ii = i0 - NG + r, jj = j0 - NG + c;
+        bool fx, fy;
+        const int mi = map_coord(ii, p.Nx, p.bc, fx);
+        const int mj = map_coord(jj, p.Ny, p.bc, fy);
+        const long long k = (long long)(mi + NG) * P + (mj + NG);
+        const int bi = clamp_int(ii + NG, 0, p.Nx + 2 * NG - 1);
+        const int bj = clamp_int(jj + NG, 0, p.Ny + 2 * NG - 1);
+        const float b = Bg[(long long)bi * P + bj];
+        // A ghost holds the interior cell's depth over its own bed: eta_g = h_src + B_g
+        // (eta itself where the beds agree, so a flat surface stays bitwise flat).
+        const float bsrc = Bg[k];
+        const float e = es[k];
+        s_e[r][c] = (b == bsrc) ? e : (e - bsrc) + b;
+        const float u = us[k], v = vs[k];
+        s_u[r][c] = fx ? -u : u;
+        s_v[r][c] = fy ? -v : v;
+        s_b[r][c] = b;
+    }
+    __syncthreads();
+
+    const float g = (float)p.g, half_g = (float)p.half_g;
+    {
+        const int fr = tid / TJ, fc = tid - (tid / TJ) * TJ;
+        const int a = fr + 1, c = fc + NG;
+        const FaceF F = face_flux_f32(g, half_g, s_e[a - 1][c], s_e[a][c], s_e[a + 1][c],
+                                      s_e[a + 2][c], s_u[a - 1][c], s_u[a][c], s_u[a + 1][c],
+                                      s_u[a + 2][c], s_v[a - 1][c], s_v[a][c], s_v[a + 1][c],
+                                      s_v[a + 2][c], s_b[a][c], s_b[a + 1][c]);
+        s_xf[0][fr][fc] = F.fh;
+        s_xf[1][fr][fc] = F.fqt;
+        s_xf[2][fr][fc] = F.fqn_m;
+        s_xf[3][fr][fc] = F.fqn_p;
+    }
+    if (tid < TI * (TJ + 1)) {
+        const int fr = tid / (TJ + 1), fc = tid - (tid / (TJ + 1)) * (TJ + 1);
+        const int r = fr + NG, a = fc + 1;
+        const FaceF F = face_flux_f32(g, half_g, s_e[r][a - 1], s_e[r][a], s_e[r][a + 1],
+                                      s_e[r][a + 2], s_v[r][a - 1], s_v[r][a], s_v[r][a + 1],
+                                      s_v[r][a + 2], s_u[r][a - 1], s_u[r][a], s_u[r][a + 1],
+                                      s_u[r][a + 2], s_b[r][a], s_b[r][a + 1]);
+        s_yf[0][fr][fc] = F.fh;
+        s_yf[1][fr][fc] = F.fqt;
+        s_yf[2][fr][fc] = F.fqn_m;
+        s_yf[3][fr][fc] = F.fqn_p;
+    }
+    __syncthreads();
+
+    const int ty = tid / TJ, tx = tid - (tid / TJ) * TJ;
+    const int ii = i0 + ty, jj = j0 + tx;
+    const bool inside = (ty < TI) && (ii < p.Nx) && (jj < p.Ny);
+    const double dtd = stage_dt_f32(p);
+    const float dt = (float)dtd;
+    float speed = 0.f;
+    if (inside) {
+        const float idx = (float)p.inv_dx, idy = (float)p.inv_dy;
+        const float rh = -idx * (s_xf[0][ty + 1][tx] - s_xf[0][ty][tx]) -
+                         idy * (s_yf[0][ty][tx + 1] - s_yf[0][ty][tx]);
+        const float rhu = -idx * (s_xf[2][ty + 1][tx] - s_xf[3][ty][tx]) -
+                          idy * (s_yf[1][ty][tx + 1] - s_yf[1][ty][tx]);
+        const float rhv = -idx * (s_xf[1][ty + 1][tx] - s_xf[1][ty][tx]) -
+                          idy * (s_yf[2][ty][tx + 1] - s_yf[3][ty][tx]);
+        const long long k = (long long)(ii + NG) * P + (jj + NG);
+        const float se = s_e[ty + NG][tx + NG], su = s_u[ty + NG][tx + NG];
+        const float sv = s_v[ty + NG][tx + NG], b = s_b[ty + NG][tx + NG];
+        float oe, ou, ov;
+        if (STAGE == 1) {
+            oe = se + dt * rh;
+            ou = su + dt * rhu;
+            ov = sv + dt * rhv;
+        } else {
+            const float ne = static_cast<const float *>(p.hn)[k];
+            const float nu = static_cast<const float *>(p.hun)[k];
+            const float nv = static_cast<const float *>(p.hvn)[k];
+            if (STAGE == 2) {
+                oe = 0.75f * ne + 0.25f * (se + dt * rh);
+                ou = 0.75f * nu + 0.25f * (su + dt * rhu);
+                ov = 0.75f * nv + 0.25f * (sv + dt * rhv);
+            } else {
+                oe = (1.f / 3.f) * ne + (2.f / 3.f) * (se + dt * rh);
+                ou = (1.f / 3.f) * nu + (2.f / 3.f) * (su + dt * rhu);
+                ov = (1.f / 3.f) * nv + (2.f / 3.f) * (sv + dt * rhv);
+            }
+        }
+        if (oe - b < H_FLOORF) {  // enforce_positivity on h = eta - B
+            oe = b + H_FLOORF;
+            ou = 0.f;
+            ov = 0.f;
+        }
+        if (!isfinite(oe) || !isfinite(ou) || !isfinite(ov)) atomicOr(p.flags, FLAG_NONFINITE);
+        static_cast<float *>(p.ho)[k] = oe;
+        static_cast<float *>(p.huo)[k] = ou;
+        static_cast<float *>(p.hvo)[k] = ov;
+        if (STAGE == 3) speed = cell_speed_f32(g, oe - b, ou, ov);
+    }
+    if (STAGE == 1 && blockIdx.x == 0 && blockIdx.y == 0 && tid == 0) {
+        p.speed[p.slot_write] = 0ull;
+        if (p.dt_log) p.dt_log[p.log_index] = (double)dt;
+    }
+    if (STAGE == 3) {
+        block_max_to_slot_f(speed, p.speed + p.slot_write);
+        if (blockIdx.x == 0 && blockIdx.y == 0 && tid == 0 && p.t_accum) *p.t_accum += (double)dt;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_max_speed_f32(const float *e, const float *hu,
+                                                       const float *hv, const float *B, int Nx,
+                                                       int Ny, long long P, float g,
+                                                       unsigned long long *slot) {
+    float v = 0.f;
+    const long long n = (long long)Nx * Ny;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t / Ny), j = (int)(t - (t / Ny) * Ny);
+        const long long k = (long long)(i + NG) * P + (j + NG);
+        v = fmaxf(v, cell_speed_f32(g, e[k] - B[k], hu[k], hv[k]));
+    }
+    block_max_to_slot_f(v, slot);
+}
+
+// FP64 host-layout staging <-> FP32 device state, for all (Nx+4) x (Ny+4) cells.
+// to_device: eta = RN32(h + B), hu, hv = RN32; B = RN32(B).
+__global__ void k_f64_to_f32(const double *src, const double *add, float *dst, int rows,
+                             int cols, long long P) {
+    const long long n = (long long)rows * cols;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t / cols), j = (int)(t - (t / cols) * cols);
+        const long long k = (long long)i * P + j;
+        const double v = add ? src[k] + add[k] : src[k];
+        dst[k] = (float)v;
+    }
+}
+
+// to_host: h = eta - B (exact in FP64 for FP32 operands), hu, hv widened.
+__global__ void k_f32_to_f64(const float *src, const float *sub, double *dst, int rows, int cols,
+                             long long P) {
+    const long long n = (long long)rows * cols;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t / cols), j = (int)(t - (t / cols) * cols);
+        const long long k = (long long)i * P + j;
+        dst[k] = sub ? (double)src[k] - (double)sub[k] : (double)src[k];
+    }
+}
+
+// Ghost refresh of the FP32 state: as k_fill_ghosts_f64, with the ghost's free surface
+// rebuilt over its own bed (eta_g = eta_src - B_src + B_g) so the depth is mirrored.
+__global__ void k_fill_ghosts_f32(float *e, float *hu, float *hv, const float *B, int Nx, int Ny,
+                                  long long P, int bc) {
+    const int NyT = Ny + 2 * NG;
+    const int n_rows = 4 * NyT, n_cols = 4 * Nx;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n_rows + n_cols) return;
+    int i, j;
+    if (t < n_rows) {
+        const int r = t / NyT;
+        j = t - r * NyT;
+        i = r < 2 ? r : Nx + r;
+    } else {
+        const int u = t - n_rows;
+        const int c = u / Nx;
+        i = NG + (u - c * Nx);
+        j = c < 2 ? c : Ny + c;
+    }
+    bool fx, fy;
+    const int si = map_coord(i - NG, Nx, bc, fx) + NG;
+    const int sj = map_coord(j - NG, Ny, bc, fy) + NG;
+    const long long kd = (long long)i * P + j, ks = (long long)si * P + sj;
+    e[kd] = (B[kd] == B[ks]) ? e[ks] : (e[ks] - B[ks]) + B[kd];
+    hu[kd] = fx ? -hu[ks] : hu[ks];
+    hv[kd] = fy ? -hv[ks] : hv[ks];
+}
+
+unsigned grid_for(long long n, int num_sms) {
+    long long blocks = (n + 255) / 256;
+    const long long cap = (long long)num_sms * 16;
+    if (blocks > cap) blocks = cap;
+    return (unsigned)(blocks < 1 ? 1 : blocks);
+}
+
+}  // namespace
+
+cudaError_t launch_stage_f32(int stage, const StageParams &p, cudaStream_t s) {
+    const dim3 grid((p.Ny + TJ - 1) / TJ, (p.Nx + TI - 1) / TI);
+    switch (stage) {
+        case 1: k_stage_f32<1><<<grid, NT, 0, s>>>(p); break;
+        case 2: k_stage_f32<2><<<grid, NT, 0, s>>>(p); break;
+        default: k_stage_f32<3><<<grid, NT, 0, s>>>(p); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_max_speed_f32(const void *e, const void *hu, const void *hv, const void *B,
+                                 int Nx, int Ny, long long pitch, double g,
+                                 unsigned long long *slot, int num_sms, cudaStream_t s) {
+    k_max_speed_f32<<<grid_for((long long)Nx * Ny, num_sms), 256, 0, s>>>(
+        static_cast<const float *>(e), static_cast<const float *>(hu),
+        static_cast<const float *>(hv), static_cast<const float *>(B), Nx, Ny, pitch, (float)g,
+        slot);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_f64_to_f32(const void *src, const void *add, void *dst, int rows, int cols,
+                              long long pitch, int num_sms, cudaStream_t s) {
+    k_f64_to_f32<<<grid_for((long long)rows * cols, num_sms), 256, 0, s>>>(
+        static_cast<const double *>(src), static_cast<const double *>(add),
+        static_cast<float *>(dst), rows, cols, pitch);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_f32_to_f64(const void *src, const void *sub, void *dst, int rows, int cols,
+                              long long pitch, int num_sms, cudaStream_t s) {
+    k_f32_to_f64<<<grid_for((long long)rows * cols, num_sms), 256, 0, s>>>(
+        static_cast<const float *>(src), static_cast<const float *>(sub),
+        static_cast<double *>(dst), rows, cols, pitch);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_ghosts_f32(void *e, void *hu, void *hv, const void *B, int Nx, int Ny,
+                                   long long pitch, int bc, cudaStream_t s) {
+    const int n = 4 * (Ny + 2 * NG) + 4 * Nx;
+    k_fill_ghosts_f32<<<(n + 255) / 256, 256, 0, s>>>(
+        static_cast<float *>(e), static_cast<float *>(hu), static_cast<float *>(hv),
+        static_cast<const float *>(B), Nx, Ny, pitch, bc);
+    return cudaGetLastError();
+}
+
+}  // namespace swe

@@ -13,7 +13,14 @@
 // (apply_divergence), the RK combine, positivity and the store.  Stage 3 also reduces
 // the max wave speed of the new state (compute_stable_dt) into a device slot with a
 // warp shuffle, a block reduction and one atomicMax per CTA.
+//
+// GB300 runs FP64 at ~2 operations/clock/SM, 1/64 of FP32, so the kernel is bound by
+// the FP64 pipe, not by HBM.  Everything that need not be an FP64 instruction is moved
+// to the integer pipe with bit-exact helpers (swe_f64_exact.cuh): compares, min/max,
+// minmod's sign logic, positive parts, exact scalings by powers of two, and the
+// reference's re-division (h*u)/h, which is decided from one exact FMA residual.
 #include "swe_common.cuh"
+#include "swe_f64_exact.cuh"
 #include "swe_launch.h"
 
 namespace swe {
@@ -21,59 +28,63 @@ namespace {
 
 constexpr int TI = 8;    // tile rows (x)
 constexpr int TJ = 32;   // tile columns (y, contiguous)
-constexpr int NT = TI * TJ;
+constexpr int NT = (TI + 1) * TJ;  // one thread per x-face; covers TI*(TJ+1) y-faces too
 constexpr int RI = TI + 4;  // staged rows incl. halo
 constexpr int RJ = TJ + 4;  // staged columns incl. halo
 
-__device__ __forceinline__ double dmin(double a, double b) { return (b < a) ? b : a; }
-__device__ __forceinline__ double dmax(double a, double b) { return (a < b) ? b : a; }
+using x64::dmax;
+using x64::dmin;
 
-// HPC_kernels.hpp:33-35
-__device__ __forceinline__ double positive_height(double h) { return h > 0.0 ? h : 0.0; }
+constexpr int64_t EPS_BITS = 0x3E45798EE2308C3ALL;  // bits of 1.0e-8
+static_assert(sizeof(double) == 8, "double is binary64");
 
-// HPC_kernels.hpp:37-39
+// safe_velocity (HPC_kernels.hpp:37-39): (h > 1e-8) ? q / h : 0.0
 __device__ __forceinline__ double safe_velocity(double q, double h) {
-    return (h > EPS) ? (q / h) : 0.0;
+    return x64::gt_pos_const(h, EPS_BITS) ? (q / h) : 0.0;
 }
 
-// HPC_kernels.hpp:41-44
-__device__ __forceinline__ double minmod(double a, double b) {
-    if (a * b <= 0.0) return 0.0;
-    return (a > 0.0 ? 1.0 : -1.0) * dmin(fabs(a), fabs(b));
+// Exact multiplication by a grid constant that may be a power of two (k != 127).
+__device__ __forceinline__ double mul_const(double c, int k, double x) {
+    return k != 127 ? x64::scale2(x, k, c) : c * x;
 }
 
 // hll_x (HPC_kernels.hpp:46-82) in normal/tangential form; hll_y (:84-120) is the
-// same with hv normal and hu tangential.
-__device__ __forceinline__ void hll_normal(double g, double hL, double qnL, double qtL,
-                                           double hR, double qnR, double qtR, double &fh,
-                                           double &fqn, double &fqt) {
-    const double unL = safe_velocity(qnL, hL);
-    const double utL = safe_velocity(qtL, hL);
-    const double unR = safe_velocity(qnR, hR);
-    const double utR = safe_velocity(qtR, hR);
+// same with hv normal and hu tangential.  The left/right states are
+// (hL, hL*unm, hL*utm) and (hR, hR*unp, hR*utp) as built at :164-169; the velocities
+// the reference recomputes from them, (hL*unm)/hL etc., come from x64::redivide.
+__device__ __forceinline__ void hll_normal(double g, double half_g, double hL, double unm,
+                                           double utm, double hR, double unp, double utp,
+                                           double &fh, double &fqn, double &fqt) {
+    const double qnL = hL * unm, qtL = hL * utm, qnR = hR * unp, qtR = hR * utp;
+    const bool wetL = x64::gt_pos_const(hL, EPS_BITS), wetR = x64::gt_pos_const(hR, EPS_BITS);
+    const double unL = wetL ? x64::redivide(qnL, hL, unm) : 0.0;
+    const double utL = wetL ? x64::redivide(qtL, hL, utm) : 0.0;
+    const double unR = wetR ? x64::redivide(qnR, hR, unp) : 0.0;
+    const double utR = wetR ? x64::redivide(qtR, hR, utp) : 0.0;
     const double cL = sqrt(g * hL);
     const double cR = sqrt(g * hR);
     const double sL = dmin(unL - cL, unR - cR);
     const double sR = dmax(unL + cL, unR + cR);
     const double FL_h = qnL;
-    const double FL_n = qnL * unL + 0.5 * g * hL * hL;
+    const double FL_n = qnL * unL + half_g * hL * hL;
     const double FL_t = qnL * utL;
     const double FR_h = qnR;
-    const double FR_n = qnR * unR + 0.5 * g * hR * hR;
+    const double FR_n = qnR * unR + half_g * hR * hR;
     const double FR_t = qnR * utR;
-    if (sL >= 0.0) {
+    if (x64::le(0.0, sL)) {
         fh = FL_h;
         fqn = FL_n;
         fqt = FL_t;
-    } else if (sR <= 0.0) {
+    } else if (x64::le(sR, 0.0)) {
         fh = FR_h;
         fqn = FR_n;
         fqt = FR_t;
     } else {
         const double inv = 1.0 / (sR - sL);
-        fh = (sR * FL_h - sL * FR_h + sL * sR * (hR - hL)) * inv;
-        fqn = (sR * FL_n - sL * FR_n + sL * sR * (qnR - qnL)) * inv;
-        fqt = (sR * FL_t - sL * FR_t + sL * sR * (qtR - qtL)) * inv;
+        const double sLsR = sL * sR;
+        fh = (sR * FL_h - sL * FR_h + sLsR * (hR - hL)) * inv;
+        fqn = (sR * FL_n - sL * FR_n + sLsR * (qnR - qnL)) * inv;
+        fqt = (sR * FL_t - sL * FR_t + sLsR * (qtR - qtL)) * inv;
     }
 }
 
@@ -84,31 +95,34 @@ struct Face {
     double fh, fqt, fqn_m, fqn_p;
 };
 
-__device__ __forceinline__ Face face_flux(double g, double eta_m1, double eta_0, double eta_p1,
-                                          double eta_p2, double qn_m1, double qn_0,
-                                          double qn_p1, double qn_p2, double qt_m1,
+__device__ __forceinline__ Face face_flux(double g, double half_g, double eta_m1, double eta_0,
+                                          double eta_p1, double eta_p2, double qn_m1,
+                                          double qn_0, double qn_p1, double qn_p2, double qt_m1,
                                           double qt_0, double qt_p1, double qt_p2,
                                           double b_minus, double b_plus) {
-    const double eta_minus = eta_0 + 0.5 * minmod(eta_0 - eta_m1, eta_p1 - eta_0);
-    const double eta_plus = eta_p1 - 0.5 * minmod(eta_p1 - eta_0, eta_p2 - eta_p1);
-    const double qn_minus = qn_0 + 0.5 * minmod(qn_0 - qn_m1, qn_p1 - qn_0);
-    const double qt_minus = qt_0 + 0.5 * minmod(qt_0 - qt_m1, qt_p1 - qt_0);
-    const double qn_plus = qn_p1 - 0.5 * minmod(qn_p1 - qn_0, qn_p2 - qn_p1);
-    const double qt_plus = qt_p1 - 0.5 * minmod(qt_p1 - qt_0, qt_p2 - qt_p1);
+    const double d_eta0 = eta_0 - eta_m1, d_eta1 = eta_p1 - eta_0, d_eta2 = eta_p2 - eta_p1;
+    const double d_qn0 = qn_0 - qn_m1, d_qn1 = qn_p1 - qn_0, d_qn2 = qn_p2 - qn_p1;
+    const double d_qt0 = qt_0 - qt_m1, d_qt1 = qt_p1 - qt_0, d_qt2 = qt_p2 - qt_p1;
+    const double eta_minus = eta_0 + x64::halve(x64::minmod(d_eta0, d_eta1));
+    const double eta_plus = eta_p1 - x64::halve(x64::minmod(d_eta1, d_eta2));
+    const double qn_minus = qn_0 + x64::halve(x64::minmod(d_qn0, d_qn1));
+    const double qt_minus = qt_0 + x64::halve(x64::minmod(d_qt0, d_qt1));
+    const double qn_plus = qn_p1 - x64::halve(x64::minmod(d_qn1, d_qn2));
+    const double qt_plus = qt_p1 - x64::halve(x64::minmod(d_qt1, d_qt2));
     const double b_star = dmax(b_minus, b_plus);
-    const double h_minus = positive_height(eta_minus - b_minus);
-    const double h_plus = positive_height(eta_plus - b_plus);
+    const double h_minus = x64::positive_part(eta_minus - b_minus);
+    const double h_plus = x64::positive_part(eta_plus - b_plus);
     const double un_minus = safe_velocity(qn_minus, h_minus);
     const double ut_minus = safe_velocity(qt_minus, h_minus);
     const double un_plus = safe_velocity(qn_plus, h_plus);
     const double ut_plus = safe_velocity(qt_plus, h_plus);
-    const double hs_minus = positive_height(eta_minus - b_star);
-    const double hs_plus = positive_height(eta_plus - b_star);
+    const double hs_minus = x64::positive_part(eta_minus - b_star);
+    const double hs_plus = x64::positive_part(eta_plus - b_star);
     double f_h, f_n, f_t;
-    hll_normal(g, hs_minus, hs_minus * un_minus, hs_minus * ut_minus, hs_plus,
-               hs_plus * un_plus, hs_plus * ut_plus, f_h, f_n, f_t);
-    const double corr_minus = 0.5 * g * (h_minus * h_minus - hs_minus * hs_minus);
-    const double corr_plus = 0.5 * g * (h_plus * h_plus - hs_plus * hs_plus);
+    hll_normal(g, half_g, hs_minus, un_minus, ut_minus, hs_plus, un_plus, ut_plus, f_h, f_n,
+               f_t);
+    const double corr_minus = half_g * (h_minus * h_minus - hs_minus * hs_minus);
+    const double corr_plus = half_g * (h_plus * h_plus - hs_plus * hs_plus);
     Face f;
     f.fh = f_h;
     f.fqt = f_t;
@@ -121,8 +135,8 @@ __device__ __forceinline__ Face face_flux(double g, double eta_m1, double eta_0,
 __device__ __forceinline__ double cell_speed(double g, double h, double hu, double hv) {
     const double u = safe_velocity(hu, h);
     const double v = safe_velocity(hv, h);
-    const double c = sqrt(g * dmax(0.0, h));
-    return dmax(fabs(u) + c, fabs(v) + c);
+    const double c = sqrt(g * x64::positive_part(h));  // std::max(0.0, h)
+    return dmax(x64::fabs_(u) + c, x64::fabs_(v) + c);
 }
 
 // Block max of per-thread non-negative speeds, then one atomicMax on the bit pattern
@@ -144,7 +158,7 @@ __device__ __forceinline__ void block_max_to_slot(double v, unsigned long long *
 __device__ __forceinline__ double stage_dt(const StageParams &p) {
     if (p.dt_fixed > 0.0) return p.dt_fixed;
     const double ms = __longlong_as_double((long long)p.speed[p.slot_read]);
-    if (ms <= EPS) return 1.0e100;  // compute_stable_dt, HPC_kernels.hpp:296
+    if (x64::le(ms, EPS)) return 1.0e100;  // compute_stable_dt, HPC_kernels.hpp:296
     return p.cfl_min_dxdy / ms;
 }
 
@@ -184,12 +198,12 @@ __global__ void __launch_bounds__(NT) k_stage_f64(const StageParams p) {
     }
     __syncthreads();
 
-    const double g = p.g;
-    // x-faces: between tile rows a = fr + 1 and a + 1, for fr in [0, TI].
-    for (int f = tid; f < (TI + 1) * TJ; f += NT) {
-        const int fr = f / TJ, fc = f - (f / TJ) * TJ;
+    const double g = p.g, half_g = p.half_g;
+    // x-faces: between tile rows a = fr + 1 and a + 1, for fr in [0, TI]: one per thread.
+    {
+        const int fr = tid / TJ, fc = tid - (tid / TJ) * TJ;
         const int a = fr + 1, c = fc + NG;
-        const Face F = face_flux(g, s_eta[a - 1][c], s_eta[a][c], s_eta[a + 1][c],
+        const Face F = face_flux(g, half_g, s_eta[a - 1][c], s_eta[a][c], s_eta[a + 1][c],
                                  s_eta[a + 2][c], s_hu[a - 1][c], s_hu[a][c], s_hu[a + 1][c],
                                  s_hu[a + 2][c], s_hv[a - 1][c], s_hv[a][c], s_hv[a + 1][c],
                                  s_hv[a + 2][c], s_B[a][c], s_B[a + 1][c]);
@@ -199,10 +213,10 @@ __global__ void __launch_bounds__(NT) k_stage_f64(const StageParams p) {
         s_xf[3][fr][fc] = F.fqn_p;
     }
     // y-faces: between tile columns a = fc + 1 and a + 1, for fc in [0, TJ].
-    for (int f = tid; f < TI * (TJ + 1); f += NT) {
-        const int fr = f / (TJ + 1), fc = f - (f / (TJ + 1)) * (TJ + 1);
+    if (tid < TI * (TJ + 1)) {
+        const int fr = tid / (TJ + 1), fc = tid - (tid / (TJ + 1)) * (TJ + 1);
         const int r = fr + NG, a = fc + 1;
-        const Face F = face_flux(g, s_eta[r][a - 1], s_eta[r][a], s_eta[r][a + 1],
+        const Face F = face_flux(g, half_g, s_eta[r][a - 1], s_eta[r][a], s_eta[r][a + 1],
                                  s_eta[r][a + 2], s_hv[r][a - 1], s_hv[r][a], s_hv[r][a + 1],
                                  s_hv[r][a + 2], s_hu[r][a - 1], s_hu[r][a], s_hu[r][a + 1],
                                  s_hu[r][a + 2], s_B[r][a], s_B[r][a + 1]);
@@ -215,18 +229,19 @@ __global__ void __launch_bounds__(NT) k_stage_f64(const StageParams p) {
 
     const int ty = tid / TJ, tx = tid - (tid / TJ) * TJ;
     const int ii = i0 + ty, jj = j0 + tx;
-    const bool inside = (ii < p.Nx) && (jj < p.Ny);
+    const bool inside = (ty < TI) && (ii < p.Nx) && (jj < p.Ny);
     const double dt = stage_dt(p);
     double speed = 0.0;
     if (inside) {
         // apply_divergence (HPC_kernels.hpp:274-276): right/top face minus-side
         // fluxes against left/bottom face plus-side fluxes.
-        const double rh = -p.inv_dx * (s_xf[0][ty + 1][tx] - s_xf[0][ty][tx]) -
-                          p.inv_dy * (s_yf[0][ty][tx + 1] - s_yf[0][ty][tx]);
-        const double rhu = -p.inv_dx * (s_xf[2][ty + 1][tx] - s_xf[3][ty][tx]) -
-                           p.inv_dy * (s_yf[1][ty][tx + 1] - s_yf[1][ty][tx]);
-        const double rhv = -p.inv_dx * (s_xf[1][ty + 1][tx] - s_xf[1][ty][tx]) -
-                           p.inv_dy * (s_yf[2][ty][tx + 1] - s_yf[3][ty][tx]);
+        // -inv_dx * (a - b) - inv_dy * (c - d); (-c) * x == -(c * x) exactly.
+        const double rh = -mul_const(p.inv_dx, p.kx, s_xf[0][ty + 1][tx] - s_xf[0][ty][tx]) -
+                          mul_const(p.inv_dy, p.ky, s_yf[0][ty][tx + 1] - s_yf[0][ty][tx]);
+        const double rhu = -mul_const(p.inv_dx, p.kx, s_xf[2][ty + 1][tx] - s_xf[3][ty][tx]) -
+                           mul_const(p.inv_dy, p.ky, s_yf[1][ty][tx + 1] - s_yf[1][ty][tx]);
+        const double rhv = -mul_const(p.inv_dx, p.kx, s_xf[1][ty + 1][tx] - s_xf[1][ty][tx]) -
+                           mul_const(p.inv_dy, p.ky, s_yf[2][ty][tx + 1] - s_yf[3][ty][tx]);
         const long long k = (long long)(ii + NG) * P + (jj + NG);
         const double sh = s_h[ty + NG][tx + NG];
         const double shu = s_hu[ty + NG][tx + NG];
@@ -241,9 +256,9 @@ __global__ void __launch_bounds__(NT) k_stage_f64(const StageParams p) {
             const double nhu = static_cast<const double *>(p.hun)[k];
             const double nhv = static_cast<const double *>(p.hvn)[k];
             if (STAGE == 2) {  // HPC_solver.hpp:271-273
-                oh = 0.75 * nh + 0.25 * (sh + dt * rh);
-                ohu = 0.75 * nhu + 0.25 * (shu + dt * rhu);
-                ohv = 0.75 * nhv + 0.25 * (shv + dt * rhv);
+                oh = 0.75 * nh + x64::scale2(sh + dt * rh, -2, 0.25);
+                ohu = 0.75 * nhu + x64::scale2(shu + dt * rhu, -2, 0.25);
+                ohv = 0.75 * nhv + x64::scale2(shv + dt * rhv, -2, 0.25);
             } else {  // HPC_solver.hpp:296-300
                 oh = (1.0 / 3.0) * nh + (2.0 / 3.0) * (sh + dt * rh);
                 ohu = (1.0 / 3.0) * nhu + (2.0 / 3.0) * (shu + dt * rhu);
@@ -251,12 +266,15 @@ __global__ void __launch_bounds__(NT) k_stage_f64(const StageParams p) {
             }
         }
         // enforce_positivity (HPC_kernels.hpp:305-312)
-        if (oh < H_FLOOR) {
+        if (x64::lt(oh, H_FLOOR)) {
             oh = H_FLOOR;
             ohu = 0.0;
             ohv = 0.0;
         }
-        if (!isfinite(oh) || !isfinite(ohu) || !isfinite(ohv)) atomicOr(p.flags, FLAG_NONFINITE);
+        if (((x64::bits(oh) & x64::ABS) >= x64::INF_BITS) ||
+            ((x64::bits(ohu) & x64::ABS) >= x64::INF_BITS) ||
+            ((x64::bits(ohv) & x64::ABS) >= x64::INF_BITS))
+            atomicOr(p.flags, FLAG_NONFINITE);
         static_cast<double *>(p.ho)[k] = oh;
         static_cast<double *>(p.huo)[k] = ohu;
         static_cast<double *>(p.hvo)[k] = ohv;

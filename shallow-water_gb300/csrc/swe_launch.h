@@ -15,4 +15,23 @@ cudaError_t launch_max_speed_f64(const void *h, const void *hu, const void *hv, 
 cudaError_t launch_fill_ghosts_f64(void *h, void *hu, void *hv, int Nx, int Ny, long long pitch,
                                    int bc, cudaStream_t s);
 
+// FP32-mixed form (swe_fp32.cu): state (eta = h + B, hu, hv) and B in FP32.
+cudaError_t launch_stage_f32(int stage, const StageParams &p, cudaStream_t s);
+cudaError_t launch_max_speed_f32(const void *e, const void *hu, const void *hv, const void *B,
+                                 int Nx, int Ny, long long pitch, double g,
+                                 unsigned long long *slot, int num_sms, cudaStream_t s);
+cudaError_t launch_f64_to_f32(const void *src, const void *add, void *dst, int rows, int cols,
+                              long long pitch, int num_sms, cudaStream_t s);
+cudaError_t launch_f32_to_f64(const void *src, const void *sub, void *dst, int rows, int cols,
+                              long long pitch, int num_sms, cudaStream_t s);
+cudaError_t launch_fill_ghosts_f32(void *e, void *hu, void *hv, const void *B, int Nx, int Ny,
+                                   long long pitch, int bc, cudaStream_t s);
+
+// Compensated totals (swe_reduce.cu): out[0..2] = (sum h, sum hu, sum hv) * dxdy.
+// partial needs 6 * totals_blocks(num_sms) doubles.
+int totals_blocks(int num_sms);
+cudaError_t launch_totals(const void *h, const void *hu, const void *hv, const void *B, bool f32,
+                          int Nx, int Ny, long long pitch, double dxdy, double *partial,
+                          double *out, int num_sms, cudaStream_t s);
+
 }  // namespace swe

@@ -1,0 +1,114 @@
+// Compensated global totals of the state: mass = sum h dx dy, momentum = sum hu dx dy,
+// sum hv dx dy over the interior (the quantity the reference's MassConservation check
+// accumulates naively, tests/sanity_checks/mass_conservation.hpp:45-56).
+//
+// Each thread keeps Neumaier-compensated FP64 sums over a fixed grid-stride set of
+// cells; warps and blocks combine (sum, compensation) pairs with the error-free
+// TwoSum; a second one-block kernel adds the per-block pairs in block order.  The
+// result is deterministic (fixed assignment and order) and accurate to about one
+// rounding of the total.  Works on both forms (FP32 eta - B is exact in FP64).
+#include "swe_common.cuh"
+#include "swe_launch.h"
+
+namespace swe {
+namespace {
+
+struct Comp {
+    double s, c;
+};
+
+__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e) {
+    s = a + b;
+    const double bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ void add(Comp &x, double v) {
+    double s, e;
+    two_sum(x.s, v, s, e);
+    x.s = s;
+    x.c += e;
+}
+
+__device__ __forceinline__ Comp merge(Comp x, Comp y) {
+    Comp r;
+    double e;
+    two_sum(x.s, y.s, r.s, e);
+    r.c = x.c + y.c + e;
+    return r;
+}
+
+constexpr int BT = 256;
+
+template <bool F32>
+__global__ void __launch_bounds__(BT) k_totals_partial(const void *h, const void *hu,
+                                                       const void *hv, const void *B, int Nx,
+                                                       int Ny, long long P, double *partial) {
+    Comp acc[3] = {{0, 0}, {0, 0}, {0, 0}};
+    const long long n = (long long)Nx * Ny;
+    for (long long t = blockIdx.x * (long long)BT + threadIdx.x; t < n;
+         t += (long long)gridDim.x * BT) {
+        const int i = (int)(t / Ny), j = (int)(t - (t / Ny) * Ny);
+        const long long k = (long long)(i + NG) * P + (j + NG);
+        double v0, v1, v2;
+        if (F32) {
+            v0 = (double)static_cast<const float *>(h)[k] - (double)static_cast<const float *>(B)[k];
+            v1 = static_cast<const float *>(hu)[k];
+            v2 = static_cast<const float *>(hv)[k];
+        } else {
+            v0 = static_cast<const double *>(h)[k];
+            v1 = static_cast<const double *>(hu)[k];
+            v2 = static_cast<const double *>(hv)[k];
+        }
+        add(acc[0], v0);
+        add(acc[1], v1);
+        add(acc[2], v2);
+    }
+    __shared__ Comp red[3][BT / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int q = 0; q < 3; ++q) {
+        Comp x = acc[q];
+        for (int o = 16; o > 0; o >>= 1) {
+            Comp y;
+            y.s = __shfl_down_sync(0xffffffffu, x.s, o);
+            y.c = __shfl_down_sync(0xffffffffu, x.c, o);
+            x = merge(x, y);
+        }
+        if (lane == 0) red[q][warp] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        Comp x = red[threadIdx.x][0];
+        for (int w = 1; w < BT / 32; ++w) x = merge(x, red[threadIdx.x][w]);
+        partial[(blockIdx.x * 3 + threadIdx.x) * 2 + 0] = x.s;
+        partial[(blockIdx.x * 3 + threadIdx.x) * 2 + 1] = x.c;
+    }
+}
+
+__global__ void k_totals_final(const double *partial, int blocks, double scale, double *out) {
+    if (threadIdx.x >= 3) return;
+    Comp x{0, 0};
+    for (int b = 0; b < blocks; ++b)
+        x = merge(x, Comp{partial[(b * 3 + threadIdx.x) * 2], partial[(b * 3 + threadIdx.x) * 2 + 1]});
+    out[threadIdx.x] = (x.s + x.c) * scale;
+}
+
+}  // namespace
+
+int totals_blocks(int num_sms) { return num_sms * 4; }
+
+cudaError_t launch_totals(const void *h, const void *hu, const void *hv, const void *B, bool f32,
+                          int Nx, int Ny, long long pitch, double dxdy, double *partial,
+                          double *out, int num_sms, cudaStream_t s) {
+    const int blocks = totals_blocks(num_sms);
+    if (f32)
+        k_totals_partial<true><<<blocks, BT, 0, s>>>(h, hu, hv, B, Nx, Ny, pitch, partial);
+    else
+        k_totals_partial<false><<<blocks, BT, 0, s>>>(h, hu, hv, B, Nx, Ny, pitch, partial);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_totals_final<<<1, 32, 0, s>>>(partial, blocks, dxdy, out);
+    return cudaGetLastError();
+}
+
+}  // namespace swe

@@ -123,6 +123,13 @@ class Solver:
         self._check(self._lib.swe_dt_log(self._ctx, _dp(out), n, ctypes.byref(w)), "swe_dt_log")
         return out[: w.value]
 
+    def totals(self):
+        """(mass, momentum_x, momentum_y) of the current state: compensated device sums
+        of h, hu, hv over the interior times dx * dy."""
+        v = [ctypes.c_double() for _ in range(3)]
+        self._check(self._lib.swe_totals(self._ctx, *(ctypes.byref(x) for x in v)), "swe_totals")
+        return tuple(x.value for x in v)
+
     def kernel_launches(self) -> int:
         return int(self._lib.swe_kernel_launches(self._ctx))
 

@@ -148,3 +148,19 @@ def test_run_snapshots_match_oracle(gpu_lib, sw, port, problems):
     assert [n for n, _ in snaps] == [0, 10, 20, 30]
     ref = port.run(p, h, hu, hv, B, 30, (dt * 30) / 30.0)
     assert bitwise_equal(snaps[-1][1], ref[0])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32_mixed"])
+def test_totals_are_compensated_sums(gpu_lib, sw, problems, precision):
+    """swe_totals equals the exactly rounded sum (math.fsum) of the downloaded state."""
+    import math
+    h, hu, hv, B = problems.random_state(300, 257, seed=3, q_scale=0.2, b_scale=0.05)
+    with sw.Solver(300, 257, 1.0, 1.3, precision=precision) as s:
+        s.upload(h, hu, hv, B)
+        s.step(3)
+        mass, mx, my = s.totals()
+        out = s.download()
+    dxdy = (1.0 / 300) * (1.3 / 257)
+    for got, a in zip((mass, mx, my), out):
+        want = math.fsum(a[2:-2, 2:-2].ravel()) * dxdy
+        assert abs(got - want) <= 4e-16 * max(abs(want), math.fsum(np.abs(a[2:-2, 2:-2]).ravel()) * dxdy)
