@@ -131,6 +131,55 @@ long long swe_kernel_launches(const swe_ctx *ctx);
  * timers, HPC_solver.hpp:27-86, time the same loop on the host). */
 int swe_last_step_ms(const swe_ctx *ctx, double *ms);
 
+/* ---- Batched ensembles ---------------------------------------------------------------
+ * Many independent grids of uneven sizes advanced together: one launch per RK stage
+ * covers every instance (a flat work list of (instance, tile) pairs), each instance
+ * keeps its own CFL dt, max-speed reduction and time, and whole RK3 steps are replayed
+ * from CUDA graphs.  No reference counterpart (the reference runs one grid per process);
+ * each instance follows the single-grid semantics above. */
+
+typedef struct swe_ens swe_ens; /* opaque */
+
+/* Tile shapes (rows x columns) the ensemble kernels are compiled for.  FP64: 8x32, 8x16,
+ * 4x64.  FP32-mixed: 8x32, 16x32, 8x64. */
+enum { SWE_SHAPE_8x32 = 0, SWE_SHAPE_8x16 = 1, SWE_SHAPE_4x64 = 2, SWE_SHAPE_16x32 = 3,
+       SWE_SHAPE_8x64 = 4 };
+
+/* n instances with interior sizes Nx[q] x Ny[q] and domain sizes Lx[q] x Ly[q] (NULL:
+ * 1.0); g, cfl, bc, precision and device come from *base (its Nx, Ny, Lx, Ly are
+ * ignored). */
+int swe_ens_create(const swe_params *base, int n, const int *Nx, const int *Ny,
+                   const double *Lx, const double *Ly, swe_ens **out);
+void swe_ens_destroy(swe_ens *ens);
+
+/* Per-instance upload (state, bathymetry; resets the instance's time to 0) and download,
+ * with the single-grid layout of that instance. */
+int swe_ens_upload(swe_ens *ens, int instance, const double *h, const double *hu,
+                   const double *hv, const double *B);
+int swe_ens_download(swe_ens *ens, int instance, double *h, double *hu, double *hv);
+
+/* n_steps RK3 steps of every instance; dt > 0 fixed for all, dt <= 0 per-instance CFL. */
+int swe_ens_step(swe_ens *ens, int n_steps, double dt);
+
+/* Per-instance simulation times / dt of the last step (arrays of n doubles). */
+int swe_ens_times(swe_ens *ens, double *t);
+int swe_ens_last_dt(swe_ens *ens, double *dt);
+
+/* Device time of the last swe_ens_step call (CUDA events on the ensemble's stream). */
+int swe_ens_last_step_ms(const swe_ens *ens, double *ms);
+long long swe_ens_kernel_launches(const swe_ens *ens);
+
+/* Schedule: tile shape (SWE_SHAPE_*) and CTAs per launch (0: one CTA per tile). */
+int swe_ens_set_schedule(swe_ens *ens, int shape, int grid);
+int swe_ens_get_schedule(const swe_ens *ens, int *shape, int *grid, int *total_tiles);
+
+/* Autotuner: times every compiled tile shape with one CTA per tile and with 2, 4 and 8
+ * CTAs per SM, `steps` RK3 steps each, on the uploaded ensemble (the state is restored
+ * after every candidate), keeps the fastest and returns its ms per step. */
+int swe_ens_tune(swe_ens *ens, int steps, double *best_ms);
+
+const char *swe_ens_last_error(const swe_ens *ens);
+
 #ifdef __cplusplus
 }
 #endif

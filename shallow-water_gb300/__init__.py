@@ -9,5 +9,6 @@ ABI.  Import it with ``importlib.import_module("shallow-water_gb300")``.
 from . import problems  # noqa: F401
 from ._lib import lib  # noqa: F401
 from .solver import Solver, SweError  # noqa: F401
+from .ensemble import Ensemble  # noqa: F401
 
-__all__ = ["Solver", "SweError", "problems", "lib"]
+__all__ = ["Solver", "SweError", "Ensemble", "problems", "lib"]

@@ -30,7 +30,12 @@ EXPORTS = (
     "swe_params_default", "swe_create", "swe_destroy", "swe_upload", "swe_download",
     "swe_step", "swe_max_wave_speed", "swe_stable_dt", "swe_dt_log", "swe_last_error",
     "swe_status_string", "swe_kernel_launches", "swe_last_step_ms", "swe_totals",
+    "swe_ens_create", "swe_ens_destroy", "swe_ens_upload", "swe_ens_download", "swe_ens_step",
+    "swe_ens_times", "swe_ens_last_dt", "swe_ens_last_step_ms", "swe_ens_kernel_launches",
+    "swe_ens_set_schedule", "swe_ens_get_schedule", "swe_ens_tune", "swe_ens_last_error",
 )
+
+SHAPES = {"8x32": 0, "8x16": 1, "4x64": 2, "16x32": 3, "8x64": 4}
 
 
 class SweParams(ctypes.Structure):
@@ -92,5 +97,33 @@ def lib(path: str = LIB_PATH):
     L.swe_totals.restype = ctypes.c_int
     L.swe_last_step_ms.argtypes = [vp, dp]
     L.swe_last_step_ms.restype = ctypes.c_int
+    ip = ctypes.POINTER(ctypes.c_int)
+    L.swe_ens_create.argtypes = [ctypes.POINTER(SweParams), ctypes.c_int, ip, ip, dp, dp,
+                                 ctypes.POINTER(vp)]
+    L.swe_ens_create.restype = ctypes.c_int
+    L.swe_ens_destroy.argtypes = [vp]
+    L.swe_ens_destroy.restype = None
+    L.swe_ens_upload.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp]
+    L.swe_ens_upload.restype = ctypes.c_int
+    L.swe_ens_download.argtypes = [vp, ctypes.c_int, dp, dp, dp]
+    L.swe_ens_download.restype = ctypes.c_int
+    L.swe_ens_step.argtypes = [vp, ctypes.c_int, ctypes.c_double]
+    L.swe_ens_step.restype = ctypes.c_int
+    L.swe_ens_times.argtypes = [vp, dp]
+    L.swe_ens_times.restype = ctypes.c_int
+    L.swe_ens_last_dt.argtypes = [vp, dp]
+    L.swe_ens_last_dt.restype = ctypes.c_int
+    L.swe_ens_last_step_ms.argtypes = [vp, dp]
+    L.swe_ens_last_step_ms.restype = ctypes.c_int
+    L.swe_ens_kernel_launches.argtypes = [vp]
+    L.swe_ens_kernel_launches.restype = ctypes.c_longlong
+    L.swe_ens_set_schedule.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    L.swe_ens_set_schedule.restype = ctypes.c_int
+    L.swe_ens_get_schedule.argtypes = [vp, ip, ip, ip]
+    L.swe_ens_get_schedule.restype = ctypes.c_int
+    L.swe_ens_tune.argtypes = [vp, ctypes.c_int, dp]
+    L.swe_ens_tune.restype = ctypes.c_int
+    L.swe_ens_last_error.argtypes = [vp]
+    L.swe_ens_last_error.restype = ctypes.c_char_p
     _lib = L
     return L

@@ -23,6 +23,7 @@ UNITS = {
     "swe_fp64.cu": ["--fmad=false"],
     "swe_fp32.cu": [],
     "swe_reduce.cu": [],
+    "swe_ensemble.cu": [],
     "swe_api.cu": [],
 }
 

@@ -340,6 +340,10 @@ int swe_step(swe_ctx *c, int n_steps, double dt, double *t_inout) {
     sp.ky = pow2_exponent(c->inv_dy);
     sp.g = c->p.g;
     sp.half_g = 0.5 * c->p.g;
+    sp.gf = (float)sp.g;
+    sp.half_gf = (float)sp.half_g;
+    sp.inv_dxf = (float)sp.inv_dx;
+    sp.inv_dyf = (float)sp.inv_dy;
     sp.cfl_min_dxdy = c->cfl_min_dxdy;
     sp.dt_fixed = dt > 0.0 ? dt : 0.0;
     sp.speed = c->speed;

@@ -31,6 +31,7 @@ struct StageParams {
     int kx, ky;                  // log2 of inv_dx / inv_dy when a power of two, else 127
     double g;                    // gravity
     double half_g;               // 0.5 * g (exact)
+    float gf, half_gf, inv_dxf, inv_dyf;  // FP32 images for the FP32-mixed form
     double cfl_min_dxdy;         // cfl * min(dx, dy) (compute_stable_dt numerator)
     double dt_fixed;             // > 0: fixed dt; otherwise adaptive from speed slot
     unsigned long long *speed;   // two max-wave-speed slots (double bit patterns)
@@ -41,6 +42,82 @@ struct StageParams {
     int log_index;               // index into dt_log for this step
     int *flags;                  // FLAG_* bits
 };
+
+// Ensemble of independent grids (one per instance) in shared field pools.
+struct EnsInst {
+    long long off;            // element offset of the instance in every field pool
+    int Nx, Ny;
+    long long pitch;
+    int tiles_j;              // tiles along y for the launched tile shape
+    int tile_base;            // first global work-list index of the instance
+    double inv_dx, inv_dy;
+    int kx, ky;
+    float inv_dxf, inv_dyf;
+    double cfl_min_dxdy;
+};
+
+struct EnsParams {
+    const void *src[3];       // stage source pools (h or eta, hu, hv)
+    const void *n[3];         // U^n pools
+    void *out[3];             // output pools
+    const void *B;            // bathymetry pool
+    const EnsInst *inst;      // per instance
+    const int *tile_inst;     // work item -> instance
+    int total_tiles;
+    int bc;
+    double g, half_g;
+    float gf, half_gf;
+    double dt_fixed;          // > 0: all instances use it
+    unsigned long long *speed;  // 2 slots per instance
+    int slot_read, slot_write;
+    double *t;                // per-instance time
+    double *dt_last;          // per-instance dt of the last step
+    int *flags;
+    int elem;                 // element size (8: FP64, 4: FP32)
+};
+
+enum : int { SHAPE_8x32 = 0, SHAPE_8x16 = 1, SHAPE_4x64 = 2, SHAPE_16x32 = 3, SHAPE_8x64 = 4 };
+
+// StageParams of instance q inside an ensemble launch.
+__device__ __forceinline__ StageParams ens_view(const EnsParams &e, int q) {
+    const EnsInst &I = e.inst[q];
+    const long long off = I.off * e.elem;
+    StageParams p;
+    p.hs = static_cast<const char *>(e.src[0]) + off;
+    p.hus = static_cast<const char *>(e.src[1]) + off;
+    p.hvs = static_cast<const char *>(e.src[2]) + off;
+    p.hn = static_cast<const char *>(e.n[0]) + off;
+    p.hun = static_cast<const char *>(e.n[1]) + off;
+    p.hvn = static_cast<const char *>(e.n[2]) + off;
+    p.B = static_cast<const char *>(e.B) + off;
+    p.ho = static_cast<char *>(e.out[0]) + off;
+    p.huo = static_cast<char *>(e.out[1]) + off;
+    p.hvo = static_cast<char *>(e.out[2]) + off;
+    p.Nx = I.Nx;
+    p.Ny = I.Ny;
+    p.pitch = I.pitch;
+    p.bc = e.bc;
+    p.inv_dx = I.inv_dx;
+    p.inv_dy = I.inv_dy;
+    p.kx = I.kx;
+    p.ky = I.ky;
+    p.g = e.g;
+    p.half_g = e.half_g;
+    p.gf = e.gf;
+    p.half_gf = e.half_gf;
+    p.inv_dxf = I.inv_dxf;
+    p.inv_dyf = I.inv_dyf;
+    p.cfl_min_dxdy = I.cfl_min_dxdy;
+    p.dt_fixed = e.dt_fixed;
+    p.speed = e.speed + 2 * q;
+    p.slot_read = e.slot_read;
+    p.slot_write = e.slot_write;
+    p.t_accum = nullptr;
+    p.dt_log = nullptr;
+    p.log_index = 0;
+    p.flags = e.flags;
+    return p;
+}
 
 // Maps a possibly out-of-domain interior coordinate a (0-based, may be -2..N+1 or
 // beyond for partial tiles) to the interior cell whose value the ghost holds.

@@ -27,11 +27,6 @@
 namespace swe {
 namespace {
 
-constexpr int TI = 8;
-constexpr int TJ = 32;
-constexpr int NT = (TI + 1) * TJ;
-constexpr int RI = TI + 4;
-constexpr int RJ = TJ + 4;
 constexpr float EPSF = 1.0e-8f;
 constexpr float H_FLOORF = 1.0e-8f;
 
@@ -49,10 +44,9 @@ __device__ __forceinline__ float sqrt_approx(float x) {
     return y;
 }
 
+// minmod(a, b) = median(a, b, 0): three min/max, no branches.
 __device__ __forceinline__ float minmodf(float a, float b) {
-    if (a > 0.f && b > 0.f) return fminf(a, b);
-    if (a < 0.f && b < 0.f) return fmaxf(a, b);
-    return 0.f;
+    return fmaxf(fminf(a, b), fminf(fmaxf(a, b), 0.f));
 }
 
 struct FaceF {
@@ -86,30 +80,29 @@ __device__ __forceinline__ FaceF face_flux_f32(float g, float half_g, float e_m1
     const float aLn = qnL * un_m, aLt = qnL * ut_m;
     const float aRn = qnR * un_p, aRt = qnR * ut_p;
     const float cL = sqrt_approx(g * hs_m), cR = sqrt_approx(g * hs_p);
-    const float sL = fminf(un_m - cL, un_p - cR);
-    const float sR = fmaxf(un_m + cL, un_p + cR);
-    float Dh = 0.f, Dn = 0.f, Dt = 0.f;
-    if (!(sL >= 0.f)) {
-        const float dFh = qnR - qnL;
-        const float dFn = (aRn - aLn) + half_g * (hs_p - hs_m) * (hs_p + hs_m);
-        const float dFt = aRt - aLt;
-        if (sR <= 0.f) {
-            Dh = dFh;
-            Dn = dFn;
-            Dt = dFt;
-        } else {
-            const float k = sL * rcp_approx(sR - sL);
-            Dh = k * (sR * (hs_p - hs_m) - dFh);
-            Dn = k * (sR * (qnR - qnL) - dFn);
-            Dt = k * (sR * (qtR - qtL) - dFt);
-        }
-    }
+    // HLL with the wave speeds clamped to sL- = min(sL, 0), sR+ = max(sR, 0) covers the
+    // three regimes without branches: sL >= 0 gives D = 0 (F* = F_L), sR <= 0 gives
+    // D = dF (F* = F_R).  At a mirrored wall sL = -sR and k is exactly -1/2, so the wall
+    // mass flux cancels exactly.
+    const float sLm = fminf(fminf(un_m - cL, un_p - cR), 0.f);
+    const float sRp = fmaxf(fmaxf(un_m + cL, un_p + cR), 0.f);
+    const float den = sRp - sLm;
+    const float k = (sLm + sRp == 0.f) ? (den > 0.f ? -0.5f : 0.f)
+                                       : sLm * rcp_approx(fmaxf(den, 1e-30f));
+    const float dFh = qnR - qnL;
+    const float dFn = (aRn - aLn) + half_g * (hs_p - hs_m) * (hs_p + hs_m);
+    const float dFt = aRt - aLt;
+    const float Dh = k * (sRp * (hs_p - hs_m) - dFh);
+    const float Dn = k * (sRp * (qnR - qnL) - dFn);
+    const float Dt = k * (sRp * (qtR - qtL) - dFt);
+    // fqn_m = F*_n + g/2 (h_m^2 - hs_m^2) = aLn + Dn + g/2 h_m^2
+    // fqn_p = F*_n + g/2 (h_p^2 - hs_p^2) = aLn + Dn + g/2 (hs_m^2 - hs_p^2) + g/2 h_p^2
     FaceF f;
     f.fh = qnL + Dh;
     f.fqt = aLt + Dt;
     const float base = aLn + Dn;
     f.fqn_m = base + half_g * h_m * h_m;
-    f.fqn_p = base + half_g * h_p * h_p;
+    f.fqn_p = (base + half_g * (hs_m - hs_p) * (hs_m + hs_p)) + half_g * h_p * h_p;
     return f;
 }
 
@@ -134,21 +127,33 @@ __device__ __forceinline__ void block_max_to_slot_f(float v, unsigned long long 
     }
 }
 
+// The step's dt, computed once per block in FP64 and shared (an FP64 division per
+// thread would cost more than the whole FP32 stencil).
 __device__ __forceinline__ double stage_dt_f32(const StageParams &p) {
-    if (p.dt_fixed > 0.0) return p.dt_fixed;
-    const double ms = __longlong_as_double((long long)p.speed[p.slot_read]);
-    if (ms <= EPS) return 1.0e100;
-    return p.cfl_min_dxdy / ms;
+    __shared__ double s_dt;
+    if (threadIdx.x == 0) {
+        double dt = p.dt_fixed;
+        if (!(dt > 0.0)) {
+            const double ms = __longlong_as_double((long long)p.speed[p.slot_read]);
+            dt = (ms <= EPS) ? 1.0e100 : p.cfl_min_dxdy / ms;
+        }
+        s_dt = dt;
+    }
+    __syncthreads();
+    return s_dt;
 }
 
-template <int STAGE>
-__global__ void __launch_bounds__(NT) k_stage_f32(const StageParams p) {
+// One tile of one RK stage (see stage_tile_f64); returns the thread's cell wave speed of
+// the new state in stage 3, else 0.  (TI + 1) * TJ threads; dt is the block's dt.
+template <int TI, int TJ, int STAGE>
+__device__ __forceinline__ float stage_tile_f32(const StageParams &p, int i0, int j0,
+                                                double dtd) {
+    constexpr int NT = (TI + 1) * TJ, RI = TI + 4, RJ = TJ + 4;
     __shared__ float s_e[RI][RJ], s_u[RI][RJ], s_v[RI][RJ], s_b[RI][RJ];
     __shared__ float s_xf[4][TI + 1][TJ];
     __shared__ float s_yf[4][TI][TJ + 1];
 
     const int tid = threadIdx.x;
-    const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
     const long long P = p.pitch;
     const float *es = static_cast<const float *>(p.hs);
     const float *us = static_cast<const float *>(p.hus);
@@ -177,7 +182,7 @@ __global__ void __launch_bounds__(NT) k_stage_f32(const StageParams p) {
     }
     __syncthreads();
 
-    const float g = (float)p.g, half_g = (float)p.half_g;
+    const float g = p.gf, half_g = p.half_gf;
     {
         const int fr = tid / TJ, fc = tid - (tid / TJ) * TJ;
         const int a = fr + 1, c = fc + NG;
@@ -204,14 +209,13 @@ __global__ void __launch_bounds__(NT) k_stage_f32(const StageParams p) {
     }
     __syncthreads();
 
+    const float dt = (float)dtd;
     const int ty = tid / TJ, tx = tid - (tid / TJ) * TJ;
     const int ii = i0 + ty, jj = j0 + tx;
     const bool inside = (ty < TI) && (ii < p.Nx) && (jj < p.Ny);
-    const double dtd = stage_dt_f32(p);
-    const float dt = (float)dtd;
     float speed = 0.f;
     if (inside) {
-        const float idx = (float)p.inv_dx, idy = (float)p.inv_dy;
+        const float idx = p.inv_dxf, idy = p.inv_dyf;
         const float rh = -idx * (s_xf[0][ty + 1][tx] - s_xf[0][ty][tx]) -
                          idy * (s_yf[0][ty][tx + 1] - s_yf[0][ty][tx]);
         const float rhu = -idx * (s_xf[2][ty + 1][tx] - s_xf[3][ty][tx]) -
@@ -235,9 +239,12 @@ __global__ void __launch_bounds__(NT) k_stage_f32(const StageParams p) {
                 ou = 0.75f * nu + 0.25f * (su + dt * rhu);
                 ov = 0.75f * nv + 0.25f * (sv + dt * rhv);
             } else {
-                oe = (1.f / 3.f) * ne + (2.f / 3.f) * (se + dt * rh);
-                ou = (1.f / 3.f) * nu + (2.f / 3.f) * (su + dt * rhu);
-                ov = (1.f / 3.f) * nv + (2.f / 3.f) * (sv + dt * rhv);
+                // 1/3 n + 2/3 s' as n + c (s' - n): the FP32 weights fl(1/3) + fl(2/3)
+                // exceed 1 by 3e-8, which would add mass every step; these sum to 1.
+                const float c = 2.f / 3.f;
+                oe = ne + c * ((se + dt * rh) - ne);
+                ou = nu + c * ((su + dt * rhu) - nu);
+                ov = nv + c * ((sv + dt * rhv) - nv);
             }
         }
         if (oe - b < H_FLOORF) {  // enforce_positivity on h = eta - B
@@ -245,19 +252,51 @@ __global__ void __launch_bounds__(NT) k_stage_f32(const StageParams p) {
             ou = 0.f;
             ov = 0.f;
         }
-        if (!isfinite(oe) || !isfinite(ou) || !isfinite(ov)) atomicOr(p.flags, FLAG_NONFINITE);
+        if (!(fabsf(oe) + fabsf(ou) + fabsf(ov) < INFINITY)) atomicOr(p.flags, FLAG_NONFINITE);
         static_cast<float *>(p.ho)[k] = oe;
         static_cast<float *>(p.huo)[k] = ou;
         static_cast<float *>(p.hvo)[k] = ov;
         if (STAGE == 3) speed = cell_speed_f32(g, oe - b, ou, ov);
     }
-    if (STAGE == 1 && blockIdx.x == 0 && blockIdx.y == 0 && tid == 0) {
+    return speed;
+}
+
+template <int TI, int TJ, int STAGE>
+__global__ void __launch_bounds__((TI + 1) * TJ) k_stage_f32(const StageParams p) {
+    const double dtd = stage_dt_f32(p);
+    const float dt = (float)dtd;
+    const float speed = stage_tile_f32<TI, TJ, STAGE>(p, blockIdx.y * TI, blockIdx.x * TJ, dtd);
+    if (STAGE == 1 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
         p.speed[p.slot_write] = 0ull;
         if (p.dt_log) p.dt_log[p.log_index] = (double)dt;
     }
     if (STAGE == 3) {
         block_max_to_slot_f(speed, p.speed + p.slot_write);
-        if (blockIdx.x == 0 && blockIdx.y == 0 && tid == 0 && p.t_accum) *p.t_accum += (double)dt;
+        if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && p.t_accum)
+            *p.t_accum += (double)dt;
+    }
+}
+
+template <int TI, int TJ, int STAGE>
+__global__ void __launch_bounds__((TI + 1) * TJ) k_ens_stage_f32(const EnsParams e) {
+    for (int T = blockIdx.x; T < e.total_tiles; T += gridDim.x) {
+        const int q = e.tile_inst[T];
+        const StageParams p = ens_view(e, q);
+        const EnsInst &I = e.inst[q];
+        const int t = T - I.tile_base;
+        const int ti = t / I.tiles_j, tj = t - (t / I.tiles_j) * I.tiles_j;
+        const double dtd = stage_dt_f32(p);
+        const float dt = (float)dtd;
+        const float speed = stage_tile_f32<TI, TJ, STAGE>(p, ti * TI, tj * TJ, dtd);
+        if (STAGE == 1 && t == 0 && threadIdx.x == 0) {
+            p.speed[p.slot_write] = 0ull;
+            if (e.dt_last) e.dt_last[q] = (double)dt;
+        }
+        if (STAGE == 3) {
+            block_max_to_slot_f(speed, p.speed + p.slot_write);
+            if (t == 0 && threadIdx.x == 0) e.t[q] += (double)dt;
+        }
+        __syncthreads();  // the next tile reuses the shared tile buffers
     }
 }
 
@@ -340,13 +379,35 @@ unsigned grid_for(long long n, int num_sms) {
 }  // namespace
 
 cudaError_t launch_stage_f32(int stage, const StageParams &p, cudaStream_t s) {
+    constexpr int TI = 8, TJ = 32, NT = (TI + 1) * TJ;
     const dim3 grid((p.Ny + TJ - 1) / TJ, (p.Nx + TI - 1) / TI);
     switch (stage) {
-        case 1: k_stage_f32<1><<<grid, NT, 0, s>>>(p); break;
-        case 2: k_stage_f32<2><<<grid, NT, 0, s>>>(p); break;
-        default: k_stage_f32<3><<<grid, NT, 0, s>>>(p); break;
+        case 1: k_stage_f32<TI, TJ, 1><<<grid, NT, 0, s>>>(p); break;
+        case 2: k_stage_f32<TI, TJ, 2><<<grid, NT, 0, s>>>(p); break;
+        default: k_stage_f32<TI, TJ, 3><<<grid, NT, 0, s>>>(p); break;
     }
     return cudaGetLastError();
+}
+
+template <int TI, int TJ>
+static cudaError_t ens_launch_f32(int stage, const EnsParams &e, int grid, cudaStream_t s) {
+    constexpr int NT = (TI + 1) * TJ;
+    switch (stage) {
+        case 1: k_ens_stage_f32<TI, TJ, 1><<<grid, NT, 0, s>>>(e); break;
+        case 2: k_ens_stage_f32<TI, TJ, 2><<<grid, NT, 0, s>>>(e); break;
+        default: k_ens_stage_f32<TI, TJ, 3><<<grid, NT, 0, s>>>(e); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ens_stage_f32(int shape, int stage, const EnsParams &e, int grid,
+                                 cudaStream_t s) {
+    switch (shape) {
+        case SHAPE_8x32: return ens_launch_f32<8, 32>(stage, e, grid, s);
+        case SHAPE_16x32: return ens_launch_f32<16, 32>(stage, e, grid, s);
+        case SHAPE_8x64: return ens_launch_f32<8, 64>(stage, e, grid, s);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_max_speed_f32(const void *e, const void *hu, const void *hv, const void *B,

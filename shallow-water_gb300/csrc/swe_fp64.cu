@@ -26,11 +26,8 @@
 namespace swe {
 namespace {
 
-constexpr int TI = 8;    // tile rows (x)
-constexpr int TJ = 32;   // tile columns (y, contiguous)
-constexpr int NT = (TI + 1) * TJ;  // one thread per x-face; covers TI*(TJ+1) y-faces too
-constexpr int RI = TI + 4;  // staged rows incl. halo
-constexpr int RJ = TJ + 4;  // staged columns incl. halo
+// Tile shapes are template parameters: TI rows (x) by TJ columns (y, contiguous),
+// (TI + 1) * TJ threads, one per x-face (which also covers the TI * (TJ + 1) y-faces).
 
 using x64::dmax;
 using x64::dmin;
@@ -155,22 +152,36 @@ __device__ __forceinline__ void block_max_to_slot(double v, unsigned long long *
     }
 }
 
+// The step's dt (compute_stable_dt, HPC_kernels.hpp:296-297, on the max speed reduced by
+// the previous step), computed once per block and shared.
 __device__ __forceinline__ double stage_dt(const StageParams &p) {
-    if (p.dt_fixed > 0.0) return p.dt_fixed;
-    const double ms = __longlong_as_double((long long)p.speed[p.slot_read]);
-    if (x64::le(ms, EPS)) return 1.0e100;  // compute_stable_dt, HPC_kernels.hpp:296
-    return p.cfl_min_dxdy / ms;
+    __shared__ double s_dt;
+    if (threadIdx.x == 0) {
+        double dt = p.dt_fixed;
+        if (!(dt > 0.0)) {
+            const double ms = __longlong_as_double((long long)p.speed[p.slot_read]);
+            dt = x64::le(ms, EPS) ? 1.0e100 : p.cfl_min_dxdy / ms;
+        }
+        s_dt = dt;
+    }
+    __syncthreads();
+    return s_dt;
 }
 
-template <int STAGE>
-__global__ void __launch_bounds__(NT) k_stage_f64(const StageParams p) {
+// One tile of one RK stage: stage the TI x TJ tile (origin i0, j0 in interior
+// coordinates) plus a 2-cell halo, compute its interfaces, and update its cells.
+// Returns the thread's cell wave speed of the new state (stage 3), else 0.
+// (TI + 1) * TJ threads; the caller provides dt (same for the whole block).
+template <int TI, int TJ, int STAGE>
+__device__ __forceinline__ double stage_tile_f64(const StageParams &p, int i0, int j0,
+                                                 double dt) {
+    constexpr int NT = (TI + 1) * TJ, RI = TI + 4, RJ = TJ + 4;
+    static_assert(TI * (TJ + 1) <= NT, "one thread per y-face");
     __shared__ double s_h[RI][RJ], s_hu[RI][RJ], s_hv[RI][RJ], s_B[RI][RJ], s_eta[RI][RJ];
     __shared__ double s_xf[4][TI + 1][TJ];  // fh, fhv, fhu_m, fhu_p
     __shared__ double s_yf[4][TI][TJ + 1];  // gh, ghu, ghv_m, ghv_p
 
     const int tid = threadIdx.x;
-    const int i0 = blockIdx.y * TI;  // interior coordinates of the tile origin
-    const int j0 = blockIdx.x * TJ;
     const long long P = p.pitch;
     const double *hs = static_cast<const double *>(p.hs);
     const double *hus = static_cast<const double *>(p.hus);
@@ -230,7 +241,6 @@ __global__ void __launch_bounds__(NT) k_stage_f64(const StageParams p) {
     const int ty = tid / TJ, tx = tid - (tid / TJ) * TJ;
     const int ii = i0 + ty, jj = j0 + tx;
     const bool inside = (ty < TI) && (ii < p.Nx) && (jj < p.Ny);
-    const double dt = stage_dt(p);
     double speed = 0.0;
     if (inside) {
         // apply_divergence (HPC_kernels.hpp:274-276): right/top face minus-side
@@ -280,13 +290,47 @@ __global__ void __launch_bounds__(NT) k_stage_f64(const StageParams p) {
         static_cast<double *>(p.hvo)[k] = ohv;
         if (STAGE == 3) speed = cell_speed(g, oh, ohu, ohv);
     }
-    if (STAGE == 1 && blockIdx.x == 0 && blockIdx.y == 0 && tid == 0) {
+    return speed;
+}
+
+// Single grid: one CTA per tile.
+template <int TI, int TJ, int STAGE>
+__global__ void __launch_bounds__((TI + 1) * TJ) k_stage_f64(const StageParams p) {
+    const double dt = stage_dt(p);
+    const double speed = stage_tile_f64<TI, TJ, STAGE>(p, blockIdx.y * TI, blockIdx.x * TJ, dt);
+    if (STAGE == 1 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
         p.speed[p.slot_write] = 0ull;  // read by nobody until stage 3 of this step
         if (p.dt_log) p.dt_log[p.log_index] = dt;
     }
     if (STAGE == 3) {
         block_max_to_slot(speed, p.speed + p.slot_write);
-        if (blockIdx.x == 0 && blockIdx.y == 0 && tid == 0 && p.t_accum) *p.t_accum += dt;
+        if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && p.t_accum)
+            *p.t_accum += dt;
+    }
+}
+
+// Ensemble: CTAs stride over a flat list of (instance, tile) work items; every tile
+// costs the same, so static striding balances.  Each instance has its own dt, max-speed
+// slots and time (per-instance CFL).
+template <int TI, int TJ, int STAGE>
+__global__ void __launch_bounds__((TI + 1) * TJ) k_ens_stage_f64(const EnsParams e) {
+    for (int T = blockIdx.x; T < e.total_tiles; T += gridDim.x) {
+        const int q = e.tile_inst[T];
+        const StageParams p = ens_view(e, q);
+        const EnsInst &I = e.inst[q];
+        const int t = T - I.tile_base;
+        const int ti = t / I.tiles_j, tj = t - (t / I.tiles_j) * I.tiles_j;
+        const double dt = stage_dt(p);
+        const double speed = stage_tile_f64<TI, TJ, STAGE>(p, ti * TI, tj * TJ, dt);
+        if (STAGE == 1 && t == 0 && threadIdx.x == 0) {
+            p.speed[p.slot_write] = 0ull;
+            if (e.dt_last) e.dt_last[q] = dt;
+        }
+        if (STAGE == 3) {
+            block_max_to_slot(speed, p.speed + p.slot_write);
+            if (t == 0 && threadIdx.x == 0) e.t[q] += dt;
+        }
+        __syncthreads();  // the next tile reuses the shared tile buffers
     }
 }
 
@@ -340,13 +384,35 @@ __global__ void k_fill_ghosts_f64(double *h, double *hu, double *hv, int Nx, int
 }  // namespace
 
 cudaError_t launch_stage_f64(int stage, const StageParams &p, cudaStream_t s) {
+    constexpr int TI = 8, TJ = 32, NT = (TI + 1) * TJ;
     const dim3 grid((p.Ny + TJ - 1) / TJ, (p.Nx + TI - 1) / TI);
     switch (stage) {
-        case 1: k_stage_f64<1><<<grid, NT, 0, s>>>(p); break;
-        case 2: k_stage_f64<2><<<grid, NT, 0, s>>>(p); break;
-        default: k_stage_f64<3><<<grid, NT, 0, s>>>(p); break;
+        case 1: k_stage_f64<TI, TJ, 1><<<grid, NT, 0, s>>>(p); break;
+        case 2: k_stage_f64<TI, TJ, 2><<<grid, NT, 0, s>>>(p); break;
+        default: k_stage_f64<TI, TJ, 3><<<grid, NT, 0, s>>>(p); break;
     }
     return cudaGetLastError();
+}
+
+template <int TI, int TJ>
+static cudaError_t ens_launch_f64(int stage, const EnsParams &e, int grid, cudaStream_t s) {
+    constexpr int NT = (TI + 1) * TJ;
+    switch (stage) {
+        case 1: k_ens_stage_f64<TI, TJ, 1><<<grid, NT, 0, s>>>(e); break;
+        case 2: k_ens_stage_f64<TI, TJ, 2><<<grid, NT, 0, s>>>(e); break;
+        default: k_ens_stage_f64<TI, TJ, 3><<<grid, NT, 0, s>>>(e); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ens_stage_f64(int shape, int stage, const EnsParams &e, int grid,
+                                 cudaStream_t s) {
+    switch (shape) {
+        case SHAPE_8x32: return ens_launch_f64<8, 32>(stage, e, grid, s);
+        case SHAPE_8x16: return ens_launch_f64<8, 16>(stage, e, grid, s);
+        case SHAPE_4x64: return ens_launch_f64<4, 64>(stage, e, grid, s);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_max_speed_f64(const void *h, const void *hu, const void *hv, int Nx, int Ny,

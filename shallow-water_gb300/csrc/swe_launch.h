@@ -9,6 +9,9 @@ namespace swe {
 
 // FP64 drop-in (swe_fp64.cu, compiled with --fmad=false).
 cudaError_t launch_stage_f64(int stage, const StageParams &p, cudaStream_t s);
+// Ensemble stage over the work list; shape is SHAPE_* (8x32, 8x16, 4x64 for FP64).
+cudaError_t launch_ens_stage_f64(int shape, int stage, const EnsParams &e, int grid,
+                                 cudaStream_t s);
 cudaError_t launch_max_speed_f64(const void *h, const void *hu, const void *hv, int Nx, int Ny,
                                  long long pitch, double g, unsigned long long *slot,
                                  int num_sms, cudaStream_t s);
@@ -17,6 +20,9 @@ cudaError_t launch_fill_ghosts_f64(void *h, void *hu, void *hv, int Nx, int Ny, 
 
 // FP32-mixed form (swe_fp32.cu): state (eta = h + B, hu, hv) and B in FP32.
 cudaError_t launch_stage_f32(int stage, const StageParams &p, cudaStream_t s);
+// Ensemble stage (FP32-mixed); shape is SHAPE_8x32, SHAPE_16x32 or SHAPE_8x64.
+cudaError_t launch_ens_stage_f32(int shape, int stage, const EnsParams &e, int grid,
+                                 cudaStream_t s);
 cudaError_t launch_max_speed_f32(const void *e, const void *hu, const void *hv, const void *B,
                                  int Nx, int Ny, long long pitch, double g,
                                  unsigned long long *slot, int num_sms, cudaStream_t s);

@@ -125,3 +125,35 @@ def random_state(Nx, Ny, seed=0, h_range=(0.5, 1.5), q_scale=0.3, b_scale=0.2, d
         hu[m] *= 1e-8
         hv[m] *= 1e-8
     return h, hu, hv, B
+
+
+def ensemble_instances(count=512, sizes=(128, 256, 512, 1024, 2048), seed=0):
+    """The batched-ensemble workload: ``count`` square instances with side drawn uniformly
+    from ``sizes``; each has its own Gaussian hump on eta = 1 (amplitude U[0.05, 0.3],
+    centre U[0.2, 0.8]^2, width^2 U[0.002, 0.02]) over a bathymetry of 4 seeded
+    Gaussians (centres U[0,1]^2, widths U[0.05, 0.15], amplitudes U[-0.2, 0.2]), u = v = 0,
+    reflecting walls (bathymetry ghosts mirrored).
+
+    Returns a list of (N, seed_q) pairs; :func:`ensemble_member` builds one member's
+    arrays on demand so a 512-member ensemble never sits on the host all at once.
+    """
+    rng = np.random.default_rng(seed)
+    sides = rng.choice(np.asarray(sizes), size=count)
+    seeds = rng.integers(0, 2**31 - 1, size=count)
+    return [(int(n), int(s)) for n, s in zip(sides, seeds)]
+
+
+def ensemble_member(N, seed):
+    """(h, hu, hv, B) of one ensemble member (see :func:`ensemble_instances`)."""
+    rng = np.random.default_rng(seed)
+    amp = rng.uniform(0.05, 0.3)
+    cx, cy = rng.uniform(0.2, 0.8, size=2)
+    w2 = rng.uniform(0.002, 0.02)
+    B, _ = gaussian_sum_bathymetry(N, N, n=4, rng=rng, width=(0.05, 0.15), amp=(-0.2, 0.2),
+                                   bc="reflecting")
+    x = centres(N)[:, None]
+    y = centres(N)[None, :]
+    eta = 1.0 + amp * np.exp(-((x - cx) ** 2 + (y - cy) ** 2) / w2)
+    h = np.maximum(0.0, eta - B)
+    z = np.zeros_like(h)
+    return np.ascontiguousarray(h), z.copy(), z.copy(), B
