@@ -113,6 +113,35 @@ int swe_stable_dt(swe_ctx *ctx, double *out);
  * (tests/sanity_checks/mass_conservation.hpp:45-56); this is the device-side twin. */
 int swe_totals(swe_ctx *ctx, double *mass, double *momentum_x, double *momentum_y);
 
+/* Capacity, in partial-sum blocks, of the fixed scratch used by swe_totals_noalloc. */
+#define SWE_TOTALS_NOALLOC_MAX_BLOCKS 1024
+
+/* swe_totals without any allocation, for callers that cannot call cudaMalloc: a host
+ * whose device memory all belongs to its own allocator (a framework's caching
+ * allocator, a pool sized at start-up), or a time-critical loop that must not stall on
+ * cudaMalloc, which can synchronise the device.  No counterpart in the reference.
+ *
+ * It takes the caller's device arrays instead of a context: h (eta for the FP32-mixed
+ * form), hu, hv and, for that form, B, in this library's device layout (ghosted
+ * (Nx + 4) x pitch rows, elements of the precision's type), and writes
+ * (sum h, sum hu, sum hv) * dxdy to out, three doubles in device memory.  It runs on
+ * `stream` (a cudaStream_t; NULL is the default stream) with the device that holds the
+ * arrays current, and returns without waiting.  The result equals swe_totals for the
+ * same state and block count.
+ *
+ * Scratch: the per-block partial sums go to one fixed device array of
+ * SWE_TOTALS_NOALLOC_MAX_BLOCKS * 6 doubles (48 KiB) inside the library, which every GPU
+ * that loads the library holds until the process exits.  `blocks` partial blocks are
+ * used (0: four per SM, capped at the capacity); more than SWE_TOTALS_NOALLOC_MAX_BLOCKS
+ * returns SWE_ERR_BAD_ARG.  Each block's entries are written before they are read, so
+ * the array needs no clearing between calls.  All calls on a device share the one array:
+ * calls that overlap on the GPU (other streams, other host threads) race and must be
+ * serialised by the caller.  The first call on each device looks up the array's
+ * address (cudaGetSymbolAddress); make that first call before any stream capture. */
+int swe_totals_noalloc(const void *h, const void *hu, const void *hv, const void *B,
+                       int precision, int Nx, int Ny, long long pitch, double dxdy, int blocks,
+                       double *out, void *stream);
+
 /* Copies the dt of each step of the last swe_step call (up to n values) to out and
  * returns how many were written in *written. */
 int swe_dt_log(swe_ctx *ctx, double *out, int n, int *written);

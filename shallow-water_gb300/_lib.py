@@ -33,7 +33,9 @@ EXPORTS = (
     "swe_ens_create", "swe_ens_destroy", "swe_ens_upload", "swe_ens_download", "swe_ens_step",
     "swe_ens_times", "swe_ens_last_dt", "swe_ens_last_step_ms", "swe_ens_kernel_launches",
     "swe_ens_set_schedule", "swe_ens_get_schedule", "swe_ens_tune", "swe_ens_last_error",
+    "swe_totals_noalloc",
 )
+TOTALS_NOALLOC_MAX_BLOCKS = 1024
 
 SHAPES = {"8x32": 0, "8x16": 1, "4x64": 2, "16x32": 3, "8x64": 4}
 
@@ -123,6 +125,9 @@ def lib(path: str = LIB_PATH):
     L.swe_ens_get_schedule.restype = ctypes.c_int
     L.swe_ens_tune.argtypes = [vp, ctypes.c_int, dp]
     L.swe_ens_tune.restype = ctypes.c_int
+    L.swe_totals_noalloc.argtypes = [vp, vp, vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_longlong, ctypes.c_double, ctypes.c_int, vp, vp]
+    L.swe_totals_noalloc.restype = ctypes.c_int
     L.swe_ens_last_error.argtypes = [vp]
     L.swe_ens_last_error.restype = ctypes.c_char_p
     _lib = L

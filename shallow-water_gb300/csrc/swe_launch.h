@@ -36,6 +36,9 @@ cudaError_t launch_fill_ghosts_f32(void *e, void *hu, void *hv, const void *B, i
 // Compensated totals (swe_reduce.cu): out[0..2] = (sum h, sum hu, sum hv) * dxdy.
 // partial needs 6 * totals_blocks(num_sms) doubles.
 int totals_blocks(int num_sms);
+cudaError_t launch_totals_blocks(const void *h, const void *hu, const void *hv, const void *B,
+                                 bool f32, int Nx, int Ny, long long pitch, double dxdy,
+                                 double *partial, double *out, int blocks, cudaStream_t s);
 cudaError_t launch_totals(const void *h, const void *hu, const void *hv, const void *B, bool f32,
                           int Nx, int Ny, long long pitch, double dxdy, double *partial,
                           double *out, int num_sms, cudaStream_t s);

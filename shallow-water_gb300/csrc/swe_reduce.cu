@@ -7,6 +7,10 @@
 // TwoSum; a second one-block kernel adds the per-block pairs in block order.  The
 // result is deterministic (fixed assignment and order) and accurate to about one
 // rounding of the total.  Works on both forms (FP32 eta - B is exact in FP64).
+#include <algorithm>
+#include <mutex>
+
+#include "../../include/swe_gb300.h"
 #include "swe_common.cuh"
 #include "swe_launch.h"
 
@@ -97,6 +101,19 @@ __global__ void k_totals_final(const double *partial, int blocks, double scale, 
 
 int totals_blocks(int num_sms) { return num_sms * 4; }
 
+cudaError_t launch_totals_blocks(const void *h, const void *hu, const void *hv, const void *B,
+                                 bool f32, int Nx, int Ny, long long pitch, double dxdy,
+                                 double *partial, double *out, int blocks, cudaStream_t s) {
+    if (f32)
+        k_totals_partial<true><<<blocks, BT, 0, s>>>(h, hu, hv, B, Nx, Ny, pitch, partial);
+    else
+        k_totals_partial<false><<<blocks, BT, 0, s>>>(h, hu, hv, B, Nx, Ny, pitch, partial);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_totals_final<<<1, 32, 0, s>>>(partial, blocks, dxdy, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_totals(const void *h, const void *hu, const void *hv, const void *B, bool f32,
                           int Nx, int Ny, long long pitch, double dxdy, double *partial,
                           double *out, int num_sms, cudaStream_t s) {
@@ -112,3 +129,63 @@ cudaError_t launch_totals(const void *h, const void *hu, const void *hv, const v
 }
 
 }  // namespace swe
+
+// ---- Allocation-free variant ------------------------------------------------------------
+//
+// Scratch for swe_totals_noalloc: the per-block compensated partial sums (6 doubles per
+// block) and nothing else.  A file-scope device array, so the entry point never calls
+// cudaMalloc; every GPU that loads this library holds it (48 KiB) until the process exits.
+// In host code the name is only a stand-in for the device copy: its device address comes
+// from cudaGetSymbolAddress, taken once per device with that device current.
+static __device__ __align__(256) double g_totals_noalloc_scratch[6 * SWE_TOTALS_NOALLOC_MAX_BLOCKS];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double *g_noalloc_ptr[kMaxDevices] = {};
+
+// Address of this device's copy of the scratch array (set-up on first use per device).
+int noalloc_scratch(int device, double **out) {
+    if (device < 0 || device >= kMaxDevices) return SWE_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device]) {
+        void *ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_totals_noalloc_scratch);
+        if (e != cudaSuccess || !ptr) {
+            cudaGetLastError();
+            return SWE_ERR_CUDA;
+        }
+        g_noalloc_ptr[device] = static_cast<double *>(ptr);
+    }
+    *out = g_noalloc_ptr[device];
+    return SWE_OK;
+}
+
+}  // namespace
+
+extern "C" int swe_totals_noalloc(const void *h, const void *hu, const void *hv, const void *B,
+                                  int precision, int Nx, int Ny, long long pitch, double dxdy,
+                                  int blocks, double *out, void *stream) {
+    using namespace swe;
+    const bool f32 = precision == SWE_PRECISION_FP32_MIXED;
+    if (!h || !hu || !hv || !out || (f32 && !B)) return SWE_ERR_BAD_ARG;
+    if (precision != SWE_PRECISION_FP64 && !f32) return SWE_ERR_BAD_ARG;
+    if (Nx < 1 || Ny < 1 || pitch < (long long)Ny + 4 || blocks < 0) return SWE_ERR_BAD_ARG;
+    int device = 0, sms = 0;
+    if (cudaGetDevice(&device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+        cudaGetLastError();
+        return SWE_ERR_NO_DEVICE;
+    }
+    if (blocks == 0) blocks = std::min(totals_blocks(sms), SWE_TOTALS_NOALLOC_MAX_BLOCKS);
+    if (blocks > SWE_TOTALS_NOALLOC_MAX_BLOCKS) return SWE_ERR_BAD_ARG;  // beyond the scratch
+    double *scratch = nullptr;
+    const int st = noalloc_scratch(device, &scratch);
+    if (st != SWE_OK) return st;
+    const cudaError_t e =
+        launch_totals_blocks(h, hu, hv, B, f32, Nx, Ny, pitch, dxdy, scratch, out, blocks,
+                             static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? SWE_OK : SWE_ERR_CUDA;
+}
+
