@@ -1,0 +1,278 @@
+// Reverse-mode (vector-Jacobian product) of one interface of the scheme.
+//
+// Forward: the interface of compute_x_fluxes / compute_y_fluxes
+// (HPC_kernels.hpp:136-184, 203-251) in normal/tangential form.  Inputs are the 4-cell
+// stencil (m1, c0 | p1, p2) of eta = h + B, the normal momentum qn and the tangential
+// momentum qt, and B of the two adjacent cells.  Outputs are the mass flux fh, the
+// tangential flux fqt, and the normal-momentum flux seen by the minus cell (with
+// corr_minus) and by the plus cell (with corr_plus).
+//
+// The VJP takes adjoints of the four outputs and returns adjoints of the 14 inputs.
+// Branches (minmod, positive parts, dry guards, HLL regimes, min/max of the wave speeds)
+// take the derivative of the branch the forward pass took, which is the discrete adjoint
+// of the scheme as executed.  Templated on the scalar type so the same code runs on the
+// host (finite-difference tests) and on the device in FP64 and FP32.
+#pragma once
+
+#include <cmath>
+
+#if defined(__CUDACC__)
+#define SWE_HD __host__ __device__ __forceinline__
+#else
+#define SWE_HD inline
+#endif
+
+namespace swe {
+namespace adj {
+
+template <class T>
+struct FaceIn {
+    T e[4], n[4], t[4];  // eta, qn, qt at m1, c0, p1, p2
+    T bm, bp;            // B at c0 and p1
+};
+
+template <class T>
+struct FaceOut {
+    T fh, fqt, fqn_m, fqn_p;
+};
+
+template <class T>
+SWE_HD T tmin(T a, T b) { return (b < a) ? b : a; }
+template <class T>
+SWE_HD T tmax(T a, T b) { return (a < b) ? b : a; }
+template <class T>
+SWE_HD T tabs(T a) { return a < T(0) ? -a : a; }
+
+// minmod value and which argument it selected (0: none / zero, 1: a, 2: b).
+template <class T>
+SWE_HD T minmod_sel(T a, T b, int &sel) {
+    if (a * b <= T(0)) {
+        sel = 0;
+        return T(0);
+    }
+    if (tabs(b) < tabs(a)) {
+        sel = 2;
+        return b;
+    }
+    sel = 1;
+    return a;
+}
+
+template <class T>
+SWE_HD void face_forward(const FaceIn<T> &in, T g, T eps, FaceOut<T> &out) {
+    const T half = T(0.5);
+    int s;
+    const T eta_m = in.e[1] + half * minmod_sel(in.e[1] - in.e[0], in.e[2] - in.e[1], s);
+    const T eta_p = in.e[2] - half * minmod_sel(in.e[2] - in.e[1], in.e[3] - in.e[2], s);
+    const T qn_m = in.n[1] + half * minmod_sel(in.n[1] - in.n[0], in.n[2] - in.n[1], s);
+    const T qt_m = in.t[1] + half * minmod_sel(in.t[1] - in.t[0], in.t[2] - in.t[1], s);
+    const T qn_p = in.n[2] - half * minmod_sel(in.n[2] - in.n[1], in.n[3] - in.n[2], s);
+    const T qt_p = in.t[2] - half * minmod_sel(in.t[2] - in.t[1], in.t[3] - in.t[2], s);
+    const T bs = tmax(in.bm, in.bp);
+    const T h_m = tmax(eta_m - in.bm, T(0)), h_p = tmax(eta_p - in.bp, T(0));
+    const T un_m = h_m > eps ? qn_m / h_m : T(0), ut_m = h_m > eps ? qt_m / h_m : T(0);
+    const T un_p = h_p > eps ? qn_p / h_p : T(0), ut_p = h_p > eps ? qt_p / h_p : T(0);
+    const T hL = tmax(eta_m - bs, T(0)), hR = tmax(eta_p - bs, T(0));
+    const T qnL = hL * un_m, qtL = hL * ut_m, qnR = hR * un_p, qtR = hR * ut_p;
+    const T unL = hL > eps ? qnL / hL : T(0), utL = hL > eps ? qtL / hL : T(0);
+    const T unR = hR > eps ? qnR / hR : T(0), utR = hR > eps ? qtR / hR : T(0);
+    const T cL = sqrt(g * hL), cR = sqrt(g * hR);
+    const T sL = tmin(unL - cL, unR - cR), sR = tmax(unL + cL, unR + cR);
+    const T FL[3] = {qnL, qnL * unL + half * g * hL * hL, qnL * utL};
+    const T FR[3] = {qnR, qnR * unR + half * g * hR * hR, qnR * utR};
+    const T UL[3] = {hL, qnL, qtL}, UR[3] = {hR, qnR, qtR};
+    T F[3];
+    if (sL >= T(0)) {
+        for (int c = 0; c < 3; ++c) F[c] = FL[c];
+    } else if (sR <= T(0)) {
+        for (int c = 0; c < 3; ++c) F[c] = FR[c];
+    } else {
+        const T inv = T(1) / (sR - sL);
+        for (int c = 0; c < 3; ++c) F[c] = (sR * FL[c] - sL * FR[c] + sL * sR * (UR[c] - UL[c])) * inv;
+    }
+    out.fh = F[0];
+    out.fqt = F[2];
+    out.fqn_m = F[1] + half * g * (h_m * h_m - hL * hL);
+    out.fqn_p = F[1] + half * g * (h_p * h_p - hR * hR);
+}
+
+// Adjoint of face_forward: given d = dJ/d(out), returns a = dJ/d(in) (overwritten).
+template <class T>
+SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceIn<T> &a) {
+    const T half = T(0.5);
+    // ---- forward recomputation, keeping branch decisions ----
+    int s_em, s_ep, s_nm, s_tm, s_np, s_tp;
+    const T de0 = in.e[1] - in.e[0], de1 = in.e[2] - in.e[1], de2 = in.e[3] - in.e[2];
+    const T dn0 = in.n[1] - in.n[0], dn1 = in.n[2] - in.n[1], dn2 = in.n[3] - in.n[2];
+    const T dt0 = in.t[1] - in.t[0], dt1 = in.t[2] - in.t[1], dt2 = in.t[3] - in.t[2];
+    const T eta_m = in.e[1] + half * minmod_sel(de0, de1, s_em);
+    const T eta_p = in.e[2] - half * minmod_sel(de1, de2, s_ep);
+    const T qn_m = in.n[1] + half * minmod_sel(dn0, dn1, s_nm);
+    const T qt_m = in.t[1] + half * minmod_sel(dt0, dt1, s_tm);
+    const T qn_p = in.n[2] - half * minmod_sel(dn1, dn2, s_np);
+    const T qt_p = in.t[2] - half * minmod_sel(dt1, dt2, s_tp);
+    const bool bstar_is_p = in.bm < in.bp;  // std::max(bm, bp) == (bm < bp) ? bp : bm
+    const T bs = bstar_is_p ? in.bp : in.bm;
+    const T xm = eta_m - in.bm, xp = eta_p - in.bp;
+    const bool pm = xm > T(0), pp = xp > T(0);
+    const T h_m = pm ? xm : T(0), h_p = pp ? xp : T(0);
+    const bool wm = h_m > eps, wp = h_p > eps;
+    const T un_m = wm ? qn_m / h_m : T(0), ut_m = wm ? qt_m / h_m : T(0);
+    const T un_p = wp ? qn_p / h_p : T(0), ut_p = wp ? qt_p / h_p : T(0);
+    const T yL = eta_m - bs, yR = eta_p - bs;
+    const bool pL = yL > T(0), pR = yR > T(0);
+    const T hL = pL ? yL : T(0), hR = pR ? yR : T(0);
+    const T qnL = hL * un_m, qtL = hL * ut_m, qnR = hR * un_p, qtR = hR * ut_p;
+    const bool wL = hL > eps, wR = hR > eps;
+    const T unL = wL ? qnL / hL : T(0), utL = wL ? qtL / hL : T(0);
+    const T unR = wR ? qnR / hR : T(0), utR = wR ? qtR / hR : T(0);
+    const T cL = sqrt(g * hL), cR = sqrt(g * hR);
+    const T a1 = unL - cL, a2 = unR - cR, b1 = unL + cL, b2 = unR + cR;
+    const bool sL_is2 = a2 < a1, sR_is2 = b1 < b2;
+    const T sL = sL_is2 ? a2 : a1, sR = sR_is2 ? b2 : b1;
+    const T FL[3] = {qnL, qnL * unL + half * g * hL * hL, qnL * utL};
+    const T FR[3] = {qnR, qnR * unR + half * g * hR * hR, qnR * utR};
+    const T UL[3] = {hL, qnL, qtL}, UR[3] = {hR, qnR, qtR};
+    const int regime = (sL >= T(0)) ? 0 : ((sR <= T(0)) ? 1 : 2);
+
+    // ---- reverse sweep ----
+    // outputs -> F, corrections
+    const T dF[3] = {d.fh, d.fqn_m + d.fqn_p, d.fqt};
+    T dh_m = g * h_m * d.fqn_m, dh_p = g * h_p * d.fqn_p;
+    T dhL = -g * hL * d.fqn_m, dhR = -g * hR * d.fqn_p;
+    // HLL
+    T dFL[3] = {0, 0, 0}, dFR[3] = {0, 0, 0}, dUL[3] = {0, 0, 0}, dUR[3] = {0, 0, 0};
+    T dsL = 0, dsR = 0;
+    if (regime == 0) {
+        for (int c = 0; c < 3; ++c) dFL[c] = dF[c];
+    } else if (regime == 1) {
+        for (int c = 0; c < 3; ++c) dFR[c] = dF[c];
+    } else {
+        const T inv = T(1) / (sR - sL);
+        for (int c = 0; c < 3; ++c) {
+            const T F = (sR * FL[c] - sL * FR[c] + sL * sR * (UR[c] - UL[c])) * inv;
+            const T dU = UR[c] - UL[c];
+            dFL[c] = dF[c] * sR * inv;
+            dFR[c] = -dF[c] * sL * inv;
+            dUR[c] = dF[c] * sL * sR * inv;
+            dUL[c] = -dUR[c];
+            dsR += dF[c] * ((FL[c] + sL * dU) - F) * inv;
+            dsL += dF[c] * ((-FR[c] + sR * dU) + F) * inv;
+        }
+    }
+    // speeds
+    T dunL = 0, dunR = 0, dcL = 0, dcR = 0;
+    if (sL_is2) {
+        dunR += dsL;
+        dcR -= dsL;
+    } else {
+        dunL += dsL;
+        dcL -= dsL;
+    }
+    if (sR_is2) {
+        dunR += dsR;
+        dcR += dsR;
+    } else {
+        dunL += dsR;
+        dcL += dsR;
+    }
+    if (cL > T(0)) dhL += dcL * g / (T(2) * cL);
+    if (cR > T(0)) dhR += dcR * g / (T(2) * cR);
+    // physical fluxes FL = (qnL, qnL unL + g/2 hL^2, qnL utL); U = (h, qn, qt)
+    T dqnL = dFL[0] + dFL[1] * unL + dFL[2] * utL + dUL[1];
+    T dqtL = dUL[2];
+    dunL += dFL[1] * qnL;
+    T dutL = dFL[2] * qnL;
+    dhL += dFL[1] * g * hL + dUL[0];
+    T dqnR = dFR[0] + dFR[1] * unR + dFR[2] * utR + dUR[1];
+    T dqtR = dUR[2];
+    dunR += dFR[1] * qnR;
+    T dutR = dFR[2] * qnR;
+    dhR += dFR[1] * g * hR + dUR[0];
+    // unL = qnL / hL (wet)
+    if (wL) {
+        dqnL += dunL / hL;
+        dqtL += dutL / hL;
+        dhL -= (dunL * unL + dutL * utL) / hL;
+    }
+    if (wR) {
+        dqnR += dunR / hR;
+        dqtR += dutR / hR;
+        dhR -= (dunR * unR + dutR * utR) / hR;
+    }
+    // qnL = hL un_m, ...
+    dhL += dqnL * un_m + dqtL * ut_m;
+    dhR += dqnR * un_p + dqtR * ut_p;
+    T dun_m = dqnL * hL, dut_m = dqtL * hL, dun_p = dqnR * hR, dut_p = dqtR * hR;
+    // hL = max(eta_m - bs, 0)
+    T deta_m = 0, deta_p = 0, dbs = 0;
+    if (pL) {
+        deta_m += dhL;
+        dbs -= dhL;
+    }
+    if (pR) {
+        deta_p += dhR;
+        dbs -= dhR;
+    }
+    // un_m = qn_m / h_m (wet)
+    T dqn_m = 0, dqt_m = 0, dqn_p = 0, dqt_p = 0;
+    if (wm) {
+        dqn_m += dun_m / h_m;
+        dqt_m += dut_m / h_m;
+        dh_m -= (dun_m * un_m + dut_m * ut_m) / h_m;
+    }
+    if (wp) {
+        dqn_p += dun_p / h_p;
+        dqt_p += dut_p / h_p;
+        dh_p -= (dun_p * un_p + dut_p * ut_p) / h_p;
+    }
+    // h_m = max(eta_m - bm, 0)
+    T dbm = 0, dbp = 0;
+    if (pm) {
+        deta_m += dh_m;
+        dbm -= dh_m;
+    }
+    if (pp) {
+        deta_p += dh_p;
+        dbp -= dh_p;
+    }
+    if (bstar_is_p)
+        dbp += dbs;
+    else
+        dbm += dbs;
+    // reconstructions: x_m = x1 + m(x1-x0, x2-x1)/2, x_p = x2 - m(x2-x1, x3-x2)/2
+    for (int k = 0; k < 4; ++k) a.e[k] = a.n[k] = a.t[k] = T(0);
+    auto recon_m = [&](T *ax, T dxm, int sel) {  // minus: first arg x1-x0, second x2-x1
+        ax[1] += dxm;
+        const T dm = half * dxm;
+        if (sel == 1) {
+            ax[1] += dm;
+            ax[0] -= dm;
+        } else if (sel == 2) {
+            ax[2] += dm;
+            ax[1] -= dm;
+        }
+    };
+    auto recon_p = [&](T *ax, T dxp, int sel) {  // plus: first arg x2-x1, second x3-x2
+        ax[2] += dxp;
+        const T dm = -half * dxp;
+        if (sel == 1) {
+            ax[2] += dm;
+            ax[1] -= dm;
+        } else if (sel == 2) {
+            ax[3] += dm;
+            ax[2] -= dm;
+        }
+    };
+    recon_m(a.e, deta_m, s_em);
+    recon_p(a.e, deta_p, s_ep);
+    recon_m(a.n, dqn_m, s_nm);
+    recon_p(a.n, dqn_p, s_np);
+    recon_m(a.t, dqt_m, s_tm);
+    recon_p(a.t, dqt_p, s_tp);
+    a.bm = dbm;
+    a.bp = dbp;
+}
+
+}  // namespace adj
+}  // namespace swe

@@ -41,6 +41,7 @@ struct StageParams {
     double *dt_log;              // optional per-step dt record
     int log_index;               // index into dt_log for this step
     int *flags;                  // FLAG_* bits
+    unsigned char *mask;         // optional: 1 where positivity clamped the cell (adjoint)
 };
 
 // Ensemble of independent grids (one per instance) in shared field pools.
@@ -116,6 +117,7 @@ __device__ __forceinline__ StageParams ens_view(const EnsParams &e, int q) {
     p.dt_log = nullptr;
     p.log_index = 0;
     p.flags = e.flags;
+    p.mask = nullptr;
     return p;
 }
 

@@ -1,0 +1,39 @@
+// Internal definition of the single-grid context (swe_ctx in include/swe_gb300.h),
+// shared by the C ABI (swe_api.cu) and the adjoint driver (swe_adjoint.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/swe_gb300.h"
+
+struct swe_ctx {
+    swe_params p{};
+    cudaStream_t stream = nullptr;
+    int num_sms = 0;
+    long long pitch = 0;       // device row pitch, elements
+    size_t field_elems = 0;    // (Nx + 4) * pitch
+    void *base = nullptr;      // single device allocation
+    void *Un[3]{}, *U1[3]{}, *U2[3]{}, *B = nullptr;
+    void *stage64[2]{};        // FP32 form: FP64 staging (B as given, scratch) in device layout
+    double *partial = nullptr; // totals: per-block compensated pairs, then the 3 results
+    unsigned long long *speed = nullptr;  // [2]
+    double *t_accum = nullptr;
+    int *flags = nullptr;
+    double *dt_log = nullptr;
+    int dt_log_cap = 0;
+    int last_steps = 0;
+    long long steps_done = 0;  // selects the speed slot parity
+    bool uploaded = false;
+    double dx = 0, dy = 0, inv_dx = 0, inv_dy = 0, cfl_min_dxdy = 0;
+    long long launches = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // bracket the stage launches of swe_step
+    double last_ms = 0.0;
+    std::string err;
+};
+
+namespace swe {
+// k with x == 2^k when x is a normal power of two with |k| <= 64, else 127.
+int pow2_exponent(double x);
+}  // namespace swe

@@ -276,11 +276,13 @@ __device__ __forceinline__ double stage_tile_f64(const StageParams &p, int i0, i
             }
         }
         // enforce_positivity (HPC_kernels.hpp:305-312)
-        if (x64::lt(oh, H_FLOOR)) {
+        const bool clamped = x64::lt(oh, H_FLOOR);
+        if (clamped) {
             oh = H_FLOOR;
             ohu = 0.0;
             ohv = 0.0;
         }
+        if (p.mask) p.mask[k] = clamped ? 1 : 0;
         if (((x64::bits(oh) & x64::ABS) >= x64::INF_BITS) ||
             ((x64::bits(ohu) & x64::ABS) >= x64::INF_BITS) ||
             ((x64::bits(ohv) & x64::ABS) >= x64::INF_BITS))
