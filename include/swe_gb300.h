@@ -160,6 +160,22 @@ long long swe_kernel_launches(const swe_ctx *ctx);
  * timers, HPC_solver.hpp:27-86, time the same loop on the host). */
 int swe_last_step_ms(const swe_ctx *ctx, double *ms);
 
+/* ---- Discrete adjoint ------------------------------------------------------------------
+ * Gradient of the gauge misfit J = sum over steps n = 1..n_steps and gauges q of
+ * (h^n(gauge_i[q], gauge_j[q]) - h_obs[(n - 1) * n_gauges + q])^2 for a run of n_steps
+ * fixed-dt steps from the context's current state (left unchanged), through a
+ * hand-written discrete adjoint of each RK stage (the derivative of the branches the
+ * forward pass takes: minmod, HLL regime, dry guards, positivity clamps).  States are
+ * recomputed from n_snapshots stored states on a binomial (optimal offline) checkpoint
+ * schedule.  Outputs, in the ghosted host layout with zero ghosts: J, dJ/dh^0,
+ * dJ/dhu^0, dJ/dhv^0 and dJ/dB with the initial state held fixed, where the ghosts of B
+ * are taken to follow the wall rule (mirror or copy of the interior).  ms (optional)
+ * receives the device time.  FP64 contexts only.  No reference counterpart. */
+int swe_adjoint_gauge(swe_ctx *ctx, int n_steps, double dt, int n_gauges, const int *gauge_i,
+                      const int *gauge_j, const double *h_obs, int n_snapshots, double *J,
+                      double *grad_h, double *grad_hu, double *grad_hv, double *grad_B,
+                      double *ms);
+
 /* ---- Batched ensembles ---------------------------------------------------------------
  * Many independent grids of uneven sizes advanced together: one launch per RK stage
  * covers every instance (a flat work list of (instance, tile) pairs), each instance

@@ -10,5 +10,6 @@ from . import problems  # noqa: F401
 from ._lib import lib  # noqa: F401
 from .solver import Solver, SweError  # noqa: F401
 from .ensemble import Ensemble  # noqa: F401
+from . import adjoint  # noqa: F401
 
-__all__ = ["Solver", "SweError", "Ensemble", "problems", "lib"]
+__all__ = ["Solver", "SweError", "Ensemble", "adjoint", "problems", "lib"]

@@ -24,6 +24,7 @@ UNITS = {
     "swe_fp32.cu": [],
     "swe_reduce.cu": [],
     "swe_ensemble.cu": [],
+    "swe_adjoint.cu": [],
     "swe_api.cu": [],
 }
 

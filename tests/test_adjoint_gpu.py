@@ -1,0 +1,132 @@
+"""GPU discrete adjoint (swe_adjoint_gauge) against (a) the CPU reference adjoint of
+tests/cpp/adjoint_ref.cpp, (b) central finite differences (eps = 1e-6) of the CPU oracle
+(the reference's algorithm) along random smooth directions, relative agreement 1e-6,
+(c) itself under every checkpoint budget (bitwise), and (d) through the
+torch.autograd.Function."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from test_adjoint_cpu import smooth_case, smooth_direction
+
+pytestmark = pytest.mark.gpu
+
+FD_REL = 1e-6
+
+
+def setup(problems, Nx, Ny, bc, steps, seed):
+    h, hu, hv, B, rng = smooth_case(problems, Nx, Ny, bc, seed)
+    ng = 7
+    gauges = np.stack([rng.integers(0, Nx, ng), rng.integers(0, Ny, ng)], axis=1)
+    obs = 1.0 + 0.01 * rng.standard_normal((steps, ng))
+    return h, hu, hv, B, gauges, obs, rng
+
+
+def oracle_J(port, p, h, hu, hv, B, steps, dt, gauges, obs):
+    """J from the CPU oracle, one step at a time."""
+    a = [np.array(x, copy=True) for x in (h, hu, hv)]
+    ws = port.Workspace(p)
+    J = 0.0
+    for n in range(steps):
+        _, _, st = ws.run_inplace(a[0], a[1], a[2], B, 1, dt)
+        assert st == 0
+        r = a[0][gauges[:, 0] + 2, gauges[:, 1] + 2] - obs[n]
+        J += float((r * r).sum())
+    ws.close()
+    return J
+
+
+def gpu_adjoint(sw, h, hu, hv, B, Nx, Ny, steps, dt, gauges, obs, bc, snapshots=None):
+    with sw.Solver(Nx, Ny, bc=bc) as s:
+        s.upload(h, hu, hv, B)
+        r = sw.adjoint.gauge_misfit_gradient(s, steps, dt, gauges, obs, snapshots)
+        out = s.download()
+    r["state_after"] = out
+    return r
+
+
+@pytest.mark.parametrize("bc", [0, 1], ids=["reflecting", "transmissive"])
+def test_gpu_adjoint_matches_cpu_reference_adjoint(gpu_lib, sw, problems, bc):
+    import adjref
+    Nx, Ny, steps, dt = 24, 20, 10, 1e-3
+    h, hu, hv, B, gauges, obs, _ = setup(problems, Nx, Ny, bc, steps, seed=3 + bc)
+    r = gpu_adjoint(sw, h, hu, hv, B, Nx, Ny, steps, dt, gauges, obs, bc)
+    J, gh, ghu, ghv, gB = adjref.run(Nx, Ny, h, hu, hv, B, steps, dt, gauges[:, 0],
+                                     gauges[:, 1], obs, bc=bc)
+    assert abs(r["J"] - J) <= 1e-12 * abs(J)
+    for got, want in zip((r["grad_h"], r["grad_hu"], r["grad_hv"], r["grad_B"]),
+                         (gh, ghu, ghv, gB)):
+        scale = np.abs(want[2:-2, 2:-2]).max()
+        assert np.abs(got[2:-2, 2:-2] - want[2:-2, 2:-2]).max() <= 1e-11 * scale
+    # the context's state is left as uploaded
+    assert np.array_equal(r["state_after"][0][2:-2, 2:-2], h[2:-2, 2:-2])
+
+
+@pytest.mark.parametrize("bc", [0, 1], ids=["reflecting", "transmissive"])
+def test_gpu_adjoint_matches_oracle_finite_differences(gpu_lib, sw, port, problems, bc):
+    Nx, Ny, steps, dt = 32, 28, 16, 1e-3
+    h, hu, hv, B, gauges, obs, rng = setup(problems, Nx, Ny, bc, steps, seed=11 + bc)
+    r = gpu_adjoint(sw, h, hu, hv, B, Nx, Ny, steps, dt, gauges, obs, bc)
+    p = port.grid(Nx, Ny, bc=bc)
+    J0 = oracle_J(port, p, h, hu, hv, B, steps, dt, gauges, obs)
+    assert abs(r["J"] - J0) <= 1e-12 * abs(J0)
+    bcs = "reflecting" if bc == 0 else "transmissive"
+    eps = 1e-6
+    for trial in range(4):
+        d = [smooth_direction(problems, Nx, Ny, rng) for _ in range(4)]
+        dB = d[3].copy()
+        problems.fill_scalar_ghosts(dB, bcs)
+
+        def J_at(s):
+            return oracle_J(port, p, h + s * d[0], hu + s * d[1], hv + s * d[2], B + s * dB,
+                            steps, dt, gauges, obs)
+
+        fd = (J_at(eps) - J_at(-eps)) / (2 * eps)
+        ad = sum(float((g[2:-2, 2:-2] * x[2:-2, 2:-2]).sum()) for g, x in
+                 zip((r["grad_h"], r["grad_hu"], r["grad_hv"], r["grad_B"]), d))
+        assert abs(fd - ad) <= FD_REL * abs(fd), (trial, fd, ad)
+
+
+def test_checkpoint_budget_does_not_change_the_gradient(gpu_lib, sw, problems):
+    Nx, Ny, steps, dt = 20, 16, 13, 1e-3
+    h, hu, hv, B, gauges, obs, _ = setup(problems, Nx, Ny, 0, steps, seed=23)
+    base = gpu_adjoint(sw, h, hu, hv, B, Nx, Ny, steps, dt, gauges, obs, 0, snapshots=steps)
+    for snaps in (0, 1, 2, 4):
+        r = gpu_adjoint(sw, h, hu, hv, B, Nx, Ny, steps, dt, gauges, obs, 0, snapshots=snaps)
+        assert r["J"] == base["J"]
+        for k in ("grad_h", "grad_hu", "grad_hv", "grad_B"):
+            assert np.array_equal(r[k], base[k]), (snaps, k)
+
+
+def test_autograd_function_gradients(gpu_lib, sw, port, problems):
+    import torch
+    Nx, Ny, steps, dt = 24, 24, 12, 1e-3
+    rng = np.random.default_rng(5)
+    Bg, _ = problems.gaussian_sum_bathymetry(Nx, Ny, n=4, rng=rng, width=(0.15, 0.3),
+                                             amp=(-0.1, 0.1))
+    B = Bg[2:-2, 2:-2] + 1e-3 * rng.standard_normal((Nx, Ny))
+    x = problems.centres(Nx)[2:-2, None]
+    y = problems.centres(Ny)[None, 2:-2]
+    eta0 = 1.0 + 0.03 * np.exp(-((x - 0.5) ** 2 + (y - 0.45) ** 2) / 0.03)
+    eta0 = eta0 + 1e-3 * rng.standard_normal((Nx, Ny))
+    gauges = np.stack([rng.integers(0, Nx, 6), rng.integers(0, Ny, 6)], axis=1)
+    obs = 1.0 + 0.01 * rng.standard_normal((steps, 6))
+    te = torch.tensor(eta0, requires_grad=True)
+    tb = torch.tensor(B, requires_grad=True)
+    J = sw.adjoint.GaugeMisfit.apply(te, tb, steps, dt, gauges, obs)
+    J.backward()
+    p = port.grid(Nx, Ny)
+
+    def J_np(e, b):
+        h, hu, hv, Bg2 = sw.adjoint.ghosted_state(e, b)
+        return oracle_J(port, p, h, hu, hv, Bg2, steps, dt, gauges, obs)
+
+    assert abs(J.item() - J_np(eta0, B)) <= 1e-12 * J.item()
+    eps = 1e-6
+    for trial in range(3):
+        de = smooth_direction(problems, Nx, Ny, rng)[2:-2, 2:-2]
+        db = smooth_direction(problems, Nx, Ny, rng)[2:-2, 2:-2]
+        fd = (J_np(eta0 + eps * de, B + eps * db) - J_np(eta0 - eps * de, B - eps * db)) / (2 * eps)
+        ad = float((te.grad.numpy() * de).sum() + (tb.grad.numpy() * db).sum())
+        assert abs(fd - ad) <= FD_REL * abs(fd), (trial, fd, ad)
