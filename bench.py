@@ -50,6 +50,14 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU work of the cpu_baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the FP32-mixed, ensemble and adjoint measurements")
+    ap.add_argument("--fp32-n", type=int, default=16384)
+    ap.add_argument("--ens-count", type=int, default=64)
+    ap.add_argument("--adj-n", type=int, default=1024)
+    ap.add_argument("--adj-steps", type=int, default=200)
+    ap.add_argument("--acc-n", type=int, default=2048)
+    ap.add_argument("--acc-steps", type=int, default=500)
     ap.add_argument("--seed", type=int, default=2026)
     return ap.parse_args()
 
@@ -181,6 +189,130 @@ def time_cpu_port(h, hu, hv, B, n, steps, warmup):
     return dt
 
 
+def rel_l1(a, b):
+    ai, bi = a[2:-2, 2:-2], b[2:-2, 2:-2]
+    return float(np.abs(ai - bi).sum() / max(np.abs(bi).sum(), 1e-300))
+
+
+def rel_linf(a, b):
+    ai, bi = a[2:-2, 2:-2], b[2:-2, 2:-2]
+    return float(np.abs(ai - bi).max() / max(np.abs(bi).max(), 1e-300))
+
+
+def form_fp32(args, sw, fp64_gcups):
+    """FP32-mixed throughput on the large grid, and its error against an FP64 GPU run of
+    the same dam break on a grid small enough to run in seconds."""
+    n = args.fp32_n
+    h, hu, hv, B = workload(n, args.seed)
+    with sw.Solver(n, n, bc="transmissive", precision="fp32_mixed") as s:
+        s.upload(h, hu, hv, B)
+        s.step(3)
+        s.step(max(args.steps, 10))
+        ms = s.last_step_ms() / max(args.steps, 10)
+    del h, hu, hv, B
+    gcups = n * n / (ms / 1e3) / 1e9
+    out = {"grid": [n, n], "ms_per_step": ms, "gcups": gcups,
+           "hbm_frac_of_measured": 108 * n * n / (ms / 1e3) / 1e9 / peaks()[0],
+           "bytes_per_cell_update": 108, "speedup_vs_fp64": gcups / fp64_gcups}
+    m, K = args.acc_n, args.acc_steps
+    h, hu, hv, B = workload(m, args.seed)
+    with sw.Solver(m, m, bc="transmissive") as s64, \
+            sw.Solver(m, m, bc="transmissive", precision="fp32_mixed") as s32:
+        s64.upload(h, hu, hv, B)
+        s32.upload(h, hu, hv, B)
+        s64.step(K)
+        s32.step(K)
+        a, b = s64.download(), s32.download()
+        m0 = s64.totals()
+        out["accuracy_vs_fp64"] = {
+            "grid": [m, m], "steps": K, "dt": "adaptive, each form its own",
+            "l1_h": rel_l1(b[0], a[0]), "linf_h": rel_linf(b[0], a[0]),
+            "l1_hu": rel_l1(b[1], a[1]), "l1_hv": rel_l1(b[2], a[2]),
+            "t_fp64": s64.time, "t_fp32": s32.time, "mass_fp64": m0[0]}
+    Bl, _ = importlib.import_module("shallow-water_gb300.problems").gaussian_sum_bathymetry(
+        m, m, n=16, seed=args.seed, bc="transmissive")
+    P = importlib.import_module("shallow-water_gb300.problems")
+    hl, hul, hvl = P.lake_at_rest(Bl, 1.0)
+    with sw.Solver(m, m, bc="transmissive", precision="fp32_mixed") as s:
+        s.upload(hl, hul, hvl, Bl)
+        s.step(200, 0.5 * s.stable_dt())
+        l = s.download()
+        wet = hl[2:-2, 2:-2] > 1e-3
+        out["lake_at_rest"] = {"grid": [m, m], "steps": 200,
+                               "max_abs_hu_hv_wet": float(max(np.abs(l[1][2:-2, 2:-2][wet]).max(),
+                                                              np.abs(l[2][2:-2, 2:-2][wet]).max())),
+                               "dry_cells": int((~wet).sum())}
+    return out
+
+
+def form_ensemble(args, sw):
+    """Batched ensemble with the size and initial-condition distribution of the
+    512-instance workload, `ens_count` members, tuned schedule, FP64 and FP32-mixed."""
+    P = importlib.import_module("shallow-water_gb300.problems")
+    specs = P.ensemble_instances(count=args.ens_count, seed=args.seed)
+    sizes = [(n, n) for n, _ in specs]
+    cells = float(sum(n * n for n, _ in specs))
+    res = {"instances": len(specs), "cells": cells,
+           "sides": sorted({n for n, _ in specs})}
+    members = [P.ensemble_member(n, sd) for n, sd in specs]
+    for prec in ("fp64", "fp32_mixed"):
+        with sw.Ensemble(sizes, precision=prec) as ens:
+            for q, mbr in enumerate(members):
+                ens.upload(q, *mbr)
+            tune = ens.tune(steps=1)
+            steps = 3 if prec == "fp64" else 20
+            ens.step(1)
+            ens.step(steps)
+            ms = ens.last_step_ms() / steps
+            bpc = 216 if prec == "fp64" else 108
+            res[prec] = {"ms_per_step": ms, "gcups": cells / (ms / 1e3) / 1e9,
+                         "hbm_frac_of_measured": bpc * cells / (ms / 1e3) / 1e9 / peaks()[0],
+                         "schedule": {"shape": tune["shape"], "grid": tune["grid"]},
+                         "launches_per_step": 3, "graph_replay": True}
+    return res
+
+
+def form_adjoint(args, sw):
+    """Adjoint/forward cost on the 1024^2 adjoint workload (seeded bathymetry, 8 seeded
+    surface bumps, 64 gauges), fixed dt, binomial checkpointing with ~sqrt(steps) states."""
+    P = importlib.import_module("shallow-water_gb300.problems")
+    n, K = args.adj_n, args.adj_steps
+    rng = np.random.default_rng(args.seed + 7)
+    B, _ = P.gaussian_sum_bathymetry(n, n, n=16, rng=rng, bc="reflecting")
+    bumps, _ = P.gaussian_sum_bathymetry(n, n, n=8, rng=rng, width=(0.02, 0.1),
+                                         amp=(-0.05, 0.05), bc="reflecting")
+    eta0 = 1.0 + bumps
+    h = np.maximum(0.0, eta0 - B)
+    z = np.zeros_like(h)
+    gauges = np.stack([rng.integers(0, n, 64), rng.integers(0, n, 64)], axis=1)
+    obs = h[gauges[:, 0] + 2, gauges[:, 1] + 2][None, :] + 1e-3 * rng.standard_normal((K, 64))
+    snaps = max(1, int(round(np.sqrt(K))))
+    with sw.Solver(n, n) as s:
+        s.upload(h, z, z, B)
+        dt = 0.5 * s.stable_dt()
+        s.step(K, dt)
+        fwd_ms = s.last_step_ms()
+        s.upload(h, z, z, B)
+        r = sw.adjoint.gauge_misfit_gradient(s, K, dt, gauges, obs, snaps)
+        r_all = sw.adjoint.gauge_misfit_gradient(s, K, dt, gauges, obs, K)
+    return {"grid": [n, n], "steps": K, "gauges": 64, "snapshots": snaps,
+            "forward_ms": fwd_ms, "adjoint_ms": r["ms"], "ratio": r["ms"] / fwd_ms,
+            "adjoint_ms_all_states_stored": r_all["ms"],
+            "ratio_all_states_stored": r_all["ms"] / fwd_ms}
+
+
+def run_forms(args, sw, fp64_gcups):
+    forms = {}
+    for name, fn in (("fp32_mixed", lambda: form_fp32(args, sw, fp64_gcups)),
+                     ("ensemble", lambda: form_ensemble(args, sw)),
+                     ("adjoint", lambda: form_adjoint(args, sw))):
+        try:
+            forms[name] = fn()
+        except Exception as exc:  # keep the headline line whatever an extra does
+            forms[name] = {"error": f"{type(exc).__name__}: {exc}"}
+    return forms
+
+
 def run_reference(args, dist: Dist):
     if dist.rank != 0:
         return
@@ -291,6 +423,8 @@ def run_gb300(args, dist: Dist):
             "kind": "port",
             "sample": f"{n}^2 workload from t=0, {s_cpu} full RK3 steps, C restatement of "
                       "HPC_solver/omp_solver (oracle/swe_oracle.c), OpenMP on all host threads"}
+    if dist.rank == 0 and dist.world == 1 and not args.no_forms:
+        line["forms"] = run_forms(args, sw, value)
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -66,7 +66,7 @@ def test_full_adjoint_matches_finite_differences(problems, bc):
     obs = 1.0 + 0.01 * rng.standard_normal((steps, ng))
     J, gh, ghu, ghv, gB = adjref.run(Nx, Ny, h, hu, hv, B, steps, dt, gi, gj, obs, bc=bc)
     bcs = "reflecting" if bc == 0 else "transmissive"
-    eps = 1e-6
+    eps = 1e-7  # see tests/test_adjoint_gpu.py on kinks of the scheme
     for trial in range(4):
         dirs = [smooth_direction(problems, Nx, Ny, rng) for _ in range(4)]
         dB = dirs[3].copy()

@@ -1,8 +1,16 @@
 """GPU discrete adjoint (swe_adjoint_gauge) against (a) the CPU reference adjoint of
-tests/cpp/adjoint_ref.cpp, (b) central finite differences (eps = 1e-6) of the CPU oracle
-(the reference's algorithm) along random smooth directions, relative agreement 1e-6,
+tests/cpp/adjoint_ref.cpp, (b) central finite differences of the CPU oracle (the
+reference's algorithm) along random smooth directions, relative agreement 1e-6,
 (c) itself under every checkpoint budget (bitwise), and (d) through the
-torch.autograd.Function."""
+torch.autograd.Function.
+
+The scheme is only piecewise smooth: minmod switches between its slopes wherever they
+are equal in magnitude (inflection lines), and max(b-, b+) and the HLL wave-speed min/max
+switch too, so J has kinks at every scale.  A central difference straddles some of them
+with a probability proportional to eps: at eps = 1e-6 the agreement is about 1e-6 in the
+median and 3e-5 at worst on these cases, at eps = 1e-7 about 1e-7.  The checks use
+eps = 1e-7 against the 1e-6 bar; rounding noise in J stays near 1e-10 relative there.
+"""
 from __future__ import annotations
 
 import numpy as np
@@ -13,6 +21,7 @@ from test_adjoint_cpu import smooth_case, smooth_direction
 pytestmark = pytest.mark.gpu
 
 FD_REL = 1e-6
+FD_EPS = 1e-7
 
 
 def setup(problems, Nx, Ny, bc, steps, seed):
@@ -72,7 +81,7 @@ def test_gpu_adjoint_matches_oracle_finite_differences(gpu_lib, sw, port, proble
     J0 = oracle_J(port, p, h, hu, hv, B, steps, dt, gauges, obs)
     assert abs(r["J"] - J0) <= 1e-12 * abs(J0)
     bcs = "reflecting" if bc == 0 else "transmissive"
-    eps = 1e-6
+    eps = FD_EPS
     for trial in range(4):
         d = [smooth_direction(problems, Nx, Ny, rng) for _ in range(4)]
         dB = d[3].copy()
@@ -123,7 +132,7 @@ def test_autograd_function_gradients(gpu_lib, sw, port, problems):
         return oracle_J(port, p, h, hu, hv, Bg2, steps, dt, gauges, obs)
 
     assert abs(J.item() - J_np(eta0, B)) <= 1e-12 * J.item()
-    eps = 1e-6
+    eps = FD_EPS
     for trial in range(3):
         de = smooth_direction(problems, Nx, Ny, rng)[2:-2, 2:-2]
         db = smooth_direction(problems, Nx, Ny, rng)[2:-2, 2:-2]
