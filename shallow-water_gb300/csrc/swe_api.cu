@@ -5,11 +5,13 @@
 // and an error-flag word, all in one allocation.  Every call runs on the context's
 // own stream and synchronises before returning; no exception crosses the boundary.
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -54,6 +56,30 @@ int set_device(swe_ctx *c) {
 
 }  // namespace
 
+bool swe::encode_tile_map_f32(CUtensorMap *m, const void *base, int rows, int cols,
+                              long long pitch, int box_rows, int box_cols) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                             cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn) {
+            cudaGetLastError();
+            return false;
+        }
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float)};
+    const cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(base), dims, strides,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // k with x == 2^k when x is a normal power of two with |k| <= 64, else 127.
 int swe::pow2_exponent(double x) {
     int k = 0;
@@ -82,7 +108,29 @@ int refresh_speed(swe_ctx *c) {
 }
 
 cudaError_t launch_stage(swe_ctx *c, int stage, const StageParams &sp) {
-    return fp32(c) ? launch_stage_f32(stage, sp, c->stream) : launch_stage_f64(stage, sp, c->stream);
+    if (fp32(c))
+        return launch_stage_f32(stage, sp, c->maps_ok ? &c->maps[stage - 1] : nullptr, c->stream);
+    return launch_stage_f64(stage, sp, c->stream);
+}
+
+// TMA maps of the three stage sources of an FP32 context (box = tile + 2-cell halo).
+// Any failure leaves maps_ok false and every tile on the mirrored-index loader.
+void build_maps(swe_ctx *c) {
+    c->maps_ok = false;
+    const char *off = std::getenv("SWE_GB300_NO_TMA");
+    if (off && off[0] == '1') return;
+    const int rows = c->p.Nx + 4, cols = c->p.Ny + 4;
+    const int bi = TILE_I_F32 + 4, bj = TILE_J_F32 + 4;
+    void *const *src[3] = {c->Un, c->U1, c->U2};
+    for (int s = 0; s < 3; ++s) {
+        StageMaps &m = c->maps[s];
+        if (!encode_tile_map_f32(&m.e, src[s][0], rows, cols, c->pitch, bi, bj) ||
+            !encode_tile_map_f32(&m.u, src[s][1], rows, cols, c->pitch, bi, bj) ||
+            !encode_tile_map_f32(&m.v, src[s][2], rows, cols, c->pitch, bi, bj) ||
+            !encode_tile_map_f32(&m.b, c->B, rows, cols, c->pitch, bi, bj))
+            return;
+    }
+    c->maps_ok = true;
 }
 
 }  // namespace
@@ -195,6 +243,7 @@ int swe_create(const swe_params *pin, swe_ctx **out) {
     e = cudaMemsetAsync(c->base, 0, 10 * fb + aux + staging, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cleanup(SWE_ERR_CUDA);
+    if (p.precision == SWE_PRECISION_FP32_MIXED) build_maps(c);
     *out = c;
     return SWE_OK;
 }

@@ -7,6 +7,7 @@
 #include <string>
 
 #include "../../include/swe_gb300.h"
+#include "swe_tma.cuh"
 
 struct swe_ctx {
     swe_params p{};
@@ -30,6 +31,8 @@ struct swe_ctx {
     long long launches = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // bracket the stage launches of swe_step
     double last_ms = 0.0;
+    swe::StageMaps maps[3]{};  // FP32 form: TMA maps of U^n, U^(1), U^(2) (stage sources)
+    bool maps_ok = false;
     std::string err;
 };
 

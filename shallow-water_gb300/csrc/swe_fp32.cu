@@ -23,6 +23,9 @@
 // form.  The wall boundary condition is applied by mirrored indices while loading.
 #include "swe_common.cuh"
 #include "swe_launch.h"
+#include "swe_tma.cuh"
+
+#include <cstring>
 
 namespace swe {
 namespace {
@@ -127,10 +130,16 @@ __device__ __forceinline__ void block_max_to_slot_f(float v, unsigned long long 
     }
 }
 
-// The step's dt, computed once per block in FP64 and shared (an FP64 division per
-// thread would cost more than the whole FP32 stencil).
-__device__ __forceinline__ double stage_dt_f32(const StageParams &p) {
+// The step's dt, computed once per block in FP64 and shared together with its FP32
+// image (an FP64 division or conversion per thread runs on GB300's slow FP64 unit).
+struct BlockDt {
+    double d;
+    float f;
+};
+
+__device__ __forceinline__ BlockDt stage_dt_f32(const StageParams &p) {
     __shared__ double s_dt;
+    __shared__ float s_dtf;
     if (threadIdx.x == 0) {
         double dt = p.dt_fixed;
         if (!(dt > 0.0)) {
@@ -138,18 +147,23 @@ __device__ __forceinline__ double stage_dt_f32(const StageParams &p) {
             dt = (ms <= EPS) ? 1.0e100 : p.cfl_min_dxdy / ms;
         }
         s_dt = dt;
+        s_dtf = (float)dt;
     }
     __syncthreads();
-    return s_dt;
+    return BlockDt{s_dt, s_dtf};
 }
 
 // One tile of one RK stage (see stage_tile_f64); returns the thread's cell wave speed of
 // the new state in stage 3, else 0.  (TI + 1) * TJ threads; dt is the block's dt.
 template <int TI, int TJ, int STAGE>
 __device__ __forceinline__ float stage_tile_f32(const StageParams &p, int i0, int j0,
-                                                double dtd) {
+                                                float dt, const tma::TileMaps *tm = nullptr) {
     constexpr int NT = (TI + 1) * TJ, RI = TI + 4, RJ = TJ + 4;
-    __shared__ float s_e[RI][RJ], s_u[RI][RJ], s_v[RI][RJ], s_b[RI][RJ];
+    // 128-byte aligned so the TMA box of each field lands on an aligned address
+    __shared__ __align__(128) float s_e[RI][RJ];
+    __shared__ __align__(128) float s_u[RI][RJ];
+    __shared__ __align__(128) float s_v[RI][RJ];
+    __shared__ __align__(128) float s_b[RI][RJ];
     __shared__ float s_xf[4][TI + 1][TJ];
     __shared__ float s_yf[4][TI][TJ + 1];
 
@@ -160,27 +174,51 @@ __device__ __forceinline__ float stage_tile_f32(const StageParams &p, int i0, in
     const float *vs = static_cast<const float *>(p.hvs);
     const float *Bg = static_cast<const float *>(p.B);
 
-    for (int t = tid; t < RI * RJ; t += NT) {
-        const int r = t / RJ, c = t - (t / RJ) * RJ;
-        const int ii = i0 - NG + r, jj = j0 - NG + c;
-        bool fx, fy;
-        const int mi = map_coord(ii, p.Nx, p.bc, fx);
-        const int mj = map_coord(jj, p.Ny, p.bc, fy);
-        const long long k = (long long)(mi + NG) * P + (mj + NG);
-        const int bi = clamp_int(ii + NG, 0, p.Nx + 2 * NG - 1);
-        const int bj = clamp_int(jj + NG, 0, p.Ny + 2 * NG - 1);
-        const float b = Bg[(long long)bi * P + bj];
-        // A ghost holds the interior cell's depth over its own bed: eta_g = h_src + B_g
-        // (eta itself where the beds agree, so a flat surface stays bitwise flat).
-        const float bsrc = Bg[k];
-        const float e = es[k];
-        s_e[r][c] = (b == bsrc) ? e : (e - bsrc) + b;
-        const float u = us[k], v = vs[k];
-        s_u[r][c] = fx ? -u : u;
-        s_v[r][c] = fy ? -v : v;
-        s_b[r][c] = b;
+    // Tiles whose halo lies inside the interior are staged by TMA; tiles that touch a
+    // wall use mirrored indices (their halo holds ghost cells).
+    const bool interior = tm != nullptr && i0 >= NG && j0 >= NG && i0 + TI + NG <= p.Nx &&
+                          j0 + TJ + NG <= p.Ny;
+    if (interior) {
+        __shared__ __align__(8) uint64_t s_bar;
+        if (tid == 0) tma::mbar_init(&s_bar, 1);
+        __syncthreads();
+        if (tid == 0) {
+            tma::mbar_arrive_expect_tx(&s_bar, 4u * RI * RJ * sizeof(float));
+            // halo origin (i0 - 2, j0 - 2) in interior coordinates = (i0, j0) in the
+            // ghosted array; j0 is a multiple of TJ, so x * 4 bytes is 16-byte aligned
+            tma::load_2d(&s_e[0][0], tm->e, j0, i0, &s_bar);
+            tma::load_2d(&s_u[0][0], tm->u, j0, i0, &s_bar);
+            tma::load_2d(&s_v[0][0], tm->v, j0, i0, &s_bar);
+            tma::load_2d(&s_b[0][0], tm->b, j0, i0, &s_bar);
+        }
+        const bool timed_out = !tma::mbar_wait(&s_bar, 0);
+        if (__syncthreads_or(timed_out)) {
+            if (tid == 0) atomicOr(p.flags, FLAG_TIMEOUT);
+            return 0.f;
+        }
+    } else {
+        for (int t = tid; t < RI * RJ; t += NT) {
+            const int r = t / RJ, c = t - (t / RJ) * RJ;
+            const int ii = i0 - NG + r, jj = j0 - NG + c;
+            bool fx, fy;
+            const int mi = map_coord(ii, p.Nx, p.bc, fx);
+            const int mj = map_coord(jj, p.Ny, p.bc, fy);
+            const long long k = (long long)(mi + NG) * P + (mj + NG);
+            const int bi = clamp_int(ii + NG, 0, p.Nx + 2 * NG - 1);
+            const int bj = clamp_int(jj + NG, 0, p.Ny + 2 * NG - 1);
+            const float b = Bg[(long long)bi * P + bj];
+            // A ghost holds the interior cell's depth over its own bed: eta_g = h_src + B_g
+            // (eta itself where the beds agree, so a flat surface stays bitwise flat).
+            const float bsrc = Bg[k];
+            const float e = es[k];
+            s_e[r][c] = (b == bsrc) ? e : (e - bsrc) + b;
+            const float u = us[k], v = vs[k];
+            s_u[r][c] = fx ? -u : u;
+            s_v[r][c] = fy ? -v : v;
+            s_b[r][c] = b;
+        }
+        __syncthreads();
     }
-    __syncthreads();
 
     const float g = p.gf, half_g = p.half_gf;
     {
@@ -209,7 +247,6 @@ __device__ __forceinline__ float stage_tile_f32(const StageParams &p, int i0, in
     }
     __syncthreads();
 
-    const float dt = (float)dtd;
     const int ty = tid / TJ, tx = tid - (tid / TJ) * TJ;
     const int ii = i0 + ty, jj = j0 + tx;
     const bool inside = (ty < TI) && (ii < p.Nx) && (jj < p.Ny);
@@ -262,10 +299,15 @@ __device__ __forceinline__ float stage_tile_f32(const StageParams &p, int i0, in
 }
 
 template <int TI, int TJ, int STAGE>
-__global__ void __launch_bounds__((TI + 1) * TJ) k_stage_f32(const StageParams p) {
-    const double dtd = stage_dt_f32(p);
-    const float dt = (float)dtd;
-    const float speed = stage_tile_f32<TI, TJ, STAGE>(p, blockIdx.y * TI, blockIdx.x * TJ, dtd);
+__global__ void __launch_bounds__((TI + 1) * TJ)
+    k_stage_f32(const StageParams p, const __grid_constant__ CUtensorMap tm_e,
+                const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ CUtensorMap tm_v,
+                const __grid_constant__ CUtensorMap tm_b, const int use_tma) {
+    const BlockDt bd = stage_dt_f32(p);
+    const float dt = bd.f;
+    const tma::TileMaps maps{&tm_e, &tm_u, &tm_v, &tm_b};
+    const float speed = stage_tile_f32<TI, TJ, STAGE>(p, blockIdx.y * TI, blockIdx.x * TJ, dt,
+                                                      use_tma ? &maps : nullptr);
     if (STAGE == 1 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
         p.speed[p.slot_write] = 0ull;
         if (p.dt_log) p.dt_log[p.log_index] = (double)dt;
@@ -285,9 +327,9 @@ __global__ void __launch_bounds__((TI + 1) * TJ) k_ens_stage_f32(const EnsParams
         const EnsInst &I = e.inst[q];
         const int t = T - I.tile_base;
         const int ti = t / I.tiles_j, tj = t - (t / I.tiles_j) * I.tiles_j;
-        const double dtd = stage_dt_f32(p);
-        const float dt = (float)dtd;
-        const float speed = stage_tile_f32<TI, TJ, STAGE>(p, ti * TI, tj * TJ, dtd);
+        const BlockDt bd = stage_dt_f32(p);
+        const float dt = bd.f;
+        const float speed = stage_tile_f32<TI, TJ, STAGE>(p, ti * TI, tj * TJ, dt);
         if (STAGE == 1 && t == 0 && threadIdx.x == 0) {
             p.speed[p.slot_write] = 0ull;
             if (e.dt_last) e.dt_last[q] = (double)dt;
@@ -378,13 +420,18 @@ unsigned grid_for(long long n, int num_sms) {
 
 }  // namespace
 
-cudaError_t launch_stage_f32(int stage, const StageParams &p, cudaStream_t s) {
-    constexpr int TI = 8, TJ = 32, NT = (TI + 1) * TJ;
+cudaError_t launch_stage_f32(int stage, const StageParams &p, const StageMaps *maps,
+                             cudaStream_t s) {
+    constexpr int TI = TILE_I_F32, TJ = TILE_J_F32, NT = (TI + 1) * TJ;
     const dim3 grid((p.Ny + TJ - 1) / TJ, (p.Nx + TI - 1) / TI);
+    StageMaps none;
+    std::memset(&none, 0, sizeof none);
+    const StageMaps &m = maps ? *maps : none;
+    const int use = maps ? 1 : 0;
     switch (stage) {
-        case 1: k_stage_f32<TI, TJ, 1><<<grid, NT, 0, s>>>(p); break;
-        case 2: k_stage_f32<TI, TJ, 2><<<grid, NT, 0, s>>>(p); break;
-        default: k_stage_f32<TI, TJ, 3><<<grid, NT, 0, s>>>(p); break;
+        case 1: k_stage_f32<TI, TJ, 1><<<grid, NT, 0, s>>>(p, m.e, m.u, m.v, m.b, use); break;
+        case 2: k_stage_f32<TI, TJ, 2><<<grid, NT, 0, s>>>(p, m.e, m.u, m.v, m.b, use); break;
+        default: k_stage_f32<TI, TJ, 3><<<grid, NT, 0, s>>>(p, m.e, m.u, m.v, m.b, use); break;
     }
     return cudaGetLastError();
 }

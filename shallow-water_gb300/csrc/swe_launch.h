@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include "swe_common.cuh"
+#include "swe_tma.cuh"
 
 namespace swe {
 
@@ -19,7 +20,14 @@ cudaError_t launch_fill_ghosts_f64(void *h, void *hu, void *hv, int Nx, int Ny, 
                                    int bc, cudaStream_t s);
 
 // FP32-mixed form (swe_fp32.cu): state (eta = h + B, hu, hv) and B in FP32.
-cudaError_t launch_stage_f32(int stage, const StageParams &p, cudaStream_t s);
+// Single-grid FP32 tile shape (rows x columns); the TMA box is (TI + 4) x (TJ + 4).
+#ifndef SWE_TILE_I_F32
+#define SWE_TILE_I_F32 8
+#endif
+constexpr int TILE_I_F32 = SWE_TILE_I_F32, TILE_J_F32 = 32;
+// maps: TMA maps of the stage source (NULL: every tile uses the mirrored-index loader).
+cudaError_t launch_stage_f32(int stage, const StageParams &p, const StageMaps *maps,
+                             cudaStream_t s);
 // Ensemble stage (FP32-mixed); shape is SHAPE_8x32, SHAPE_16x32 or SHAPE_8x64.
 cudaError_t launch_ens_stage_f32(int shape, int stage, const EnsParams &e, int grid,
                                  cudaStream_t s);
