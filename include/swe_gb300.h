@@ -225,6 +225,15 @@ int swe_ens_tune(swe_ens *ens, int steps, double *best_ms);
 
 const char *swe_ens_last_error(const swe_ens *ens);
 
+/* ---- Self-test (no counterpart in the reference) ------------------------------------
+ * The FP64 kernels compute double division, square root and part of the multiplications
+ * and additions correctly rounded with integer arithmetic instead of FP64 instructions.
+ * This runs n operand pairs (hashed from seed: every operand class, physical scales,
+ * near-equal pairs, exact quotients and their neighbours) through both those routines
+ * and the device's own IEEE operations on the current device, and writes how many
+ * results differed (NaN results compare equal to any NaN).  Expected: 0. */
+int swe_selftest_soft_f64(long long n, unsigned long long seed, long long *mismatches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -33,7 +33,7 @@ EXPORTS = (
     "swe_ens_create", "swe_ens_destroy", "swe_ens_upload", "swe_ens_download", "swe_ens_step",
     "swe_ens_times", "swe_ens_last_dt", "swe_ens_last_step_ms", "swe_ens_kernel_launches",
     "swe_ens_set_schedule", "swe_ens_get_schedule", "swe_ens_tune", "swe_ens_last_error",
-    "swe_totals_noalloc", "swe_adjoint_gauge",
+    "swe_totals_noalloc", "swe_adjoint_gauge", "swe_selftest_soft_f64",
 )
 TOTALS_NOALLOC_MAX_BLOCKS = 1024
 
@@ -131,6 +131,9 @@ def lib(path: str = LIB_PATH):
     L.swe_adjoint_gauge.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ip, ip, dp,
                                     ctypes.c_int, dp, dp, dp, dp, dp, dp]
     L.swe_adjoint_gauge.restype = ctypes.c_int
+    L.swe_selftest_soft_f64.argtypes = [ctypes.c_longlong, ctypes.c_ulonglong,
+                                        ctypes.POINTER(ctypes.c_longlong)]
+    L.swe_selftest_soft_f64.restype = ctypes.c_int
     L.swe_ens_last_error.argtypes = [vp]
     L.swe_ens_last_error.restype = ctypes.c_char_p
     _lib = L

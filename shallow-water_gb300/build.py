@@ -25,6 +25,7 @@ UNITS = {
     "swe_reduce.cu": [],
     "swe_ensemble.cu": [],
     "swe_adjoint.cu": [],
+    "swe_selftest.cu": [],
     "swe_api.cu": [],
 }
 

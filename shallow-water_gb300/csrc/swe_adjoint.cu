@@ -31,6 +31,10 @@
 namespace swe {
 namespace {
 
+#ifndef SWE_ADJ_MIN_BLOCKS
+#define SWE_ADJ_MIN_BLOCKS 1  // resident CTAs per SM the register budget is sized for
+#endif
+
 constexpr int ATI = 8, ATJ = 32;
 constexpr int ANT = (ATI + 3) * ATJ;       // one thread per x-face of the gather region
 constexpr int SR = ATI + 6, SC = ATJ + 6;  // state tile, halo 3
@@ -89,7 +93,7 @@ __device__ __forceinline__ int virtual_coords(int a, int N, int bc, int *v, bool
 }
 
 template <int STAGE>
-__global__ void __launch_bounds__(ANT) k_adj_stage(const AdjParams a) {
+__global__ void __launch_bounds__(ANT, SWE_ADJ_MIN_BLOCKS) k_adj_stage(const AdjParams a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     AdjSmem &S = *reinterpret_cast<AdjSmem *>(smem_raw);
     const int tid = threadIdx.x;

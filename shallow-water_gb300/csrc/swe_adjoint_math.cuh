@@ -96,7 +96,23 @@ SWE_HD void face_forward(const FaceIn<T> &in, T g, T eps, FaceOut<T> &out) {
     out.fqn_p = F[1] + half * g * (h_p * h_p - hR * hR);
 }
 
+template <class T>
+SWE_HD T trsqrt(T x) {
+#if defined(__CUDA_ARCH__)
+    return rsqrt(x);
+#else
+    return T(1) / sqrt(x);
+#endif
+}
+
 // Adjoint of face_forward: given d = dJ/d(out), returns a = dJ/d(in) (overwritten).
+//
+// The forward part is recomputed for its branch decisions and intermediates with one
+// reciprocal per depth (q/h as q * (1/h)), the hydrostatic velocities (hs*u)/hs taken as
+// u (equal in exact arithmetic) and the wave speed from rsqrt; these differ from the
+// forward's rounding by an ulp, which matters only at exact ties of a branch test.  The
+// reverse sweep reuses the same reciprocals, so one interface costs three divisions and
+// two reciprocal square roots instead of two dozen divisions.
 template <class T>
 SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceIn<T> &a) {
     const T half = T(0.5);
@@ -117,16 +133,19 @@ SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceI
     const bool pm = xm > T(0), pp = xp > T(0);
     const T h_m = pm ? xm : T(0), h_p = pp ? xp : T(0);
     const bool wm = h_m > eps, wp = h_p > eps;
-    const T un_m = wm ? qn_m / h_m : T(0), ut_m = wm ? qt_m / h_m : T(0);
-    const T un_p = wp ? qn_p / h_p : T(0), ut_p = wp ? qt_p / h_p : T(0);
+    const T rm = wm ? T(1) / h_m : T(0), rp = wp ? T(1) / h_p : T(0);
+    const T un_m = qn_m * rm, ut_m = qt_m * rm;
+    const T un_p = qn_p * rp, ut_p = qt_p * rp;
     const T yL = eta_m - bs, yR = eta_p - bs;
     const bool pL = yL > T(0), pR = yR > T(0);
     const T hL = pL ? yL : T(0), hR = pR ? yR : T(0);
     const T qnL = hL * un_m, qtL = hL * ut_m, qnR = hR * un_p, qtR = hR * ut_p;
     const bool wL = hL > eps, wR = hR > eps;
-    const T unL = wL ? qnL / hL : T(0), utL = wL ? qtL / hL : T(0);
-    const T unR = wR ? qnR / hR : T(0), utR = wR ? qtR / hR : T(0);
-    const T cL = sqrt(g * hL), cR = sqrt(g * hR);
+    const T unL = wL ? un_m : T(0), utL = wL ? ut_m : T(0);
+    const T unR = wR ? un_p : T(0), utR = wR ? ut_p : T(0);
+    const T ghL = g * hL, ghR = g * hR;
+    const T rcL = ghL > T(0) ? trsqrt(ghL) : T(0), rcR = ghR > T(0) ? trsqrt(ghR) : T(0);
+    const T cL = ghL * rcL, cR = ghR * rcR;
     const T a1 = unL - cL, a2 = unR - cR, b1 = unL + cL, b2 = unR + cR;
     const bool sL_is2 = a2 < a1, sR_is2 = b1 < b2;
     const T sL = sL_is2 ? a2 : a1, sR = sR_is2 ? b2 : b1;
@@ -136,11 +155,9 @@ SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceI
     const int regime = (sL >= T(0)) ? 0 : ((sR <= T(0)) ? 1 : 2);
 
     // ---- reverse sweep ----
-    // outputs -> F, corrections
     const T dF[3] = {d.fh, d.fqn_m + d.fqn_p, d.fqt};
     T dh_m = g * h_m * d.fqn_m, dh_p = g * h_p * d.fqn_p;
     T dhL = -g * hL * d.fqn_m, dhR = -g * hR * d.fqn_p;
-    // HLL
     T dFL[3] = {0, 0, 0}, dFR[3] = {0, 0, 0}, dUL[3] = {0, 0, 0}, dUR[3] = {0, 0, 0};
     T dsL = 0, dsR = 0;
     if (regime == 0) {
@@ -149,18 +166,18 @@ SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceI
         for (int c = 0; c < 3; ++c) dFR[c] = dF[c];
     } else {
         const T inv = T(1) / (sR - sL);
+        const T sLi = sL * inv, sRi = sR * inv, sLsRi = sL * sRi;
         for (int c = 0; c < 3; ++c) {
-            const T F = (sR * FL[c] - sL * FR[c] + sL * sR * (UR[c] - UL[c])) * inv;
             const T dU = UR[c] - UL[c];
-            dFL[c] = dF[c] * sR * inv;
-            dFR[c] = -dF[c] * sL * inv;
-            dUR[c] = dF[c] * sL * sR * inv;
+            const T F = sRi * FL[c] - sLi * FR[c] + sLsRi * dU;
+            dFL[c] = dF[c] * sRi;
+            dFR[c] = -dF[c] * sLi;
+            dUR[c] = dF[c] * sLsRi;
             dUL[c] = -dUR[c];
             dsR += dF[c] * ((FL[c] + sL * dU) - F) * inv;
             dsL += dF[c] * ((-FR[c] + sR * dU) + F) * inv;
         }
     }
-    // speeds
     T dunL = 0, dunR = 0, dcL = 0, dcR = 0;
     if (sL_is2) {
         dunR += dsL;
@@ -176,34 +193,24 @@ SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceI
         dunL += dsR;
         dcL += dsR;
     }
-    if (cL > T(0)) dhL += dcL * g / (T(2) * cL);
-    if (cR > T(0)) dhR += dcR * g / (T(2) * cR);
+    dhL += dcL * half * g * rcL;  // dc/dh = g / (2 c)
+    dhR += dcR * half * g * rcR;
     // physical fluxes FL = (qnL, qnL unL + g/2 hL^2, qnL utL); U = (h, qn, qt)
-    T dqnL = dFL[0] + dFL[1] * unL + dFL[2] * utL + dUL[1];
-    T dqtL = dUL[2];
+    const T dqnL = dFL[0] + dFL[1] * unL + dFL[2] * utL + dUL[1];
+    const T dqtL = dUL[2];
     dunL += dFL[1] * qnL;
     T dutL = dFL[2] * qnL;
     dhL += dFL[1] * g * hL + dUL[0];
-    T dqnR = dFR[0] + dFR[1] * unR + dFR[2] * utR + dUR[1];
-    T dqtR = dUR[2];
+    const T dqnR = dFR[0] + dFR[1] * unR + dFR[2] * utR + dUR[1];
+    const T dqtR = dUR[2];
     dunR += dFR[1] * qnR;
     T dutR = dFR[2] * qnR;
     dhR += dFR[1] * g * hR + dUR[0];
-    // unL = qnL / hL (wet)
-    if (wL) {
-        dqnL += dunL / hL;
-        dqtL += dutL / hL;
-        dhL -= (dunL * unL + dutL * utL) / hL;
-    }
-    if (wR) {
-        dqnR += dunR / hR;
-        dqtR += dutR / hR;
-        dhR -= (dunR * unR + dutR * utR) / hR;
-    }
-    // qnL = hL un_m, ...
+    // unL = un_m (wet L), qnL = hL un_m, ...
+    T dun_m = dqnL * hL + (wL ? dunL : T(0)), dut_m = dqtL * hL + (wL ? dutL : T(0));
+    T dun_p = dqnR * hR + (wR ? dunR : T(0)), dut_p = dqtR * hR + (wR ? dutR : T(0));
     dhL += dqnL * un_m + dqtL * ut_m;
     dhR += dqnR * un_p + dqtR * ut_p;
-    T dun_m = dqnL * hL, dut_m = dqtL * hL, dun_p = dqnR * hR, dut_p = dqtR * hR;
     // hL = max(eta_m - bs, 0)
     T deta_m = 0, deta_p = 0, dbs = 0;
     if (pL) {
@@ -215,17 +222,10 @@ SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceI
         dbs -= dhR;
     }
     // un_m = qn_m / h_m (wet)
-    T dqn_m = 0, dqt_m = 0, dqn_p = 0, dqt_p = 0;
-    if (wm) {
-        dqn_m += dun_m / h_m;
-        dqt_m += dut_m / h_m;
-        dh_m -= (dun_m * un_m + dut_m * ut_m) / h_m;
-    }
-    if (wp) {
-        dqn_p += dun_p / h_p;
-        dqt_p += dut_p / h_p;
-        dh_p -= (dun_p * un_p + dut_p * ut_p) / h_p;
-    }
+    const T dqn_m = dun_m * rm, dqt_m = dut_m * rm;
+    const T dqn_p = dun_p * rp, dqt_p = dut_p * rp;
+    dh_m -= (dun_m * un_m + dut_m * ut_m) * rm;
+    dh_p -= (dun_p * un_p + dut_p * ut_p) * rp;
     // h_m = max(eta_m - bm, 0)
     T dbm = 0, dbp = 0;
     if (pm) {

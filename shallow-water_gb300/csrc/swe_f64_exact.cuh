@@ -14,8 +14,12 @@
 
 #if defined(__CUDACC__)
 #define SWE_HD __host__ __device__ __forceinline__
+// Rare-operand fallbacks are out of line on the device: inlined, the compiler may
+// if-convert them and issue their FP64 instructions for every lane on every call.
+#define SWE_COLD static __host__ __device__ __noinline__
 #else
 #define SWE_HD inline
+#define SWE_COLD static inline
 #endif
 
 namespace swe {
@@ -26,9 +30,14 @@ constexpr int64_t ABS = INT64_MAX;
 constexpr int64_t INF_BITS = 0x7FF0000000000000LL;
 constexpr int64_t MANT = 0x000FFFFFFFFFFFFFLL;
 
+// On the device the casts are opaque moves: seen through, the compiler folds bit tests
+// and sign splices back into FP64 compares, abs, neg and copysign, which run on the
+// scarce FP64 pipe.
 SWE_HD int64_t bits(double x) {
 #if defined(__CUDA_ARCH__)
-    return __double_as_longlong(x);
+    int64_t b;
+    asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+    return b;
 #else
     int64_t b;
     std::memcpy(&b, &x, sizeof b);
@@ -38,7 +47,9 @@ SWE_HD int64_t bits(double x) {
 
 SWE_HD double from_bits(int64_t b) {
 #if defined(__CUDA_ARCH__)
-    return __longlong_as_double(b);
+    double x;
+    asm("mov.b64 %0, %1;" : "=d"(x) : "l"(b));
+    return x;
 #else
     double x;
     std::memcpy(&x, &b, sizeof x);
@@ -84,13 +95,20 @@ SWE_HD double positive_part(double x) {
     return (b > 0 && b <= INF_BITS) ? x : 0.0;
 }
 
-// 0.5 * x
+SWE_COLD double mul_cold(double a, double b) { return a * b; }
+SWE_COLD double div_cold(double a, double b) { return a / b; }
+
+// 0.5 * x, on the bit pattern for every input: exponent decrement for normal results;
+// for |x| below 2^-1021 the magnitude bits are proportional to the value, so halving is
+// a right shift rounded half to even; infinities and NaN are returned (NaN quietened).
 SWE_HD double halve(double x) {
     const int64_t b = bits(x);
     const int64_t e = (b >> 52) & 0x7FF;
     if (e > 1 && e < 0x7FF) return from_bits(b - (1LL << 52));
-    if ((b & ABS) == 0) return x;
-    return 0.5 * x;
+    const int64_t mag = b & ABS;
+    if (e == 0x7FF) return from_bits(mag > INF_BITS ? (b | (1LL << 51)) : b);
+    const int64_t h = (mag >> 1) + (mag & (mag >> 1) & 1);
+    return from_bits((b & SIGN) | h);
 }
 
 // x * 2^k for |k| small, exact when the result stays normal; else the FP64 product
@@ -100,14 +118,15 @@ SWE_HD double scale2(double x, int k, double p2k) {
     const int64_t e = (b >> 52) & 0x7FF;
     const int64_t en = e + k;
     if (e > 0 && e < 0x7FF && en > 0 && en < 0x7FF) return from_bits(b + ((int64_t)k << 52));
-    if ((b & ABS) == 0) return x * p2k;
-    return x * p2k;
+    if ((b & ABS) == 0) return x;  // +-0 * 2^k
+    return mul_cold(x, p2k);
 }
 
 SWE_HD double fabs_(double x) { return from_bits(bits(x) & ABS); }
+SWE_HD double neg(double x) { return from_bits(bits(x) ^ SIGN); }
 
 // Plain minmod (HPC_kernels.hpp:41-44), the fallback.
-SWE_HD double minmod_plain(double a, double b) {
+SWE_COLD double minmod_plain(double a, double b) {
     if (a * b <= 0.0) return 0.0;
     const double fa = fabs_(a), fb = fabs_(b);
     return (a > 0.0 ? 1.0 : -1.0) * ((fb < fa) ? fb : fa);
@@ -144,11 +163,11 @@ SWE_HD double redivide(double P, double H, double q) {
     const int64_t eq = (bq >> 52) & 0x7FF, eH = (bH >> 52) & 0x7FF;
     if ((bq & ABS) == 0) {
         if (eH > 0 && eH < 0x7FF && bH > 0) return q;  // P = +-0, H > 0: P / H = q
-        return P / H;
+        return div_cold(P, H);
     }
     // Range that keeps H*q, the residual and the threshold normal and exact.
     if (eq < 123 || eq > 1923 || eH < 1 || eH > 1923 || bH < 0 || eH + eq > 3046)
-        return P / H;
+        return div_cold(P, H);
     const double e = fma_rn(H, q, -P);
     const int64_t be = bits(e);
     if ((be & ABS) == 0) return q;

@@ -19,8 +19,11 @@
 // to the integer pipe with bit-exact helpers (swe_f64_exact.cuh): compares, min/max,
 // minmod's sign logic, positive parts, exact scalings by powers of two, and the
 // reference's re-division (h*u)/h, which is decided from one exact FMA residual.
+// Divisions and square roots, about twenty FP64-pipe slots each, are computed
+// correctly rounded on the integer pipe (swe_soft_f64.cuh).
 #include "swe_common.cuh"
 #include "swe_f64_exact.cuh"
+#include "swe_soft_f64.cuh"
 #include "swe_launch.h"
 
 namespace swe {
@@ -37,12 +40,44 @@ static_assert(sizeof(double) == 8, "double is binary64");
 
 // safe_velocity (HPC_kernels.hpp:37-39): (h > 1e-8) ? q / h : 0.0
 __device__ __forceinline__ double safe_velocity(double q, double h) {
-    return x64::gt_pos_const(h, EPS_BITS) ? (q / h) : 0.0;
+    return x64::gt_pos_const(h, EPS_BITS) ? sf::div_rn(q, h) : 0.0;
+}
+
+// Work split between the FP64 pipe and the integer pipes.  Each group of operations
+// below runs either as FP64 instructions or as the correctly rounded integer routines
+// of swe_soft_f64.cuh (identical results); moving part of the adds and multiplies off
+// the FP64 pipe balances it against the integer pipes that carry the rest.
+//   multiply groups: 0 momenta h*u, 1 physical fluxes, 2 HLL combination,
+//                    3 wave-speed and bathymetry-correction products, 4 cell update;
+//   add groups:      0 stencil differences, 1 reconstruction and depths, 2 wave
+//                    speeds and flux sums, 3 HLL combination, 4 corrections and
+//                    cell update.
+#ifndef SWE_F64_SOFT_MUL
+#define SWE_F64_SOFT_MUL 0x00
+#endif
+#ifndef SWE_F64_SOFT_ADD
+#define SWE_F64_SOFT_ADD 0x00
+#endif
+
+template <int G>
+__device__ __forceinline__ double fmul(double a, double b) {
+    if constexpr (((SWE_F64_SOFT_MUL) >> G) & 1) return sf::mul_rn(a, b);
+    else return a * b;
+}
+template <int G>
+__device__ __forceinline__ double fadd(double a, double b) {
+    if constexpr (((SWE_F64_SOFT_ADD) >> G) & 1) return sf::add_rn(a, b);
+    else return a + b;
+}
+template <int G>
+__device__ __forceinline__ double fsub(double a, double b) {
+    if constexpr (((SWE_F64_SOFT_ADD) >> G) & 1) return sf::sub_rn(a, b);
+    else return a - b;
 }
 
 // Exact multiplication by a grid constant that may be a power of two (k != 127).
 __device__ __forceinline__ double mul_const(double c, int k, double x) {
-    return k != 127 ? x64::scale2(x, k, c) : c * x;
+    return k != 127 ? x64::scale2(x, k, c) : fmul<4>(c, x);
 }
 
 // hll_x (HPC_kernels.hpp:46-82) in normal/tangential form; hll_y (:84-120) is the
@@ -52,22 +87,23 @@ __device__ __forceinline__ double mul_const(double c, int k, double x) {
 __device__ __forceinline__ void hll_normal(double g, double half_g, double hL, double unm,
                                            double utm, double hR, double unp, double utp,
                                            double &fh, double &fqn, double &fqt) {
-    const double qnL = hL * unm, qtL = hL * utm, qnR = hR * unp, qtR = hR * utp;
+    const double qnL = fmul<0>(hL, unm), qtL = fmul<0>(hL, utm);
+    const double qnR = fmul<0>(hR, unp), qtR = fmul<0>(hR, utp);
     const bool wetL = x64::gt_pos_const(hL, EPS_BITS), wetR = x64::gt_pos_const(hR, EPS_BITS);
     const double unL = wetL ? x64::redivide(qnL, hL, unm) : 0.0;
     const double utL = wetL ? x64::redivide(qtL, hL, utm) : 0.0;
     const double unR = wetR ? x64::redivide(qnR, hR, unp) : 0.0;
     const double utR = wetR ? x64::redivide(qtR, hR, utp) : 0.0;
-    const double cL = sqrt(g * hL);
-    const double cR = sqrt(g * hR);
-    const double sL = dmin(unL - cL, unR - cR);
-    const double sR = dmax(unL + cL, unR + cR);
+    const double cL = sf::sqrt_rn(fmul<3>(g, hL));
+    const double cR = sf::sqrt_rn(fmul<3>(g, hR));
+    const double sL = dmin(fsub<2>(unL, cL), fsub<2>(unR, cR));
+    const double sR = dmax(fadd<2>(unL, cL), fadd<2>(unR, cR));
     const double FL_h = qnL;
-    const double FL_n = qnL * unL + half_g * hL * hL;
-    const double FL_t = qnL * utL;
+    const double FL_n = fadd<2>(fmul<1>(qnL, unL), fmul<1>(fmul<1>(half_g, hL), hL));
+    const double FL_t = fmul<1>(qnL, utL);
     const double FR_h = qnR;
-    const double FR_n = qnR * unR + half_g * hR * hR;
-    const double FR_t = qnR * utR;
+    const double FR_n = fadd<2>(fmul<1>(qnR, unR), fmul<1>(fmul<1>(half_g, hR), hR));
+    const double FR_t = fmul<1>(qnR, utR);
     if (x64::le(0.0, sL)) {
         fh = FL_h;
         fqn = FL_n;
@@ -77,11 +113,19 @@ __device__ __forceinline__ void hll_normal(double g, double half_g, double hL, d
         fqn = FR_n;
         fqt = FR_t;
     } else {
-        const double inv = 1.0 / (sR - sL);
-        const double sLsR = sL * sR;
-        fh = (sR * FL_h - sL * FR_h + sLsR * (hR - hL)) * inv;
-        fqn = (sR * FL_n - sL * FR_n + sLsR * (qnR - qnL)) * inv;
-        fqt = (sR * FL_t - sL * FR_t + sLsR * (qtR - qtL)) * inv;
+        // (sR*FL - sL*FR + sL*sR*(UR - UL)) / (sR - sL), the division as a product with
+        // the reciprocal exactly as the reference writes it
+        const double inv = sf::div_rn(1.0, fsub<3>(sR, sL));
+        const double sLsR = fmul<2>(sL, sR);
+        fh = fmul<2>(fadd<3>(fsub<3>(fmul<2>(sR, FL_h), fmul<2>(sL, FR_h)),
+                             fmul<2>(sLsR, fsub<3>(hR, hL))),
+                     inv);
+        fqn = fmul<2>(fadd<3>(fsub<3>(fmul<2>(sR, FL_n), fmul<2>(sL, FR_n)),
+                              fmul<2>(sLsR, fsub<3>(qnR, qnL))),
+                      inv);
+        fqt = fmul<2>(fadd<3>(fsub<3>(fmul<2>(sR, FL_t), fmul<2>(sL, FR_t)),
+                              fmul<2>(sLsR, fsub<3>(qtR, qtL))),
+                      inv);
     }
 }
 
@@ -97,34 +141,39 @@ __device__ __forceinline__ Face face_flux(double g, double half_g, double eta_m1
                                           double qn_0, double qn_p1, double qn_p2, double qt_m1,
                                           double qt_0, double qt_p1, double qt_p2,
                                           double b_minus, double b_plus) {
-    const double d_eta0 = eta_0 - eta_m1, d_eta1 = eta_p1 - eta_0, d_eta2 = eta_p2 - eta_p1;
-    const double d_qn0 = qn_0 - qn_m1, d_qn1 = qn_p1 - qn_0, d_qn2 = qn_p2 - qn_p1;
-    const double d_qt0 = qt_0 - qt_m1, d_qt1 = qt_p1 - qt_0, d_qt2 = qt_p2 - qt_p1;
-    const double eta_minus = eta_0 + x64::halve(x64::minmod(d_eta0, d_eta1));
-    const double eta_plus = eta_p1 - x64::halve(x64::minmod(d_eta1, d_eta2));
-    const double qn_minus = qn_0 + x64::halve(x64::minmod(d_qn0, d_qn1));
-    const double qt_minus = qt_0 + x64::halve(x64::minmod(d_qt0, d_qt1));
-    const double qn_plus = qn_p1 - x64::halve(x64::minmod(d_qn1, d_qn2));
-    const double qt_plus = qt_p1 - x64::halve(x64::minmod(d_qt1, d_qt2));
+    const double d_eta0 = fsub<0>(eta_0, eta_m1), d_eta1 = fsub<0>(eta_p1, eta_0);
+    const double d_eta2 = fsub<0>(eta_p2, eta_p1);
+    const double d_qn0 = fsub<0>(qn_0, qn_m1), d_qn1 = fsub<0>(qn_p1, qn_0);
+    const double d_qn2 = fsub<0>(qn_p2, qn_p1);
+    const double d_qt0 = fsub<0>(qt_0, qt_m1), d_qt1 = fsub<0>(qt_p1, qt_0);
+    const double d_qt2 = fsub<0>(qt_p2, qt_p1);
+    const double eta_minus = fadd<1>(eta_0, x64::halve(x64::minmod(d_eta0, d_eta1)));
+    const double eta_plus = fsub<1>(eta_p1, x64::halve(x64::minmod(d_eta1, d_eta2)));
+    const double qn_minus = fadd<1>(qn_0, x64::halve(x64::minmod(d_qn0, d_qn1)));
+    const double qt_minus = fadd<1>(qt_0, x64::halve(x64::minmod(d_qt0, d_qt1)));
+    const double qn_plus = fsub<1>(qn_p1, x64::halve(x64::minmod(d_qn1, d_qn2)));
+    const double qt_plus = fsub<1>(qt_p1, x64::halve(x64::minmod(d_qt1, d_qt2)));
     const double b_star = dmax(b_minus, b_plus);
-    const double h_minus = x64::positive_part(eta_minus - b_minus);
-    const double h_plus = x64::positive_part(eta_plus - b_plus);
+    const double h_minus = x64::positive_part(fsub<1>(eta_minus, b_minus));
+    const double h_plus = x64::positive_part(fsub<1>(eta_plus, b_plus));
     const double un_minus = safe_velocity(qn_minus, h_minus);
     const double ut_minus = safe_velocity(qt_minus, h_minus);
     const double un_plus = safe_velocity(qn_plus, h_plus);
     const double ut_plus = safe_velocity(qt_plus, h_plus);
-    const double hs_minus = x64::positive_part(eta_minus - b_star);
-    const double hs_plus = x64::positive_part(eta_plus - b_star);
+    const double hs_minus = x64::positive_part(fsub<1>(eta_minus, b_star));
+    const double hs_plus = x64::positive_part(fsub<1>(eta_plus, b_star));
     double f_h, f_n, f_t;
     hll_normal(g, half_g, hs_minus, un_minus, ut_minus, hs_plus, un_plus, ut_plus, f_h, f_n,
                f_t);
-    const double corr_minus = half_g * (h_minus * h_minus - hs_minus * hs_minus);
-    const double corr_plus = half_g * (h_plus * h_plus - hs_plus * hs_plus);
+    const double corr_minus =
+        fmul<3>(half_g, fsub<4>(fmul<3>(h_minus, h_minus), fmul<3>(hs_minus, hs_minus)));
+    const double corr_plus =
+        fmul<3>(half_g, fsub<4>(fmul<3>(h_plus, h_plus), fmul<3>(hs_plus, hs_plus)));
     Face f;
     f.fh = f_h;
     f.fqt = f_t;
-    f.fqn_m = f_n + corr_minus;
-    f.fqn_p = f_n + corr_plus;
+    f.fqn_m = fadd<4>(f_n, corr_minus);
+    f.fqn_p = fadd<4>(f_n, corr_plus);
     return f;
 }
 
@@ -132,7 +181,7 @@ __device__ __forceinline__ Face face_flux(double g, double half_g, double eta_m1
 __device__ __forceinline__ double cell_speed(double g, double h, double hu, double hv) {
     const double u = safe_velocity(hu, h);
     const double v = safe_velocity(hv, h);
-    const double c = sqrt(g * x64::positive_part(h));  // std::max(0.0, h)
+    const double c = sf::sqrt_rn(g * x64::positive_part(h));  // std::max(0.0, h)
     return dmax(x64::fabs_(u) + c, x64::fabs_(v) + c);
 }
 
@@ -202,8 +251,8 @@ __device__ __forceinline__ double stage_tile_f64(const StageParams &p, int i0, i
         const int bj = clamp_int(jj + NG, 0, p.Ny + 2 * NG - 1);
         const double b_ = Bg[(long long)bi * P + bj];
         s_h[r][c] = h_;
-        s_hu[r][c] = fx ? -hu_ : hu_;
-        s_hv[r][c] = fy ? -hv_ : hv_;
+        s_hu[r][c] = fx ? x64::neg(hu_) : hu_;
+        s_hv[r][c] = fy ? x64::neg(hv_) : hv_;
         s_B[r][c] = b_;
         s_eta[r][c] = h_ + b_;
     }
@@ -246,33 +295,40 @@ __device__ __forceinline__ double stage_tile_f64(const StageParams &p, int i0, i
         // apply_divergence (HPC_kernels.hpp:274-276): right/top face minus-side
         // fluxes against left/bottom face plus-side fluxes.
         // -inv_dx * (a - b) - inv_dy * (c - d); (-c) * x == -(c * x) exactly.
-        const double rh = -mul_const(p.inv_dx, p.kx, s_xf[0][ty + 1][tx] - s_xf[0][ty][tx]) -
-                          mul_const(p.inv_dy, p.ky, s_yf[0][ty][tx + 1] - s_yf[0][ty][tx]);
-        const double rhu = -mul_const(p.inv_dx, p.kx, s_xf[2][ty + 1][tx] - s_xf[3][ty][tx]) -
-                           mul_const(p.inv_dy, p.ky, s_yf[1][ty][tx + 1] - s_yf[1][ty][tx]);
-        const double rhv = -mul_const(p.inv_dx, p.kx, s_xf[1][ty + 1][tx] - s_xf[1][ty][tx]) -
-                           mul_const(p.inv_dy, p.ky, s_yf[2][ty][tx + 1] - s_yf[3][ty][tx]);
+        const double rh =
+            fsub<4>(x64::neg(mul_const(p.inv_dx, p.kx, fsub<4>(s_xf[0][ty + 1][tx], s_xf[0][ty][tx]))),
+                    mul_const(p.inv_dy, p.ky, fsub<4>(s_yf[0][ty][tx + 1], s_yf[0][ty][tx])));
+        const double rhu =
+            fsub<4>(x64::neg(mul_const(p.inv_dx, p.kx, fsub<4>(s_xf[2][ty + 1][tx], s_xf[3][ty][tx]))),
+                    mul_const(p.inv_dy, p.ky, fsub<4>(s_yf[1][ty][tx + 1], s_yf[1][ty][tx])));
+        const double rhv =
+            fsub<4>(x64::neg(mul_const(p.inv_dx, p.kx, fsub<4>(s_xf[1][ty + 1][tx], s_xf[1][ty][tx]))),
+                    mul_const(p.inv_dy, p.ky, fsub<4>(s_yf[2][ty][tx + 1], s_yf[3][ty][tx])));
         const long long k = (long long)(ii + NG) * P + (jj + NG);
         const double sh = s_h[ty + NG][tx + NG];
         const double shu = s_hu[ty + NG][tx + NG];
         const double shv = s_hv[ty + NG][tx + NG];
+        // U + dt * L(U)
+        const double eh = fadd<4>(sh, fmul<4>(dt, rh));
+        const double ehu = fadd<4>(shu, fmul<4>(dt, rhu));
+        const double ehv = fadd<4>(shv, fmul<4>(dt, rhv));
         double oh, ohu, ohv;
         if (STAGE == 1) {  // HPC_solver.hpp:246-248
-            oh = sh + dt * rh;
-            ohu = shu + dt * rhu;
-            ohv = shv + dt * rhv;
+            oh = eh;
+            ohu = ehu;
+            ohv = ehv;
         } else {
             const double nh = static_cast<const double *>(p.hn)[k];
             const double nhu = static_cast<const double *>(p.hun)[k];
             const double nhv = static_cast<const double *>(p.hvn)[k];
             if (STAGE == 2) {  // HPC_solver.hpp:271-273
-                oh = 0.75 * nh + x64::scale2(sh + dt * rh, -2, 0.25);
-                ohu = 0.75 * nhu + x64::scale2(shu + dt * rhu, -2, 0.25);
-                ohv = 0.75 * nhv + x64::scale2(shv + dt * rhv, -2, 0.25);
+                oh = fadd<4>(fmul<4>(0.75, nh), x64::scale2(eh, -2, 0.25));
+                ohu = fadd<4>(fmul<4>(0.75, nhu), x64::scale2(ehu, -2, 0.25));
+                ohv = fadd<4>(fmul<4>(0.75, nhv), x64::scale2(ehv, -2, 0.25));
             } else {  // HPC_solver.hpp:296-300
-                oh = (1.0 / 3.0) * nh + (2.0 / 3.0) * (sh + dt * rh);
-                ohu = (1.0 / 3.0) * nhu + (2.0 / 3.0) * (shu + dt * rhu);
-                ohv = (1.0 / 3.0) * nhv + (2.0 / 3.0) * (shv + dt * rhv);
+                oh = fadd<4>(fmul<4>(1.0 / 3.0, nh), fmul<4>(2.0 / 3.0, eh));
+                ohu = fadd<4>(fmul<4>(1.0 / 3.0, nhu), fmul<4>(2.0 / 3.0, ehu));
+                ohv = fadd<4>(fmul<4>(1.0 / 3.0, nhv), fmul<4>(2.0 / 3.0, ehv));
             }
         }
         // enforce_positivity (HPC_kernels.hpp:305-312)
