@@ -274,7 +274,8 @@ def form_ensemble(args, sw):
 
 def form_adjoint(args, sw):
     """Adjoint/forward cost on the 1024^2 adjoint workload (seeded bathymetry, 8 seeded
-    surface bumps, 64 gauges), fixed dt, binomial checkpointing with ~sqrt(steps) states."""
+    surface bumps, 64 gauges), fixed dt: binomial checkpointing with ~sqrt(steps) states,
+    every state stored, and the tape mode (every state and stage state kept)."""
     P = importlib.import_module("shallow-water_gb300.problems")
     n, K = args.adj_n, args.adj_steps
     rng = np.random.default_rng(args.seed + 7)
@@ -295,10 +296,13 @@ def form_adjoint(args, sw):
         s.upload(h, z, z, B)
         r = sw.adjoint.gauge_misfit_gradient(s, K, dt, gauges, obs, snaps)
         r_all = sw.adjoint.gauge_misfit_gradient(s, K, dt, gauges, obs, K)
+        r_tape = sw.adjoint.gauge_misfit_gradient(s, K, dt, gauges, obs, "tape")
     return {"grid": [n, n], "steps": K, "gauges": 64, "snapshots": snaps,
             "forward_ms": fwd_ms, "adjoint_ms": r["ms"], "ratio": r["ms"] / fwd_ms,
             "adjoint_ms_all_states_stored": r_all["ms"],
-            "ratio_all_states_stored": r_all["ms"] / fwd_ms}
+            "ratio_all_states_stored": r_all["ms"] / fwd_ms,
+            "adjoint_ms_tape": r_tape["ms"], "ratio_tape": r_tape["ms"] / fwd_ms,
+            "tape_bytes": int((75 * K + 400) * (n + 4) * (n + 4))}
 
 
 def run_forms(args, sw, fp64_gcups):

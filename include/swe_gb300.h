@@ -167,10 +167,14 @@ int swe_last_step_ms(const swe_ctx *ctx, double *ms);
  * hand-written discrete adjoint of each RK stage (the derivative of the branches the
  * forward pass takes: minmod, HLL regime, dry guards, positivity clamps).  States are
  * recomputed from n_snapshots stored states on a binomial (optimal offline) checkpoint
- * schedule.  Outputs, in the ghosted host layout with zero ghosts: J, dJ/dh^0,
+ * schedule.  n_snapshots = SWE_ADJ_TAPE_ALL instead keeps every state and every step's
+ * stage states and clamp masks from one forward sweep (device memory about
+ * (75 n_steps + 400) bytes per cell), so the reverse sweep recomputes nothing.
+ * Outputs, in the ghosted host layout with zero ghosts: J, dJ/dh^0,
  * dJ/dhu^0, dJ/dhv^0 and dJ/dB with the initial state held fixed, where the ghosts of B
  * are taken to follow the wall rule (mirror or copy of the interior).  ms (optional)
  * receives the device time.  FP64 contexts only.  No reference counterpart. */
+#define SWE_ADJ_TAPE_ALL (-1)
 int swe_adjoint_gauge(swe_ctx *ctx, int n_steps, double dt, int n_gauges, const int *gauge_i,
                       const int *gauge_j, const double *h_obs, int n_snapshots, double *J,
                       double *grad_h, double *grad_hu, double *grad_hv, double *grad_B,

@@ -36,6 +36,7 @@ EXPORTS = (
     "swe_totals_noalloc", "swe_adjoint_gauge", "swe_selftest_soft_f64",
 )
 TOTALS_NOALLOC_MAX_BLOCKS = 1024
+ADJ_TAPE_ALL = -1  # n_snapshots value of swe_adjoint_gauge's tape mode
 
 SHAPES = {"8x32": 0, "8x16": 1, "4x64": 2, "16x32": 3, "8x64": 4}
 

@@ -23,7 +23,8 @@ def gauge_misfit_gradient(solver: Solver, steps: int, dt: float, gauges, h_obs,
 
     ``gauges`` is a sequence of (i, j) interior cells, ``h_obs`` a (steps, n_gauges)
     array.  ``snapshots`` stored states drive the binomial checkpoint schedule (default
-    about sqrt(steps)).  Returns a dict with J, grad_h, grad_hu, grad_hv, grad_B (ghosted
+    about sqrt(steps)); ``snapshots="tape"`` keeps every state and every step's stage
+    states instead (no recomputation, about 75 bytes per cell and step).  Returns a dict with J, grad_h, grad_hu, grad_hv, grad_B (ghosted
     arrays, zero ghosts; grad_B holds the initial state fixed) and ms (device time)."""
     g = np.asarray(gauges, dtype=np.int32).reshape(-1, 2)
     gi = np.ascontiguousarray(g[:, 0])
@@ -31,6 +32,8 @@ def gauge_misfit_gradient(solver: Solver, steps: int, dt: float, gauges, h_obs,
     obs = np.ascontiguousarray(h_obs, dtype=np.float64).reshape(steps, len(gi))
     if snapshots is None:
         snapshots = max(1, int(round(np.sqrt(steps))))
+    elif snapshots == "tape":
+        snapshots = L.ADJ_TAPE_ALL
     shape = (solver.Nx + 4, solver.Ny + 4)
     out = [np.zeros(shape) for _ in range(4)]
     J = ctypes.c_double()

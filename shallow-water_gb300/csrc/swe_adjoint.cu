@@ -7,11 +7,12 @@
 // One adjoint step (transition k -> k+1, U^k in the work buffer):
 //  1. recompute the three stages with clamp masks, U^(k+1) into a separate buffer;
 //  2. add the gauge source 2 (h - h_obs) of step k+1 to lambda and accumulate J;
-//  3. reverse stages 3, 2, 1 with k_adj_stage: per tile, recompute every interface whose
-//     stencil touches the tile, apply its VJP (swe_adjoint_math.cuh) to the adjoint of the
-//     divergence, and gather the contributions per cell (ghost slots folded onto the
-//     interior cells they mirror, normal momentum negated at reflecting walls).  No
-//     atomics: the result does not depend on scheduling.
+//  3. reverse stages 3, 2, 1, each in two passes: k_adj_faces applies the VJP of every
+//     x- and y-interface once (swe_adjoint_math.cuh) to the adjoint of the divergence and
+//     stores its 14 stencil contributions; k_adj_gather sums, per cell, the contributions
+//     of the interfaces whose stencil holds it (ghost slots folded onto the interior
+//     cells they mirror, normal momentum negated at reflecting walls).  No atomics: the
+//     result does not depend on scheduling.
 // States U^k come from a binomial checkpoint schedule over `n_snapshots` stored states,
 // chosen by dynamic programming to minimise the number of recomputed forward steps
 // (Griewank-Walther binomial checkpointing, cost recursion
@@ -31,21 +32,9 @@
 namespace swe {
 namespace {
 
-#ifndef SWE_ADJ_MIN_BLOCKS
-#define SWE_ADJ_MIN_BLOCKS 1  // resident CTAs per SM the register budget is sized for
-#endif
-
-constexpr int ATI = 8, ATJ = 32;
-constexpr int ANT = (ATI + 3) * ATJ;       // one thread per x-face of the gather region
-constexpr int SR = ATI + 6, SC = ATJ + 6;  // state tile, halo 3
-constexpr int WR = ATI + 4, WC = ATJ + 4;  // divergence-adjoint tile, halo 2
-constexpr int CR = ATI + 3, CC = ATJ + 3;  // contribution buffer (x: CR x ATJ, y: ATI x CC)
-
-struct AdjSmem {
-    double h[SR][SC], hu[SR][SC], hv[SR][SC], B[SR][SC], eta[SR][SC];
-    double w[3][WR][WC];
-    double C[14][CR][CC];  // per face: eta(4), qn(4), qt(4), bm, bp
-};
+constexpr int AFT = 128;  // threads per block of the interface pass
+constexpr int AGT = 256;  // threads per block of the gather pass
+constexpr int NC = 14;    // contributions per interface: eta(4), qn(4), qt(4), bm, bp
 
 struct AdjParams {
     const double *h, *hu, *hv, *B;       // stage source state, bathymetry
@@ -54,11 +43,87 @@ struct AdjParams {
     double *ls_h, *ls_hu, *ls_hv;        // adjoint of the stage source (written)
     double *ln_h, *ln_hu, *ln_hv;        // adjoint of U^n (stage 3 writes, 2 adds, 1 reads)
     double *gB;                          // dJ/dB (accumulated)
+    double *cx, *cy;                     // interface contributions, NC planes each
+    long long px, py;                    // plane sizes: (Nx + 1) * Ny, Nx * (Ny + 1)
     int Nx, Ny;
     long long pitch;
     int bc;
     double inv_dx, inv_dy, g, dt;
 };
+
+// Adjoint of the divergence at interior cell (i, j): cs * dt * lo, zero where the stage
+// clamped the depth (its output did not depend on the fluxes there) and outside.
+template <int STAGE>
+__device__ __forceinline__ void w_at(const AdjParams &a, int i, int j, double w[3]) {
+    constexpr double cs = STAGE == 1 ? 1.0 : (STAGE == 2 ? 0.25 : 2.0 / 3.0);
+    w[0] = w[1] = w[2] = 0.0;
+    if (i < 0 || i >= a.Nx || j < 0 || j >= a.Ny) return;
+    const long long k = (long long)(i + NG) * a.pitch + (j + NG);
+    if (a.mask[k]) return;
+    const double f = cs * a.dt;
+    w[0] = f * a.lo_h[k];
+    w[1] = f * a.lo_hu[k];
+    w[2] = f * a.lo_hv[k];
+}
+
+// One interface per thread.  DIR 0: x-interface f in [-1, Nx - 1] between rows f and
+// f + 1 at column j; DIR 1: y-interface f in [-1, Ny - 1] between columns f and f + 1 at
+// row i.  The stencil is staged exactly as the forward kernel stages it: the state of
+// ghost cells from the mirrored (reflecting, normal momentum negated) or clamped
+// (transmissive) interior cell, B where it lies, ghosts included.
+template <int STAGE, int DIR>
+__global__ void __launch_bounds__(AFT) k_adj_faces(const AdjParams a) {
+    const int t = blockIdx.x * AFT + threadIdx.x;
+    const int along = DIR == 0 ? a.Ny : a.Ny + 1;  // contiguous index range
+    if (t >= along) return;
+    const int f = DIR == 0 ? (int)blockIdx.y - 1 : t - 1;  // interface index
+    const int o = DIR == 0 ? t : (int)blockIdx.y;          // the other coordinate
+    const long long P = a.pitch;
+    adj::FaceIn<double> in;
+    for (int q = 0; q < 4; ++q) {
+        const int c = f - 1 + q;  // stencil cell along the normal
+        bool fl;
+        const int m = map_coord(c, DIR == 0 ? a.Nx : a.Ny, a.bc, fl);
+        const long long ks = DIR == 0 ? (long long)(m + NG) * P + (o + NG)
+                                      : (long long)(o + NG) * P + (m + NG);
+        const int cb = clamp_int(c + NG, 0, (DIR == 0 ? a.Nx : a.Ny) + 3);
+        const long long kb = DIR == 0 ? (long long)cb * P + (o + NG) : (long long)(o + NG) * P + cb;
+        const double b = a.B[kb];
+        const double qn = DIR == 0 ? a.hu[ks] : a.hv[ks];
+        in.e[q] = a.h[ks] + b;
+        in.n[q] = fl ? -qn : qn;
+        in.t[q] = DIR == 0 ? a.hv[ks] : a.hu[ks];
+        if (q == 1) in.bm = b;
+        if (q == 2) in.bp = b;
+    }
+    double wm[3], wp[3];
+    if (DIR == 0) {
+        w_at<STAGE>(a, f, o, wm);
+        w_at<STAGE>(a, f + 1, o, wp);
+    } else {
+        w_at<STAGE>(a, o, f, wm);
+        w_at<STAGE>(a, o, f + 1, wp);
+    }
+    const double inv = DIR == 0 ? a.inv_dx : a.inv_dy;
+    const int n = DIR == 0 ? 1 : 2, tg = DIR == 0 ? 2 : 1;  // normal / tangential field
+    adj::FaceOut<double> d;
+    d.fh = inv * (wp[0] - wm[0]);
+    d.fqt = inv * (wp[tg] - wm[tg]);
+    d.fqn_m = -inv * wm[n];
+    d.fqn_p = inv * wp[n];
+    adj::FaceIn<double> ad;
+    adj::face_vjp(in, a.g, EPS, d, ad);
+    double *C = DIR == 0 ? a.cx : a.cy;
+    const long long pl = DIR == 0 ? a.px : a.py;
+    const long long idx = DIR == 0 ? (long long)(f + 1) * a.Ny + o : (long long)o * (a.Ny + 1) + (f + 1);
+    for (int q = 0; q < 4; ++q) {
+        C[(q)*pl + idx] = ad.e[q];
+        C[(4 + q) * pl + idx] = ad.n[q];
+        C[(8 + q) * pl + idx] = ad.t[q];
+    }
+    C[12 * pl + idx] = ad.bm;
+    C[13 * pl + idx] = ad.bp;
+}
 
 // Interior coordinate a plus the ghost coordinates whose values are copies of cell a
 // (reflecting: mirrored, normal component negated; transmissive: clamped).
@@ -92,174 +157,54 @@ __device__ __forceinline__ int virtual_coords(int a, int N, int bc, int *v, bool
     return n;
 }
 
+// Sums, for interior cell a along one direction (rows for DIR 0, columns for DIR 1), the
+// contributions of the interfaces whose stencil holds a or a ghost copy of it.
+template <int DIR>
+__device__ __forceinline__ void gather_dir(const AdjParams &a, int ca, int other, double &acc_h,
+                                           double &acc_qn, double &acc_qt, double &acc_B) {
+    const int N = DIR == 0 ? a.Nx : a.Ny;
+    const double *C = DIR == 0 ? a.cx : a.cy;
+    const long long pl = DIR == 0 ? a.px : a.py;
+    auto at = [&](int f) {  // linear index of interface f (valid range [-1, N - 1])
+        return DIR == 0 ? (long long)(f + 1) * a.Ny + other : (long long)other * (a.Ny + 1) + (f + 1);
+    };
+    int v[5];
+    bool fl[5];
+    const int nv = virtual_coords(ca, N, a.bc, v, fl);
+    for (int q = 0; q < nv; ++q) {
+        for (int k = 0; k < 4; ++k) {
+            const int f = v[q] + 1 - k;  // interface whose stencil slot k is cell v
+            if (f < -1 || f > N - 1) continue;
+            const long long x = at(f);
+            const double ce = C[k * pl + x], cn = C[(4 + k) * pl + x];
+            acc_h += ce;
+            acc_B += ce;
+            acc_qn += fl[q] ? -cn : cn;
+            acc_qt += C[(8 + k) * pl + x];
+        }
+        const int fm = v[q], fp = v[q] - 1;  // interfaces with cell v as minus / plus side
+        if (fm >= -1 && fm <= N - 1) acc_B += C[12 * pl + at(fm)];
+        if (fp >= -1 && fp <= N - 1) acc_B += C[13 * pl + at(fp)];
+    }
+}
+
+// Per interior cell: adjoint of the stage source and of U^n, and dJ/dB.
 template <int STAGE>
-__global__ void __launch_bounds__(ANT, SWE_ADJ_MIN_BLOCKS) k_adj_stage(const AdjParams a) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    AdjSmem &S = *reinterpret_cast<AdjSmem *>(smem_raw);
-    const int tid = threadIdx.x;
-    const int i0 = blockIdx.y * ATI, j0 = blockIdx.x * ATJ;
-    const long long P = a.pitch;
-    const double cs = STAGE == 1 ? 1.0 : (STAGE == 2 ? 0.25 : 2.0 / 3.0);
-
-    for (int t = tid; t < SR * SC; t += ANT) {
-        const int r = t / SC, c = t - (t / SC) * SC;
-        const int ii = i0 - 3 + r, jj = j0 - 3 + c;
-        bool fx, fy;
-        const int mi = map_coord(ii, a.Nx, a.bc, fx), mj = map_coord(jj, a.Ny, a.bc, fy);
-        const long long k = (long long)(mi + NG) * P + (mj + NG);
-        const double h = a.h[k], hu = a.hu[k], hv = a.hv[k];
-        const int bi = clamp_int(ii + NG, 0, a.Nx + 3), bj = clamp_int(jj + NG, 0, a.Ny + 3);
-        const double b = a.B[(long long)bi * P + bj];
-        S.h[r][c] = h;
-        S.hu[r][c] = fx ? -hu : hu;
-        S.hv[r][c] = fy ? -hv : hv;
-        S.B[r][c] = b;
-        S.eta[r][c] = h + b;
-    }
-    for (int t = tid; t < WR * WC; t += ANT) {
-        const int r = t / WC, c = t - (t / WC) * WC;
-        const int ii = i0 - 2 + r, jj = j0 - 2 + c;
-        double w0 = 0.0, w1 = 0.0, w2 = 0.0;
-        if (ii >= 0 && ii < a.Nx && jj >= 0 && jj < a.Ny) {
-            const long long k = (long long)(ii + NG) * P + (jj + NG);
-            if (!a.mask[k]) {
-                const double f = cs * a.dt;
-                w0 = f * a.lo_h[k];
-                w1 = f * a.lo_hu[k];
-                w2 = f * a.lo_hv[k];
-            }
-        }
-        S.w[0][r][c] = w0;
-        S.w[1][r][c] = w1;
-        S.w[2][r][c] = w2;
-    }
-    __syncthreads();
-
-    // ---- x-faces f in [i0-2, i0+ATI]: one per thread ----
-    {
-        const int fr = tid / ATJ, col = tid - (tid / ATJ) * ATJ;
-        const int f = i0 - 2 + fr, jj = j0 + col;
-        adj::FaceIn<double> ad;
-        for (int q = 0; q < 4; ++q) ad.e[q] = ad.n[q] = ad.t[q] = 0.0;
-        ad.bm = ad.bp = 0.0;
-        if (f >= -1 && f <= a.Nx - 1 && jj < a.Ny) {
-            adj::FaceIn<double> in;
-            for (int q = 0; q < 4; ++q) {
-                in.e[q] = S.eta[fr + q][col + 3];
-                in.n[q] = S.hu[fr + q][col + 3];
-                in.t[q] = S.hv[fr + q][col + 3];
-            }
-            in.bm = S.B[fr + 1][col + 3];
-            in.bp = S.B[fr + 2][col + 3];
-            adj::FaceOut<double> d;
-            d.fh = a.inv_dx * (S.w[0][fr + 1][col + 2] - S.w[0][fr][col + 2]);
-            d.fqt = a.inv_dx * (S.w[2][fr + 1][col + 2] - S.w[2][fr][col + 2]);
-            d.fqn_m = -a.inv_dx * S.w[1][fr][col + 2];
-            d.fqn_p = a.inv_dx * S.w[1][fr + 1][col + 2];
-            adj::face_vjp(in, a.g, EPS, d, ad);
-        }
-        for (int q = 0; q < 4; ++q) {
-            S.C[q][fr][col] = ad.e[q];
-            S.C[4 + q][fr][col] = ad.n[q];
-            S.C[8 + q][fr][col] = ad.t[q];
-        }
-        S.C[12][fr][col] = ad.bm;
-        S.C[13][fr][col] = ad.bp;
-    }
-    __syncthreads();
-
-    const int ty = tid / ATJ, tx = tid - (tid / ATJ) * ATJ;
-    const int ci = i0 + ty, cj = j0 + tx;
-    const bool own = tid < ATI * ATJ && ci < a.Nx && cj < a.Ny;
+__global__ void __launch_bounds__(AGT) k_adj_gather(const AdjParams a) {
+    const int cj = blockIdx.x * AGT + threadIdx.x, ci = blockIdx.y;
+    if (cj >= a.Ny) return;
+    constexpr double cs = STAGE == 1 ? 1.0 : (STAGE == 2 ? 0.25 : 2.0 / 3.0);
     double acc_h = 0.0, acc_hu = 0.0, acc_hv = 0.0, acc_B = 0.0;
-    if (own) {
-        int v[5];
-        bool fl[5];
-        const int nv = virtual_coords(ci, a.Nx, a.bc, v, fl);
-        for (int q = 0; q < nv; ++q) {
-            for (int k = 0; k < 4; ++k) {
-                const int f = v[q] + 1 - k;  // face whose stencil slot k is row v
-                const int fr = f - i0 + 2;
-                if (f < -1 || f > a.Nx - 1 || fr < 0 || fr >= CR) continue;
-                const double ce = S.C[k][fr][tx], cn = S.C[4 + k][fr][tx];
-                acc_h += ce;
-                acc_B += ce;
-                acc_hu += fl[q] ? -cn : cn;
-                acc_hv += S.C[8 + k][fr][tx];
-            }
-            const int fm = v[q], fp = v[q] - 1;  // faces with row v as minus / plus cell
-            if (fm >= -1 && fm <= a.Nx - 1 && fm - i0 + 2 >= 0 && fm - i0 + 2 < CR)
-                acc_B += S.C[12][fm - i0 + 2][tx];
-            if (fp >= -1 && fp <= a.Nx - 1 && fp - i0 + 2 >= 0 && fp - i0 + 2 < CR)
-                acc_B += S.C[13][fp - i0 + 2][tx];
-        }
-    }
-    __syncthreads();
-
-    // ---- y-faces f in [j0-2, j0+ATJ] for the tile rows ----
-    if (tid < ATI * CC) {
-        const int row = tid / CC, gc = tid - (tid / CC) * CC;
-        const int f = j0 - 2 + gc, ii = i0 + row;
-        adj::FaceIn<double> ad;
-        for (int q = 0; q < 4; ++q) ad.e[q] = ad.n[q] = ad.t[q] = 0.0;
-        ad.bm = ad.bp = 0.0;
-        if (f >= -1 && f <= a.Ny - 1 && ii < a.Nx) {
-            adj::FaceIn<double> in;
-            for (int q = 0; q < 4; ++q) {
-                in.e[q] = S.eta[row + 3][gc + q];
-                in.n[q] = S.hv[row + 3][gc + q];
-                in.t[q] = S.hu[row + 3][gc + q];
-            }
-            in.bm = S.B[row + 3][gc + 1];
-            in.bp = S.B[row + 3][gc + 2];
-            adj::FaceOut<double> d;
-            d.fh = a.inv_dy * (S.w[0][row + 2][gc + 1] - S.w[0][row + 2][gc]);
-            d.fqt = a.inv_dy * (S.w[1][row + 2][gc + 1] - S.w[1][row + 2][gc]);
-            d.fqn_m = -a.inv_dy * S.w[2][row + 2][gc];
-            d.fqn_p = a.inv_dy * S.w[2][row + 2][gc + 1];
-            adj::face_vjp(in, a.g, EPS, d, ad);
-        }
-        for (int q = 0; q < 4; ++q) {
-            S.C[q][row][gc] = ad.e[q];
-            S.C[4 + q][row][gc] = ad.n[q];
-            S.C[8 + q][row][gc] = ad.t[q];
-        }
-        S.C[12][row][gc] = ad.bm;
-        S.C[13][row][gc] = ad.bp;
-    }
-    __syncthreads();
-
-    if (!own) return;
-    {
-        int v[5];
-        bool fl[5];
-        const int nv = virtual_coords(cj, a.Ny, a.bc, v, fl);
-        for (int q = 0; q < nv; ++q) {
-            for (int k = 0; k < 4; ++k) {
-                const int f = v[q] + 1 - k;
-                const int gc = f - j0 + 2;
-                if (f < -1 || f > a.Ny - 1 || gc < 0 || gc >= CC) continue;
-                const double ce = S.C[k][ty][gc], cn = S.C[4 + k][ty][gc];
-                acc_h += ce;
-                acc_B += ce;
-                acc_hv += fl[q] ? -cn : cn;
-                acc_hu += S.C[8 + k][ty][gc];
-            }
-            const int fm = v[q], fp = v[q] - 1;
-            if (fm >= -1 && fm <= a.Ny - 1 && fm - j0 + 2 >= 0 && fm - j0 + 2 < CC)
-                acc_B += S.C[12][ty][fm - j0 + 2];
-            if (fp >= -1 && fp <= a.Ny - 1 && fp - j0 + 2 >= 0 && fp - j0 + 2 < CC)
-                acc_B += S.C[13][ty][fp - j0 + 2];
-        }
-    }
-    const long long k = (long long)(ci + NG) * P + (cj + NG);
+    gather_dir<0>(a, ci, cj, acc_h, acc_hu, acc_hv, acc_B);
+    gather_dir<1>(a, cj, ci, acc_h, acc_hv, acc_hu, acc_B);
+    const long long k = (long long)(ci + NG) * a.pitch + (cj + NG);
     const bool m = a.mask[k];
     const double l0 = m ? 0.0 : a.lo_h[k], l1 = m ? 0.0 : a.lo_hu[k], l2 = m ? 0.0 : a.lo_hv[k];
     double o0 = acc_h + cs * l0, o1 = acc_hu + cs * l1, o2 = acc_hv + cs * l2;
-    if (STAGE == 3) {
-        a.ln_h[k] = l0 / 3.0;
-        a.ln_hu[k] = l1 / 3.0;
-        a.ln_hv[k] = l2 / 3.0;
+    if (STAGE == 3) {  // the forward's (1.0 / 3.0) * U^n
+        a.ln_h[k] = (1.0 / 3.0) * l0;
+        a.ln_hu[k] = (1.0 / 3.0) * l1;
+        a.ln_hv[k] = (1.0 / 3.0) * l2;
     } else if (STAGE == 2) {
         a.ln_h[k] += 0.75 * l0;
         a.ln_hu[k] += 0.75 * l1;
@@ -296,6 +241,10 @@ struct Adj {
     double *snap;
     int S;
     double *W[3], *Un1[3], *lam[3], *lamA[3], *lamB[3], *ln[3], *gB;
+    double *cx, *cy;  // interface contributions of the stage being reversed
+    bool tape = false;              // every state and every step's stage states kept
+    double *tU1 = nullptr, *tU2 = nullptr;  // tape: U^(1), U^(2) of step k at 3 k fields
+    unsigned char *tmask = nullptr;         // tape: clamp masks of step k at 3 k fields
     unsigned char *mask[3];
     int *gi, *gj;
     double *obs, *J;
@@ -335,28 +284,37 @@ StageParams fwd_params(const Adj &A) {
     return sp;
 }
 
-// One forward step W -> out (out may be W); masks optional.
-cudaError_t forward_step(Adj &A, double *const *W, double *const *out, bool masks) {
+// One forward step W -> out (out may be W) with the stage states in U1, U2 and the
+// clamp masks in mk[0..2] (null: not kept).
+cudaError_t forward_step_into(Adj &A, double *const *W, double *const *out, double *const *U1,
+                              double *const *U2, unsigned char *const *mk) {
     swe_ctx *c = A.c;
     StageParams sp = fwd_params(A);
-    double *U1[3] = {(double *)c->U1[0], (double *)c->U1[1], (double *)c->U1[2]};
-    double *U2[3] = {(double *)c->U2[0], (double *)c->U2[1], (double *)c->U2[2]};
     sp.hn = W[0]; sp.hun = W[1]; sp.hvn = W[2];
     sp.hs = W[0]; sp.hus = W[1]; sp.hvs = W[2];
     sp.ho = U1[0]; sp.huo = U1[1]; sp.hvo = U1[2];
-    sp.mask = masks ? A.mask[0] : nullptr;
+    sp.mask = mk[0];
     ACK(launch_stage_f64(1, sp, c->stream));
     sp.hs = U1[0]; sp.hus = U1[1]; sp.hvs = U1[2];
     sp.ho = U2[0]; sp.huo = U2[1]; sp.hvo = U2[2];
-    sp.mask = masks ? A.mask[1] : nullptr;
+    sp.mask = mk[1];
     ACK(launch_stage_f64(2, sp, c->stream));
     sp.hs = U2[0]; sp.hus = U2[1]; sp.hvs = U2[2];
     sp.ho = out[0]; sp.huo = out[1]; sp.hvo = out[2];
-    sp.mask = masks ? A.mask[2] : nullptr;
+    sp.mask = mk[2];
     ACK(launch_stage_f64(3, sp, c->stream));
     c->launches += 3;
     ++A.fwd_steps;
     return cudaSuccess;
+}
+
+// One forward step W -> out through the context's stage buffers; masks optional.
+cudaError_t forward_step(Adj &A, double *const *W, double *const *out, bool masks) {
+    swe_ctx *c = A.c;
+    double *U1[3] = {(double *)c->U1[0], (double *)c->U1[1], (double *)c->U1[2]};
+    double *U2[3] = {(double *)c->U2[0], (double *)c->U2[1], (double *)c->U2[2]};
+    unsigned char *none[3] = {nullptr, nullptr, nullptr};
+    return forward_step_into(A, W, out, U1, U2, masks ? A.mask : none);
 }
 
 cudaError_t launch_adj(Adj &A, int stage, double *const *state, double *const *lo,
@@ -378,13 +336,30 @@ cudaError_t launch_adj(Adj &A, int stage, double *const *state, double *const *l
     p.inv_dy = c->inv_dy;
     p.g = c->p.g;
     p.dt = A.dt;
-    const dim3 grid((c->p.Ny + ATJ - 1) / ATJ, (c->p.Nx + ATI - 1) / ATI);
-    const size_t smem = sizeof(AdjSmem);
+    p.cx = A.cx;
+    p.cy = A.cy;
+    p.px = (long long)(c->p.Nx + 1) * c->p.Ny;
+    p.py = (long long)c->p.Nx * (c->p.Ny + 1);
+    const dim3 gx((c->p.Ny + AFT - 1) / AFT, c->p.Nx + 1), gy((c->p.Ny + 1 + AFT - 1) / AFT, c->p.Nx);
+    const dim3 gg((c->p.Ny + AGT - 1) / AGT, c->p.Nx);
     switch (stage) {
-        case 1: k_adj_stage<1><<<grid, ANT, smem, c->stream>>>(p); break;
-        case 2: k_adj_stage<2><<<grid, ANT, smem, c->stream>>>(p); break;
-        default: k_adj_stage<3><<<grid, ANT, smem, c->stream>>>(p); break;
+        case 1:
+            k_adj_faces<1, 0><<<gx, AFT, 0, c->stream>>>(p);
+            k_adj_faces<1, 1><<<gy, AFT, 0, c->stream>>>(p);
+            k_adj_gather<1><<<gg, AGT, 0, c->stream>>>(p);
+            break;
+        case 2:
+            k_adj_faces<2, 0><<<gx, AFT, 0, c->stream>>>(p);
+            k_adj_faces<2, 1><<<gy, AFT, 0, c->stream>>>(p);
+            k_adj_gather<2><<<gg, AGT, 0, c->stream>>>(p);
+            break;
+        default:
+            k_adj_faces<3, 0><<<gx, AFT, 0, c->stream>>>(p);
+            k_adj_faces<3, 1><<<gy, AFT, 0, c->stream>>>(p);
+            k_adj_gather<3><<<gg, AGT, 0, c->stream>>>(p);
+            break;
     }
+    c->launches += 2;
     ++c->launches;
     return cudaGetLastError();
 }
@@ -422,6 +397,44 @@ cudaError_t load_slot(Adj &A, int slot) {
 cudaError_t store_slot(Adj &A, int slot) {
     double *dst[3] = {slot_field(A, slot, 0), slot_field(A, slot, 1), slot_field(A, slot, 2)};
     return copy_state(A, dst, A.W);
+}
+
+double *tape_field(double *base, Adj &A, int k, int f) { return base + ((size_t)k * 3 + f) * A.fe; }
+
+// Tape mode: one forward sweep keeps U^k in slot k and the stage states and clamp masks
+// of step k in the tape; the reverse sweep then recomputes nothing.
+cudaError_t taped(Adj &A, int n) {
+    swe_ctx *c = A.c;
+    for (int k = 0; k < n; ++k) {
+        double *W[3], *out[3], *U1[3], *U2[3];
+        unsigned char *mk[3];
+        for (int f = 0; f < 3; ++f) {
+            W[f] = slot_field(A, k, f);
+            out[f] = slot_field(A, k + 1, f);
+            U1[f] = tape_field(A.tU1, A, k, f);
+            U2[f] = tape_field(A.tU2, A, k, f);
+            mk[f] = A.tmask + ((size_t)k * 3 + f) * A.fe;
+        }
+        ACK(forward_step_into(A, W, out, U1, U2, mk));
+    }
+    for (int k = n - 1; k >= 0; --k) {
+        double *Wk[3], *U1[3], *U2[3];
+        const unsigned char *mk[3];
+        for (int f = 0; f < 3; ++f) {
+            Wk[f] = slot_field(A, k, f);
+            U1[f] = tape_field(A.tU1, A, k, f);
+            U2[f] = tape_field(A.tU2, A, k, f);
+            mk[f] = A.tmask + ((size_t)k * 3 + f) * A.fe;
+        }
+        k_gauge<<<1, 32, 0, c->stream>>>(slot_field(A, k + 1, 0), c->pitch, A.gi, A.gj, A.ng,
+                                         A.obs + (size_t)k * A.ng, A.lam[0], A.J);
+        ++c->launches;
+        ACK(cudaGetLastError());
+        ACK(launch_adj(A, 3, U2, A.lam, mk[2], A.lamA));
+        ACK(launch_adj(A, 2, U1, A.lamA, mk[1], A.lamB));
+        ACK(launch_adj(A, 1, Wk, A.lamB, mk[0], A.lam));
+    }
+    return cudaSuccess;
 }
 
 // Adjoint of steps [l, l+n) with U^l in `slot` and s free snapshot slots.
@@ -479,8 +492,6 @@ void build_schedule(Adj &A, int N, int S) {
     }
 }
 
-bool adj_attr_set = false;
-
 }  // namespace
 }  // namespace swe
 
@@ -492,7 +503,8 @@ extern "C" int swe_adjoint_gauge(swe_ctx *c, int n_steps, double dt, int n_gauge
                                  double *grad_hv, double *grad_B, double *ms) {
     if (!c) return SWE_ERR_BAD_ARG;
     if (!c->uploaded || c->p.precision != SWE_PRECISION_FP64 || n_steps < 1 || !(dt > 0.0) ||
-        n_gauges < 0 || (n_gauges > 0 && (!gauge_i || !gauge_j || !h_obs)) || n_snapshots < 0 ||
+        n_gauges < 0 || (n_gauges > 0 && (!gauge_i || !gauge_j || !h_obs)) ||
+        (n_snapshots < 0 && n_snapshots != SWE_ADJ_TAPE_ALL) ||
         !J || !grad_h || !grad_hu || !grad_hv || !grad_B) {
         c->err = "swe_adjoint_gauge: bad argument (needs an uploaded FP64 context)";
         return SWE_ERR_BAD_ARG;
@@ -503,24 +515,22 @@ extern "C" int swe_adjoint_gauge(swe_ctx *c, int n_steps, double dt, int n_gauge
             return SWE_ERR_BAD_ARG;
         }
     if (cudaSetDevice(c->p.device) != cudaSuccess) return SWE_ERR_CUDA;
-    if (!adj_attr_set) {
-        for (auto k : {k_adj_stage<1>, k_adj_stage<2>, k_adj_stage<3>})
-            if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)sizeof(AdjSmem)) != cudaSuccess) {
-                c->err = "swe_adjoint_gauge: cannot opt in to the adjoint kernel's shared memory";
-                return SWE_ERR_CUDA;
-            }
-        adj_attr_set = true;
-    }
     Adj A;
     A.c = c;
     A.fe = c->field_elems;
-    A.S = std::min(n_snapshots, n_steps);
+    A.tape = n_snapshots == SWE_ADJ_TAPE_ALL;
+    A.S = A.tape ? n_steps : std::min(n_snapshots, n_steps);
     A.ng = n_gauges;
     A.dt = dt;
     const size_t fb = A.fe * sizeof(double);
     auto rounded = [](size_t n) { return (n + 255) / 256 * 256; };
+    const size_t cx_bytes = (size_t)NC * (c->p.Nx + 1) * c->p.Ny * sizeof(double);
+    const size_t cy_bytes = (size_t)NC * c->p.Nx * (c->p.Ny + 1) * sizeof(double);
     const size_t bytes = rounded((size_t)(A.S + 1) * 3 * fb) + 19 * rounded(fb) + 3 * rounded(A.fe) +
+                         rounded(cx_bytes) + rounded(cy_bytes) +
+                         (A.tape ? 2 * rounded((size_t)n_steps * 3 * fb) +
+                                       rounded((size_t)n_steps * 3 * A.fe)
+                                 : 0) +
                          2 * rounded(sizeof(int) * (n_gauges + 1)) +
                          rounded(sizeof(double) * ((size_t)n_steps * n_gauges + 1)) +
                          rounded(sizeof(double)) + rounded(2 * sizeof(unsigned long long));
@@ -552,6 +562,13 @@ extern "C" int swe_adjoint_gauge(swe_ctx *c, int n_steps, double dt, int n_gauge
         A.mask[f] = (unsigned char *)take(A.fe);
     }
     A.gB = (double *)take(fb);
+    A.cx = (double *)take(cx_bytes);
+    A.cy = (double *)take(cy_bytes);
+    if (A.tape) {
+        A.tU1 = (double *)take((size_t)n_steps * 3 * fb);
+        A.tU2 = (double *)take((size_t)n_steps * 3 * fb);
+        A.tmask = (unsigned char *)take((size_t)n_steps * 3 * A.fe);
+    }
     A.gi = (int *)take(sizeof(int) * (n_gauges + 1));
     A.gj = (int *)take(sizeof(int) * (n_gauges + 1));
     A.obs = (double *)take(sizeof(double) * ((size_t)n_steps * n_gauges + 1));
@@ -576,9 +593,9 @@ extern "C" int swe_adjoint_gauge(swe_ctx *c, int n_steps, double dt, int n_gauge
     if (e == cudaSuccess) e = copy_state(A, A.W, Un);
     if (e == cudaSuccess) e = store_slot(A, 0);
     if (e != cudaSuccess) return fail(e);
-    build_schedule(A, n_steps, A.S);
+    if (!A.tape) build_schedule(A, n_steps, A.S);
     cudaEventRecord(e0, st);
-    e = reverse(A, 0, n_steps, 0, A.S);
+    e = A.tape ? taped(A, n_steps) : reverse(A, 0, n_steps, 0, A.S);
     cudaEventRecord(e1, st);
     if (e != cudaSuccess) return fail(e);
     double Jh = 0.0;

@@ -15,6 +15,9 @@
 #pragma once
 
 #include <cmath>
+#include <type_traits>
+
+#include "swe_soft_f64.cuh"
 
 #if defined(__CUDACC__)
 #define SWE_HD __host__ __device__ __forceinline__
@@ -96,6 +99,55 @@ SWE_HD void face_forward(const FaceIn<T> &in, T g, T eps, FaceOut<T> &out) {
     out.fqn_p = F[1] + half * g * (h_p * h_p - hR * hR);
 }
 
+// Branch tests and reciprocals of face_vjp.  For double they work on the bit patterns
+// (the same decisions as the IEEE comparisons for every non-NaN operand) and the
+// reciprocal is the correctly rounded integer-pipe division, so the GPU spends its
+// scarce FP64 slots on the arithmetic alone.
+template <class T>
+SWE_HD bool lt_(T a, T b) {
+    if constexpr (std::is_same<T, double>::value) return x64::lt(a, b);
+    else return a < b;
+}
+template <class T>
+SWE_HD bool pos_(T a) {  // a > 0
+    if constexpr (std::is_same<T, double>::value) {
+        const int64_t b = x64::bits(a);
+        return b > 0 && b <= x64::INF_BITS;
+    } else {
+        return a > T(0);
+    }
+}
+template <class T>
+SWE_HD T rcp_(T a) {
+    if constexpr (std::is_same<T, double>::value) return sf::div_rn(1.0, a);
+    else return T(1) / a;
+}
+template <class T>
+SWE_HD T half_(T a) {  // 0.5 * a, exact
+    if constexpr (std::is_same<T, double>::value) return x64::halve(a);
+    else return T(0.5) * a;
+}
+// minmod_sel with the sign and magnitude tests on the bit patterns for double.
+template <class T>
+SWE_HD T msel_(T a, T b, int &sel) {
+    if constexpr (std::is_same<T, double>::value) {
+        const int64_t ba = x64::bits(a), bb = x64::bits(b);
+        const int64_t ma = ba & x64::ABS, mb = bb & x64::ABS;
+        if (ma == 0 || mb == 0 || (ba ^ bb) < 0) {
+            sel = 0;
+            return T(0);
+        }
+        if (mb < ma) {
+            sel = 2;
+            return b;
+        }
+        sel = 1;
+        return a;
+    } else {
+        return minmod_sel(a, b, sel);
+    }
+}
+
 template <class T>
 SWE_HD T trsqrt(T x) {
 #if defined(__CUDA_ARCH__)
@@ -121,38 +173,38 @@ SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceI
     const T de0 = in.e[1] - in.e[0], de1 = in.e[2] - in.e[1], de2 = in.e[3] - in.e[2];
     const T dn0 = in.n[1] - in.n[0], dn1 = in.n[2] - in.n[1], dn2 = in.n[3] - in.n[2];
     const T dt0 = in.t[1] - in.t[0], dt1 = in.t[2] - in.t[1], dt2 = in.t[3] - in.t[2];
-    const T eta_m = in.e[1] + half * minmod_sel(de0, de1, s_em);
-    const T eta_p = in.e[2] - half * minmod_sel(de1, de2, s_ep);
-    const T qn_m = in.n[1] + half * minmod_sel(dn0, dn1, s_nm);
-    const T qt_m = in.t[1] + half * minmod_sel(dt0, dt1, s_tm);
-    const T qn_p = in.n[2] - half * minmod_sel(dn1, dn2, s_np);
-    const T qt_p = in.t[2] - half * minmod_sel(dt1, dt2, s_tp);
-    const bool bstar_is_p = in.bm < in.bp;  // std::max(bm, bp) == (bm < bp) ? bp : bm
+    const T eta_m = in.e[1] + half * msel_(de0, de1, s_em);
+    const T eta_p = in.e[2] - half * msel_(de1, de2, s_ep);
+    const T qn_m = in.n[1] + half * msel_(dn0, dn1, s_nm);
+    const T qt_m = in.t[1] + half * msel_(dt0, dt1, s_tm);
+    const T qn_p = in.n[2] - half * msel_(dn1, dn2, s_np);
+    const T qt_p = in.t[2] - half * msel_(dt1, dt2, s_tp);
+    const bool bstar_is_p = lt_(in.bm, in.bp);  // std::max(bm, bp) == (bm < bp) ? bp : bm
     const T bs = bstar_is_p ? in.bp : in.bm;
     const T xm = eta_m - in.bm, xp = eta_p - in.bp;
-    const bool pm = xm > T(0), pp = xp > T(0);
+    const bool pm = pos_(xm), pp = pos_(xp);
     const T h_m = pm ? xm : T(0), h_p = pp ? xp : T(0);
-    const bool wm = h_m > eps, wp = h_p > eps;
-    const T rm = wm ? T(1) / h_m : T(0), rp = wp ? T(1) / h_p : T(0);
+    const bool wm = lt_(eps, h_m), wp = lt_(eps, h_p);
+    const T rm = wm ? rcp_(h_m) : T(0), rp = wp ? rcp_(h_p) : T(0);
     const T un_m = qn_m * rm, ut_m = qt_m * rm;
     const T un_p = qn_p * rp, ut_p = qt_p * rp;
     const T yL = eta_m - bs, yR = eta_p - bs;
-    const bool pL = yL > T(0), pR = yR > T(0);
+    const bool pL = pos_(yL), pR = pos_(yR);
     const T hL = pL ? yL : T(0), hR = pR ? yR : T(0);
     const T qnL = hL * un_m, qtL = hL * ut_m, qnR = hR * un_p, qtR = hR * ut_p;
-    const bool wL = hL > eps, wR = hR > eps;
+    const bool wL = lt_(eps, hL), wR = lt_(eps, hR);
     const T unL = wL ? un_m : T(0), utL = wL ? ut_m : T(0);
     const T unR = wR ? un_p : T(0), utR = wR ? ut_p : T(0);
     const T ghL = g * hL, ghR = g * hR;
-    const T rcL = ghL > T(0) ? trsqrt(ghL) : T(0), rcR = ghR > T(0) ? trsqrt(ghR) : T(0);
+    const T rcL = pos_(ghL) ? trsqrt(ghL) : T(0), rcR = pos_(ghR) ? trsqrt(ghR) : T(0);
     const T cL = ghL * rcL, cR = ghR * rcR;
     const T a1 = unL - cL, a2 = unR - cR, b1 = unL + cL, b2 = unR + cR;
-    const bool sL_is2 = a2 < a1, sR_is2 = b1 < b2;
+    const bool sL_is2 = lt_(a2, a1), sR_is2 = lt_(b1, b2);
     const T sL = sL_is2 ? a2 : a1, sR = sR_is2 ? b2 : b1;
     const T FL[3] = {qnL, qnL * unL + half * g * hL * hL, qnL * utL};
     const T FR[3] = {qnR, qnR * unR + half * g * hR * hR, qnR * utR};
     const T UL[3] = {hL, qnL, qtL}, UR[3] = {hR, qnR, qtR};
-    const int regime = (sL >= T(0)) ? 0 : ((sR <= T(0)) ? 1 : 2);
+    const int regime = !lt_(sL, T(0)) ? 0 : (!lt_(T(0), sR) ? 1 : 2);
 
     // ---- reverse sweep ----
     const T dF[3] = {d.fh, d.fqn_m + d.fqn_p, d.fqt};
@@ -165,18 +217,22 @@ SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceI
     } else if (regime == 1) {
         for (int c = 0; c < 3; ++c) dFR[c] = dF[c];
     } else {
-        const T inv = T(1) / (sR - sL);
+        // F = (sR FL - sL FR + sL sR dU) / (sR - sL) with dU = UR - UL, G = FR - FL:
+        // dF/dsR = sL (G - sL dU) / (sR - sL)^2, dF/dsL = sR (sR dU - G) / (sR - sL)^2
+        const T inv = rcp_(sR - sL);
         const T sLi = sL * inv, sRi = sR * inv, sLsRi = sL * sRi;
+        T gR = 0, gL = 0;
         for (int c = 0; c < 3; ++c) {
-            const T dU = UR[c] - UL[c];
-            const T F = sRi * FL[c] - sLi * FR[c] + sLsRi * dU;
+            const T dU = UR[c] - UL[c], G = FR[c] - FL[c];
             dFL[c] = dF[c] * sRi;
             dFR[c] = -dF[c] * sLi;
             dUR[c] = dF[c] * sLsRi;
             dUL[c] = -dUR[c];
-            dsR += dF[c] * ((FL[c] + sL * dU) - F) * inv;
-            dsL += dF[c] * ((-FR[c] + sR * dU) + F) * inv;
+            gR += dF[c] * (G - sL * dU);
+            gL += dF[c] * (sR * dU - G);
         }
+        dsR = gR * sLi * inv;
+        dsL = gL * sRi * inv;
     }
     T dunL = 0, dunR = 0, dcL = 0, dcR = 0;
     if (sL_is2) {
@@ -241,35 +297,18 @@ SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceI
     else
         dbm += dbs;
     // reconstructions: x_m = x1 + m(x1-x0, x2-x1)/2, x_p = x2 - m(x2-x1, x3-x2)/2
-    for (int k = 0; k < 4; ++k) a.e[k] = a.n[k] = a.t[k] = T(0);
-    auto recon_m = [&](T *ax, T dxm, int sel) {  // minus: first arg x1-x0, second x2-x1
-        ax[1] += dxm;
-        const T dm = half * dxm;
-        if (sel == 1) {
-            ax[1] += dm;
-            ax[0] -= dm;
-        } else if (sel == 2) {
-            ax[2] += dm;
-            ax[1] -= dm;
-        }
+    // reconstructions x_m = x1 + m(x1-x0, x2-x1)/2 and x_p = x2 - m(x2-x1, x3-x2)/2, with
+    // minmod selecting its first argument (sel 1), its second (sel 2) or zero (sel 0)
+    auto recon = [&](T *ax, T dxm, int sm, T dxp, int sp) {
+        const T hm = half_(dxm), hp = half_(dxp);
+        ax[0] = sm == 1 ? -hm : T(0);
+        ax[1] = (sm == 0 ? dxm : (sm == 1 ? dxm + hm : hm)) + (sp == 1 ? hp : T(0));
+        ax[2] = (sm == 2 ? hm : T(0)) + (sp == 0 ? dxp : (sp == 1 ? hp : dxp + hp));
+        ax[3] = sp == 2 ? -hp : T(0);
     };
-    auto recon_p = [&](T *ax, T dxp, int sel) {  // plus: first arg x2-x1, second x3-x2
-        ax[2] += dxp;
-        const T dm = -half * dxp;
-        if (sel == 1) {
-            ax[2] += dm;
-            ax[1] -= dm;
-        } else if (sel == 2) {
-            ax[3] += dm;
-            ax[2] -= dm;
-        }
-    };
-    recon_m(a.e, deta_m, s_em);
-    recon_p(a.e, deta_p, s_ep);
-    recon_m(a.n, dqn_m, s_nm);
-    recon_p(a.n, dqn_p, s_np);
-    recon_m(a.t, dqt_m, s_tm);
-    recon_p(a.t, dqt_p, s_tp);
+    recon(a.e, deta_m, s_em, deta_p, s_ep);
+    recon(a.n, dqn_m, s_nm, dqn_p, s_np);
+    recon(a.t, dqt_m, s_tm, dqt_p, s_tp);
     a.bm = dbm;
     a.bp = dbp;
 }

@@ -101,7 +101,7 @@ def test_checkpoint_budget_does_not_change_the_gradient(gpu_lib, sw, problems):
     Nx, Ny, steps, dt = 20, 16, 13, 1e-3
     h, hu, hv, B, gauges, obs, _ = setup(problems, Nx, Ny, 0, steps, seed=23)
     base = gpu_adjoint(sw, h, hu, hv, B, Nx, Ny, steps, dt, gauges, obs, 0, snapshots=steps)
-    for snaps in (0, 1, 2, 4):
+    for snaps in (0, 1, 2, 4, "tape"):
         r = gpu_adjoint(sw, h, hu, hv, B, Nx, Ny, steps, dt, gauges, obs, 0, snapshots=snaps)
         assert r["J"] == base["J"]
         for k in ("grad_h", "grad_hu", "grad_hv", "grad_B"):
