@@ -59,7 +59,12 @@ typedef struct swe_params {
     int bc;           /* swe_bc */
     int precision;    /* swe_precision */
     int device;       /* CUDA device ordinal */
-    int reserved[5];  /* must be zero */
+    int x_halo_lo;    /* nonzero: this grid is an x-slab whose 2 ghost rows below row 0
+                         hold the neighbour slab's rows (swe_halo), not the wall rule */
+    int x_halo_hi;    /* the same for the 2 ghost rows above row Nx - 1 */
+    int reserved;     /* must be zero */
+    double dx, dy;    /* > 0: cell sizes used instead of Lx / Nx and Ly / Ny, so that an
+                         x-slab keeps its grid's dx exactly; 0: derived */
 } swe_params;
 
 typedef struct swe_ctx swe_ctx; /* opaque */
@@ -97,6 +102,29 @@ int swe_download(swe_ctx *ctx, double *h, double *hu, double *hv);
  * Returns SWE_ERR_NONFINITE if any stage produced a non-finite interior value (the
  * state is then undefined), checked once per call. */
 int swe_step(swe_ctx *ctx, int n_steps, double dt, double *t_inout);
+
+/* ---- Slabs (x-decomposition over several GPUs) ---------------------------------------
+ * The reference's 4-GPU backend splits x into slabs (build_subdomains,
+ * cuda_solver_4gpu.hpp:281-304) and exchanges two ghost rows per neighbour after every
+ * stage.  A slab is a context created with x_halo_lo / x_halo_hi set on its interface
+ * sides (FP64 only): its stage kernels read those ghost rows as stored, swe_download
+ * leaves them as they are, and swe_upload keeps the uploaded ones.  A driver then runs
+ * each step as swe_stage(1..3) with one global dt (the max of every slab's
+ * swe_max_wave_speed), exchanging the just-written buffer's interface rows with swe_halo
+ * after every stage; the result is bitwise that of one grid.  No reference counterpart
+ * for the entry points themselves. */
+
+/* One RK stage with fixed dt > 0: stage 1: U1 = Un + dt L(Un); 2: U2 = 3/4 Un +
+ * 1/4 (U1 + dt L(U1)); 3: Un = 1/3 Un + 2/3 (U2 + dt L(U2)), after which
+ * swe_max_wave_speed reports the new state (HPC_solver.hpp:244-301).  Buffers: stage s
+ * writes buffer s % 3 (0: U^n, 1: U^(1), 2: U^(2)).  SWE_ERR_NONFINITE as swe_step. */
+int swe_stage(swe_ctx *ctx, int stage, double dt);
+
+/* Interface rows of buffer (0: U^n, 1: U^(1), 2: U^(2)) on side (0: low x, 1: high x).
+ * op 0 copies the 2 interior rows next to that side (rows 0, 1 or Nx - 2, Nx - 1) to
+ * rows; op 1 copies rows into that side's 2 ghost rows.  rows holds h, hu, hv, each
+ * 2 x (Ny + 4) doubles in row order, in host or device memory; synchronous. */
+int swe_halo(swe_ctx *ctx, int buffer, int side, int op, double *rows);
 
 /* Max over interior cells of max(|u| + c, |v| + c), c = sqrt(g max(0, h)), of the
  * current state (the reduction inside compute_stable_dt). */

@@ -29,6 +29,8 @@ class _Grid(ctypes.Structure):
         ("cfl", ctypes.c_double),
         ("bc", ctypes.c_int),
         ("threads", ctypes.c_int),
+        ("dx", ctypes.c_double),
+        ("dy", ctypes.c_double),
     ]
 
 
@@ -79,8 +81,9 @@ def _p(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
-def grid(Nx, Ny, Lx=1.0, Ly=1.0, g=G_REFERENCE, cfl=0.45, bc=BC_REFLECTING, threads=0):
-    return _Grid(Nx, Ny, Lx, Ly, g, cfl, bc, threads)
+def grid(Nx, Ny, Lx=1.0, Ly=1.0, g=G_REFERENCE, cfl=0.45, bc=BC_REFLECTING, threads=0,
+         dx=0.0, dy=0.0):
+    return _Grid(Nx, Ny, Lx, Ly, g, cfl, bc, threads, dx, dy)
 
 
 def run(p: _Grid, h, hu, hv, B, steps, dt_fixed=0.0):

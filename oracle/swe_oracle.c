@@ -30,8 +30,8 @@ static view_t make_view(const swe_oracle_grid *p) {
     v.Nx_total = p->Nx + 4;
     v.Ny_total = p->Ny + 4;
     v.stride = v.Ny_total;
-    v.dx = p->Lx / p->Nx; /* include/core/grid.hpp:19-20 */
-    v.dy = p->Ly / p->Ny;
+    v.dx = p->dx > 0.0 ? p->dx : p->Lx / p->Nx; /* include/core/grid.hpp:19-20 */
+    v.dy = p->dy > 0.0 ? p->dy : p->Ly / p->Ny;
     v.g = p->g;
     return v;
 }

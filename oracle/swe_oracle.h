@@ -29,6 +29,7 @@ typedef struct swe_oracle_grid {
     double cfl;   /* CFL number for compute_stable_dt */
     int bc;       /* SWE_ORACLE_BC_* */
     int threads;  /* OpenMP threads; <= 0 uses the OpenMP default */
+    double dx, dy;/* > 0: cell sizes used instead of Lx / Nx, Ly / Ny (a slab of a grid) */
 } swe_oracle_grid;
 
 /* Runs `steps` SSP-RK3 steps in place on h, hu, hv (ghosts refreshed on return).

@@ -11,5 +11,6 @@ from ._lib import lib  # noqa: F401
 from .solver import Solver, SweError  # noqa: F401
 from .ensemble import Ensemble  # noqa: F401
 from . import adjoint  # noqa: F401
+from . import slabs  # noqa: F401
 
-__all__ = ["Solver", "SweError", "Ensemble", "adjoint", "problems", "lib"]
+__all__ = ["Solver", "SweError", "Ensemble", "adjoint", "slabs", "problems", "lib"]

@@ -33,7 +33,8 @@ EXPORTS = (
     "swe_ens_create", "swe_ens_destroy", "swe_ens_upload", "swe_ens_download", "swe_ens_step",
     "swe_ens_times", "swe_ens_last_dt", "swe_ens_last_step_ms", "swe_ens_kernel_launches",
     "swe_ens_set_schedule", "swe_ens_get_schedule", "swe_ens_tune", "swe_ens_last_error",
-    "swe_totals_noalloc", "swe_adjoint_gauge", "swe_selftest_soft_f64",
+    "swe_totals_noalloc", "swe_adjoint_gauge", "swe_selftest_soft_f64", "swe_stage",
+    "swe_halo",
 )
 TOTALS_NOALLOC_MAX_BLOCKS = 1024
 ADJ_TAPE_ALL = -1  # n_snapshots value of swe_adjoint_gauge's tape mode
@@ -53,7 +54,11 @@ class SweParams(ctypes.Structure):
         ("bc", ctypes.c_int),
         ("precision", ctypes.c_int),
         ("device", ctypes.c_int),
-        ("reserved", ctypes.c_int * 5),
+        ("x_halo_lo", ctypes.c_int),
+        ("x_halo_hi", ctypes.c_int),
+        ("reserved", ctypes.c_int),
+        ("dx", ctypes.c_double),
+        ("dy", ctypes.c_double),
     ]
 
 
@@ -132,6 +137,10 @@ def lib(path: str = LIB_PATH):
     L.swe_adjoint_gauge.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ip, ip, dp,
                                     ctypes.c_int, dp, dp, dp, dp, dp, dp]
     L.swe_adjoint_gauge.restype = ctypes.c_int
+    L.swe_stage.argtypes = [vp, ctypes.c_int, ctypes.c_double]
+    L.swe_stage.restype = ctypes.c_int
+    L.swe_halo.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]
+    L.swe_halo.restype = ctypes.c_int
     L.swe_selftest_soft_f64.argtypes = [ctypes.c_longlong, ctypes.c_ulonglong,
                                         ctypes.POINTER(ctypes.c_longlong)]
     L.swe_selftest_soft_f64.restype = ctypes.c_int

@@ -92,6 +92,35 @@ namespace {
 
 bool fp32(const swe_ctx *c) { return c->p.precision == SWE_PRECISION_FP32_MIXED; }
 
+// Launch parameters shared by every stage of a context (buffers set per stage).
+StageParams stage_params(swe_ctx *c, double dt) {
+    StageParams sp{};
+    sp.B = c->B;
+    sp.Nx = c->p.Nx;
+    sp.Ny = c->p.Ny;
+    sp.pitch = c->pitch;
+    sp.bc = c->p.bc;
+    sp.inv_dx = c->inv_dx;
+    sp.inv_dy = c->inv_dy;
+    sp.kx = pow2_exponent(c->inv_dx);
+    sp.ky = pow2_exponent(c->inv_dy);
+    sp.g = c->p.g;
+    sp.half_g = 0.5 * c->p.g;
+    sp.gf = (float)sp.g;
+    sp.half_gf = (float)sp.half_g;
+    sp.inv_dxf = (float)sp.inv_dx;
+    sp.inv_dyf = (float)sp.inv_dy;
+    sp.cfl_min_dxdy = c->cfl_min_dxdy;
+    sp.dt_fixed = dt > 0.0 ? dt : 0.0;
+    sp.speed = c->speed;
+    sp.t_accum = c->t_accum;
+    sp.dt_log = c->dt_log;
+    sp.flags = c->flags;
+    sp.halo_lo = c->p.x_halo_lo;
+    sp.halo_hi = c->p.x_halo_hi;
+    return sp;
+}
+
 // Max wave speed of U^n into the slot the next step reads.
 int refresh_speed(swe_ctx *c) {
     unsigned long long *slot = c->speed + (c->steps_done & 1);
@@ -175,12 +204,15 @@ int swe_create(const swe_params *pin, swe_ctx **out) {
     if (p.nG != 2 || p.Nx < 2 || p.Ny < 2 || !(p.Lx > 0.0) || !(p.Ly > 0.0) ||
         !(p.cfl > 0.0) || (p.bc != SWE_BC_REFLECTING && p.bc != SWE_BC_TRANSMISSIVE))
         return SWE_ERR_BAD_ARG;
-    for (int r : p.reserved)
-        if (r != 0) return SWE_ERR_BAD_ARG;
+    if (p.reserved != 0 || !(p.dx >= 0.0) || !(p.dy >= 0.0)) return SWE_ERR_BAD_ARG;
+    p.x_halo_lo = p.x_halo_lo != 0;
+    p.x_halo_hi = p.x_halo_hi != 0;
     // Device indices are int: keep (Nx + 4) * pitch below 2^31 per field.
     if ((long long)(p.Nx + 4) * (long long)(p.Ny + 36) >= (1ll << 31)) return SWE_ERR_BAD_ARG;
     if (p.precision != SWE_PRECISION_FP64 && p.precision != SWE_PRECISION_FP32_MIXED)
         return SWE_ERR_UNSUPPORTED;
+    if ((p.x_halo_lo || p.x_halo_hi) && p.precision != SWE_PRECISION_FP64)
+        return SWE_ERR_UNSUPPORTED;  // slabs are an FP64 drop-in feature
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= p.device || p.device < 0) {
         cudaGetLastError();
@@ -195,8 +227,8 @@ int swe_create(const swe_params *pin, swe_ctx **out) {
         return st;
     }
     // HPC_solver.hpp:91-93 and include/core/grid.hpp:19-20; 1.0 / dx as apply_divergence.
-    c->dx = p.Lx / p.Nx;
-    c->dy = p.Ly / p.Ny;
+    c->dx = p.dx > 0.0 ? p.dx : p.Lx / p.Nx;
+    c->dy = p.dy > 0.0 ? p.dy : p.Ly / p.Ny;
     c->inv_dx = 1.0 / c->dx;
     c->inv_dy = 1.0 / c->dy;
     c->cfl_min_dxdy = p.cfl * std::min(c->dx, c->dy);
@@ -328,7 +360,7 @@ int swe_download(swe_ctx *c, double *h, double *hu, double *hv) {
         }
     } else {
         CK(launch_fill_ghosts_f64(c->Un[0], c->Un[1], c->Un[2], c->p.Nx, c->p.Ny, c->pitch,
-                                  c->p.bc, c->stream));
+                                  c->p.bc, c->stream, c->p.x_halo_lo, c->p.x_halo_hi));
         ++c->launches;
         for (int f = 0; f < 3; ++f)
             CK(cudaMemcpy2DAsync(dst[f], row, c->Un[f], spitch, row, (size_t)(c->p.Nx + 4),
@@ -358,28 +390,7 @@ int swe_step(swe_ctx *c, int n_steps, double dt, double *t_inout) {
     CK(cudaMemcpyAsync(c->t_accum, &t0, sizeof(double), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemsetAsync(c->flags, 0, sizeof(int), c->stream));
 
-    StageParams sp{};
-    sp.B = c->B;
-    sp.Nx = c->p.Nx;
-    sp.Ny = c->p.Ny;
-    sp.pitch = c->pitch;
-    sp.bc = c->p.bc;
-    sp.inv_dx = c->inv_dx;
-    sp.inv_dy = c->inv_dy;
-    sp.kx = pow2_exponent(c->inv_dx);
-    sp.ky = pow2_exponent(c->inv_dy);
-    sp.g = c->p.g;
-    sp.half_g = 0.5 * c->p.g;
-    sp.gf = (float)sp.g;
-    sp.half_gf = (float)sp.half_g;
-    sp.inv_dxf = (float)sp.inv_dx;
-    sp.inv_dyf = (float)sp.inv_dy;
-    sp.cfl_min_dxdy = c->cfl_min_dxdy;
-    sp.dt_fixed = dt > 0.0 ? dt : 0.0;
-    sp.speed = c->speed;
-    sp.t_accum = c->t_accum;
-    sp.dt_log = c->dt_log;
-    sp.flags = c->flags;
+    StageParams sp = stage_params(c, dt);
     CK(cudaEventRecord(c->ev0, c->stream));
     for (int s = 0; s < n_steps; ++s) {
         sp.slot_read = (int)(c->steps_done & 1);
@@ -414,6 +425,57 @@ int swe_step(swe_ctx *c, int n_steps, double dt, double *t_inout) {
     if (t_inout) *t_inout = t1;
     if (flags & FLAG_NONFINITE)
         return fail(c, SWE_ERR_NONFINITE, "non-finite state detected in GB300 solver");
+    return SWE_OK;
+}
+
+int swe_stage(swe_ctx *c, int stage, double dt) {
+    if (!c || stage < 1 || stage > 3 || !(dt > 0.0))
+        return fail(c, SWE_ERR_BAD_ARG, "swe_stage: stage must be 1..3 and dt > 0");
+    if (!c->uploaded) return fail(c, SWE_ERR_BAD_ARG, "swe_stage: no state uploaded");
+    int st = set_device(c);
+    if (st) return st;
+    StageParams sp = stage_params(c, dt);
+    sp.slot_read = (int)(c->steps_done & 1);
+    sp.slot_write = sp.slot_read ^ 1;
+    sp.t_accum = nullptr;
+    sp.dt_log = nullptr;
+    sp.hn = c->Un[0]; sp.hun = c->Un[1]; sp.hvn = c->Un[2];
+    void *const *src = stage == 1 ? c->Un : (stage == 2 ? c->U1 : c->U2);
+    void *const *dst = stage == 1 ? c->U1 : (stage == 2 ? c->U2 : c->Un);
+    sp.hs = src[0]; sp.hus = src[1]; sp.hvs = src[2];
+    sp.ho = dst[0]; sp.huo = dst[1]; sp.hvo = dst[2];
+    CK(cudaMemsetAsync(c->flags, 0, sizeof(int), c->stream));
+    CK(launch_stage(c, stage, sp));
+    ++c->launches;
+    if (stage == 3) ++c->steps_done;  // the stage wrote the new state's max speed
+    int flags = 0;
+    CK(cudaMemcpyAsync(&flags, c->flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (flags & FLAG_NONFINITE)
+        return fail(c, SWE_ERR_NONFINITE, "non-finite state detected in GB300 solver");
+    return SWE_OK;
+}
+
+int swe_halo(swe_ctx *c, int buffer, int side, int op, double *rows) {
+    if (!c || !rows || buffer < 0 || buffer > 2 || side < 0 || side > 1 || op < 0 || op > 1)
+        return fail(c, SWE_ERR_BAD_ARG, "swe_halo: bad argument");
+    if (fp32(c)) return fail(c, SWE_ERR_UNSUPPORTED, "swe_halo: slabs are FP64 only");
+    int st = set_device(c);
+    if (st) return st;
+    void *const *buf = buffer == 0 ? c->Un : (buffer == 1 ? c->U1 : c->U2);
+    // ghosted row index of the first of the two rows
+    const int r0 = op == 0 ? (side == 0 ? NG : c->p.Nx) : (side == 0 ? 0 : c->p.Nx + NG);
+    const size_t row = (size_t)(c->p.Ny + 4) * sizeof(double);
+    const size_t dp = (size_t)c->pitch * sizeof(double);
+    for (int f = 0; f < 3; ++f) {
+        double *dev = static_cast<double *>(buf[f]) + (size_t)r0 * c->pitch;
+        double *hst = rows + (size_t)f * 2 * (c->p.Ny + 4);
+        if (op == 0)
+            CK(cudaMemcpy2DAsync(hst, row, dev, dp, row, 2, cudaMemcpyDefault, c->stream));
+        else
+            CK(cudaMemcpy2DAsync(dev, dp, hst, row, row, 2, cudaMemcpyDefault, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
     return SWE_OK;
 }
 

@@ -42,6 +42,7 @@ struct StageParams {
     int log_index;               // index into dt_log for this step
     int *flags;                  // FLAG_* bits
     unsigned char *mask;         // optional: 1 where positivity clamped the cell (adjoint)
+    int halo_lo, halo_hi;        // x sides whose ghost rows a neighbour slab supplies
 };
 
 // Ensemble of independent grids (one per instance) in shared field pools.
@@ -144,6 +145,17 @@ __device__ __forceinline__ int map_coord(int a, int N, int bc, bool &flip) {
         }
     }
     return a < 0 ? 0 : (a >= N ? N - 1 : a);
+}
+
+// Row coordinate of a stencil cell: ghost rows on a slab-interface side are read where
+// they lie (they hold the neighbour's rows); other ghosts follow the wall rule.
+__device__ __forceinline__ int map_row(int a, int N, int bc, bool halo_lo, bool halo_hi,
+                                       bool &flip) {
+    if ((a < 0 && halo_lo) || (a >= N && halo_hi)) {
+        flip = false;
+        return a;
+    }
+    return map_coord(a, N, bc, flip);
 }
 
 __device__ __forceinline__ int clamp_int(int a, int lo, int hi) {

@@ -242,7 +242,7 @@ __device__ __forceinline__ double stage_tile_f64(const StageParams &p, int i0, i
         const int r = t / RJ, c = t - (t / RJ) * RJ;
         const int ii = i0 - NG + r, jj = j0 - NG + c;
         bool fx, fy;
-        const int mi = map_coord(ii, p.Nx, p.bc, fx);
+        const int mi = map_row(ii, p.Nx, p.bc, p.halo_lo, p.halo_hi, fx);
         const int mj = map_coord(jj, p.Ny, p.bc, fy);
         const long long k = (long long)(mi + NG) * P + (mj + NG);
         const double hv_ = hvs[k], hu_ = hus[k], h_ = hs[k];
@@ -413,7 +413,7 @@ __global__ void __launch_bounds__(256) k_max_speed_f64(const double *h, const do
 // columns over all rows take the mirrored column (hv negated), so a corner holds the
 // doubly mirrored interior cell.  Transmissive walls copy the nearest interior cell.
 __global__ void k_fill_ghosts_f64(double *h, double *hu, double *hv, int Nx, int Ny,
-                                  long long P, int bc) {
+                                  long long P, int bc, int halo_lo, int halo_hi) {
     const int NyT = Ny + 2 * NG;
     const int n_rows = 4 * NyT;  // rows 0, 1, Nx+2, Nx+3, every column
     const int n_cols = 4 * Nx;   // columns 0, 1, Ny+2, Ny+3 of interior rows
@@ -422,6 +422,7 @@ __global__ void k_fill_ghosts_f64(double *h, double *hu, double *hv, int Nx, int
     int i, j;
     if (t < n_rows) {
         const int r = t / NyT;
+        if (r < 2 ? halo_lo : halo_hi) return;  // the neighbour slab's rows
         j = t - r * NyT;
         i = r < 2 ? r : Nx + r;  // 0, 1, Nx+2, Nx+3
     } else {
@@ -488,12 +489,12 @@ cudaError_t launch_max_speed_f64(const void *h, const void *hu, const void *hv, 
 }
 
 cudaError_t launch_fill_ghosts_f64(void *h, void *hu, void *hv, int Nx, int Ny, long long pitch,
-                                   int bc, cudaStream_t s) {
+                                   int bc, cudaStream_t s, int halo_lo, int halo_hi) {
     const int n = 4 * (Ny + 2 * NG) + 4 * Nx;
     k_fill_ghosts_f64<<<(n + 255) / 256, 256, 0, s>>>(static_cast<double *>(h),
                                                        static_cast<double *>(hu),
                                                        static_cast<double *>(hv), Nx, Ny, pitch,
-                                                       bc);
+                                                       bc, halo_lo, halo_hi);
     return cudaGetLastError();
 }
 

@@ -16,8 +16,9 @@ cudaError_t launch_ens_stage_f64(int shape, int stage, const EnsParams &e, int g
 cudaError_t launch_max_speed_f64(const void *h, const void *hu, const void *hv, int Nx, int Ny,
                                  long long pitch, double g, unsigned long long *slot,
                                  int num_sms, cudaStream_t s);
+// Ghost refresh by the wall rule; x-ghost rows on slab-interface sides are left as stored.
 cudaError_t launch_fill_ghosts_f64(void *h, void *hu, void *hv, int Nx, int Ny, long long pitch,
-                                   int bc, cudaStream_t s);
+                                   int bc, cudaStream_t s, int halo_lo = 0, int halo_hi = 0);
 
 // FP32-mixed form (swe_fp32.cu): state (eta = h + B, hu, hv) and B in FP32.
 // Single-grid FP32 tile shape (rows x columns); the TMA box is (TI + 4) x (TJ + 4).

@@ -45,7 +45,10 @@ class Solver:
 
     def __init__(self, Nx: int, Ny: int, Lx: float = 1.0, Ly: float = 1.0,
                  g: float = 9.80665, cfl: float = 0.45, bc="reflecting",
-                 precision="fp64", device: int = 0):
+                 precision="fp64", device: int = 0, x_halo=(False, False),
+                 dx: float = 0.0, dy: float = 0.0):
+        """``x_halo`` marks the low / high x sides whose ghost rows a neighbour slab
+        supplies, ``dx``/``dy`` > 0 fix the cell sizes (see ``slabs.SlabGrid``)."""
         self._lib = L.lib()
         p = L.SweParams()
         self._lib.swe_params_default(ctypes.byref(p))
@@ -53,6 +56,8 @@ class Solver:
         p.bc = _BC[bc] if isinstance(bc, str) else int(bc)
         p.precision = _PREC[precision] if isinstance(precision, str) else int(precision)
         p.device = device
+        p.x_halo_lo, p.x_halo_hi = int(bool(x_halo[0])), int(bool(x_halo[1]))
+        p.dx, p.dy = float(dx), float(dy)
         self.params = p
         self.Nx, self.Ny = Nx, Ny
         self._ctx = ctypes.c_void_p()
@@ -106,6 +111,23 @@ class Solver:
         self.time = t.value
         self._check(st, "swe_step")
         return self.time
+
+    def stage(self, stage: int, dt: float):
+        """One RK stage with fixed dt (swe_stage); stage s writes buffer s % 3."""
+        self._check(self._lib.swe_stage(self._ctx, int(stage), float(dt)), "swe_stage")
+
+    def halo_pack(self, buffer: int, side: int) -> np.ndarray:
+        """The 2 interior rows next to x side ``side`` of ``buffer``: (3, 2, Ny + 4)."""
+        rows = np.empty((3, 2, self.Ny + 4), dtype=np.float64)
+        self._check(self._lib.swe_halo(self._ctx, int(buffer), int(side), 0, _dp(rows)),
+                    "swe_halo")
+        return rows
+
+    def halo_unpack(self, buffer: int, side: int, rows: np.ndarray):
+        """Writes (3, 2, Ny + 4) rows into the ghost rows of x side ``side``."""
+        rows = np.ascontiguousarray(rows, dtype=np.float64).reshape(3, 2, self.Ny + 4)
+        self._check(self._lib.swe_halo(self._ctx, int(buffer), int(side), 1, _dp(rows)),
+                    "swe_halo")
 
     def max_wave_speed(self) -> float:
         v = ctypes.c_double()

@@ -1,0 +1,90 @@
+"""x-slab decomposition (shallow-water_gb300/slabs.py; the reference's multi-GPU split,
+cuda_solver_4gpu.hpp:281-304): the slabs stepped with per-stage halo exchange and one
+global CFL dt give bitwise the whole grid's result.  CPU: slabs computed by the oracle,
+in one process and as gloo ranks (world size 2 and 3).  GPU: slabs as library contexts
+with x_halo sides on one device, against one context over the whole grid."""
+from __future__ import annotations
+
+import os
+import socket
+
+import numpy as np
+import pytest
+
+import slab_oracle as so
+
+
+def free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def whole_grid(port, Nx, Ny, bc, steps, seed=5):
+    h, hu, hv, B = so.case(Nx, Ny, bc, seed)
+    p = port.grid(Nx, Ny, bc=so.BC[bc], threads=1)
+    oh, ohu, ohv, dts, t, st = port.run(p, h, hu, hv, B, steps)
+    assert st == 0
+    return (oh, ohu, ohv), t
+
+
+def test_partition(sw):
+    S = sw.slabs
+    assert S.partition(10, 3) == [(0, 3), (3, 6), (6, 10)]
+    assert S.partition(64, 1) == [(0, 64)]
+    with pytest.raises(ValueError):
+        S.partition(5, 3)
+
+
+@pytest.mark.parametrize("bc", ["reflecting", "transmissive"])
+@pytest.mark.parametrize("parts", [2, 3, 4])
+def test_slabs_in_process_bitwise(sw, port, bc, parts):
+    Nx, Ny, steps = 23, 17, 12
+    want, t_want = whole_grid(port, Nx, Ny, bc, steps)
+    h, hu, hv, B = so.case(Nx, Ny, bc, 5)
+    grid = sw.slabs.SlabGrid(Nx, Ny, bc=bc, parts=parts,
+                             make_local=so.make_oracle_local(Ny, port.G_REFERENCE, 0.45, bc))
+    grid.upload(h, hu, hv, B)
+    t = grid.step(steps)
+    got = grid.download()
+    assert t == t_want
+    for a, b in zip(got, want):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("world,bc", [(2, "reflecting"), (3, "transmissive")])
+def test_slabs_gloo_ranks_bitwise(port, tmp_path, world, bc):
+    import torch.multiprocessing as mp
+    Nx, Ny, steps = 20, 12, 8
+    mp.spawn(so.gloo_worker, args=(world, free_port(), Nx, Ny, bc, steps, str(tmp_path)),
+             nprocs=world, join=True)
+    r = np.load(os.path.join(tmp_path, "slabs.npz"))
+    want, t_want = whole_grid(port, Nx, Ny, bc, steps)
+    assert float(r["t"]) == t_want
+    for k, b in zip(("h", "hu", "hv"), want):
+        assert np.array_equal(r[k], b)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bc", ["reflecting", "transmissive"])
+@pytest.mark.parametrize("parts", [2, 3])
+def test_slabs_gpu_bitwise(gpu_lib, sw, port, bc, parts):
+    Nx, Ny, steps = 70, 45, 15
+    h, hu, hv, B = so.case(Nx, Ny, bc, 5)
+    with sw.Solver(Nx, Ny, bc=bc) as s:
+        s.upload(h, hu, hv, B)
+        t_want = s.step(steps)
+        want = s.download()
+    grid = sw.slabs.SlabGrid(Nx, Ny, bc=bc, parts=parts)
+    try:
+        grid.upload(h, hu, hv, B)
+        t = grid.step(steps)
+        got = grid.download()
+    finally:
+        grid.close()
+    assert t == t_want
+    for a, b in zip(got, want):
+        assert np.array_equal(a, b)
+    oracle, t_o = whole_grid(port, Nx, Ny, bc, steps)
+    for a, b in zip(got, oracle):
+        assert np.array_equal(a, b)
