@@ -34,9 +34,13 @@ sys.path.insert(0, ROOT)
 
 METRIC = "GCUPS & % HBM roofline: FP32-mixed vs FP64 at stated L1 error; adjoint/forward"
 BYTES_PER_CELL_FP64 = 216  # algorithmic bytes per cell-update: 56 + 80 + 80 (stages 1-3)
-# dram bytes per stage launch per interior cell from the committed ncu capture
-# (profiles/stage_f64_ncu.md); None until measured.
-NCU_TRAFFIC_BYTES_PER_CELL_LAUNCH = None
+# DRAM bytes per stage launch per interior cell, mean of the three stages, from one
+# ncu capture of this bench at 8192^2 (dram__bytes_read.sum + dram__bytes_write.sum).
+NCU_TRAFFIC_BYTES_PER_CELL_LAUNCH = 71.7
+# FP64-pipe lane operations (DADD + DMUL + DFMA) per cell update, three stages, from the
+# ncu thread-level instruction counts of the stage kernel; the pipe executes 2 per clock
+# per SM, so its peak is 2 x SMs x clock.
+FP64_OPS_PER_CELL_UPDATE = 559.8
 
 
 def parse():
@@ -52,8 +56,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the FP32-mixed, ensemble and adjoint measurements")
+    ap.add_argument("--forms", default="fp32_mixed,ensemble,adjoint",
+                    help="comma list of the extra forms to measure")
     ap.add_argument("--fp32-n", type=int, default=16384)
-    ap.add_argument("--ens-count", type=int, default=64)
+    ap.add_argument("--ens-count", type=int, default=512)
     ap.add_argument("--adj-n", type=int, default=1024)
     ap.add_argument("--adj-steps", type=int, default=200)
     ap.add_argument("--acc-n", type=int, default=2048)
@@ -163,6 +169,23 @@ def peaks():
         return float(m["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         return 6800.0, "fallback"
+
+
+def fp64_pipe(gcups: float, dev: int):
+    """The bound that limits the FP64 stage kernel on GB300: FP64-pipe operations per
+    second against 2 per clock per SM at the maximum SM clock."""
+    import torch
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            mhz = float(json.load(f)["sm_max_mhz"])
+    except (OSError, KeyError, ValueError):
+        mhz = 2070.0
+    peak = 2.0 * sms * mhz * 1e6 / 1e9
+    achieved = gcups * FP64_OPS_PER_CELL_UPDATE
+    return {"achieved": achieved, "peak": peak, "unit": "G FP64 lane-ops/s",
+            "frac": achieved / peak, "ops_per_cell_update": FP64_OPS_PER_CELL_UPDATE,
+            "peak_source": f"2 x {sms} SMs x {mhz:.0f} MHz"}
 
 
 def cpu_threads() -> int:
@@ -307,9 +330,12 @@ def form_adjoint(args, sw):
 
 def run_forms(args, sw, fp64_gcups):
     forms = {}
+    wanted = set(args.forms.split(","))
     for name, fn in (("fp32_mixed", lambda: form_fp32(args, sw, fp64_gcups)),
                      ("ensemble", lambda: form_ensemble(args, sw)),
                      ("adjoint", lambda: form_adjoint(args, sw))):
+        if name not in wanted:
+            continue
         try:
             forms[name] = fn()
         except Exception as exc:  # keep the headline line whatever an extra does
@@ -410,6 +436,7 @@ def run_gb300(args, dist: Dist):
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "kernel": "k_stage_f64 (3 launches per step)",
                      "algorithmic_bytes_per_launch": algo_bytes_launch},
+        "fp64_pipe_roofline": fp64_pipe(value, dev),
         "e2e": e2e,
         "gpu_launches": launches,
         "wall_ms_per_step": wall * 1e3 / K,
