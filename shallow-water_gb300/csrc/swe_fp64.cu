@@ -43,6 +43,17 @@ __device__ __forceinline__ double safe_velocity(double q, double h) {
     return x64::gt_pos_const(h, EPS_BITS) ? sf::div_rn(q, h) : 0.0;
 }
 
+// safe_velocity of two momenta over the same depth (one shared reciprocal).
+__device__ __forceinline__ void safe_velocity2(double q1, double q2, double h, double &u1,
+                                               double &u2) {
+    if (x64::gt_pos_const(h, EPS_BITS)) {
+        sf::div2_rn(q1, q2, h, u1, u2);
+    } else {
+        u1 = 0.0;
+        u2 = 0.0;
+    }
+}
+
 // Work split between the FP64 pipe and the integer pipes.  Each group of operations
 // below runs either as FP64 instructions or as the correctly rounded integer routines
 // of swe_soft_f64.cuh (identical results); moving part of the adds and multiplies off
@@ -153,34 +164,39 @@ __device__ __forceinline__ Face face_flux(double g, double half_g, double eta_m1
     const double qt_minus = fadd<1>(qt_0, x64::halve(x64::minmod(d_qt0, d_qt1)));
     const double qn_plus = fsub<1>(qn_p1, x64::halve(x64::minmod(d_qn1, d_qn2)));
     const double qt_plus = fsub<1>(qt_p1, x64::halve(x64::minmod(d_qt1, d_qt2)));
-    const double b_star = dmax(b_minus, b_plus);
+    // b_star = std::max(b_minus, b_plus) is bitwise one of them: on that side
+    // hs = positive(eta - b_star) is h itself and corr = half_g * (h*h - h*h) is +0, so
+    // only the other side's hs and correction are computed (the same operations as the
+    // reference's on that side); f_n + (+0) is f_n with -0 turned into +0.
+    const bool m_star = !x64::lt(b_minus, b_plus);
+    const double b_star = m_star ? b_minus : b_plus;
     const double h_minus = x64::positive_part(fsub<1>(eta_minus, b_minus));
     const double h_plus = x64::positive_part(fsub<1>(eta_plus, b_plus));
-    const double un_minus = safe_velocity(qn_minus, h_minus);
-    const double ut_minus = safe_velocity(qt_minus, h_minus);
-    const double un_plus = safe_velocity(qn_plus, h_plus);
-    const double ut_plus = safe_velocity(qt_plus, h_plus);
-    const double hs_minus = x64::positive_part(fsub<1>(eta_minus, b_star));
-    const double hs_plus = x64::positive_part(fsub<1>(eta_plus, b_star));
+    double un_minus, ut_minus, un_plus, ut_plus;
+    safe_velocity2(qn_minus, qt_minus, h_minus, un_minus, ut_minus);
+    safe_velocity2(qn_plus, qt_plus, h_plus, un_plus, ut_plus);
+    const double h_o = m_star ? h_plus : h_minus;  // the side b_star is not taken from
+    const double hs_o = x64::positive_part(fsub<1>(m_star ? eta_plus : eta_minus, b_star));
+    const double hs_minus = m_star ? h_minus : hs_o;
+    const double hs_plus = m_star ? hs_o : h_plus;
     double f_h, f_n, f_t;
     hll_normal(g, half_g, hs_minus, un_minus, ut_minus, hs_plus, un_plus, ut_plus, f_h, f_n,
                f_t);
-    const double corr_minus =
-        fmul<3>(half_g, fsub<4>(fmul<3>(h_minus, h_minus), fmul<3>(hs_minus, hs_minus)));
-    const double corr_plus =
-        fmul<3>(half_g, fsub<4>(fmul<3>(h_plus, h_plus), fmul<3>(hs_plus, hs_plus)));
+    const double corr_o = fmul<3>(half_g, fsub<4>(fmul<3>(h_o, h_o), fmul<3>(hs_o, hs_o)));
+    const double fqn_o = fadd<4>(f_n, corr_o);
+    const double fqn_s = x64::bits(f_n) == x64::SIGN ? 0.0 : f_n;
     Face f;
     f.fh = f_h;
     f.fqt = f_t;
-    f.fqn_m = fadd<4>(f_n, corr_minus);
-    f.fqn_p = fadd<4>(f_n, corr_plus);
+    f.fqn_m = m_star ? fqn_s : fqn_o;
+    f.fqn_p = m_star ? fqn_o : fqn_s;
     return f;
 }
 
 // Per-cell wave speed max(|u| + c, |v| + c) (compute_stable_dt body, :288-293).
 __device__ __forceinline__ double cell_speed(double g, double h, double hu, double hv) {
-    const double u = safe_velocity(hu, h);
-    const double v = safe_velocity(hv, h);
+    double u, v;
+    safe_velocity2(hu, hv, h, u, v);
     const double c = sf::sqrt_rn(g * x64::positive_part(h));  // std::max(0.0, h)
     return dmax(x64::fabs_(u) + c, x64::fabs_(v) + c);
 }
@@ -351,9 +367,25 @@ __device__ __forceinline__ double stage_tile_f64(const StageParams &p, int i0, i
     return speed;
 }
 
+// Resident threads per SM the register budget is sized for: 1152 (36 warps, four
+// 8x32 tiles) keeps the FP64 pipe fed while other CTAs load or synchronise.
+#ifndef SWE_F64_THREADS_PER_SM
+#define SWE_F64_THREADS_PER_SM 1152
+#endif
+#ifndef SWE_ENS_F64_THREADS_PER_SM
+#define SWE_ENS_F64_THREADS_PER_SM 1152
+#endif
+constexpr int min_blocks(int TI, int TJ) {
+    return SWE_F64_THREADS_PER_SM / ((TI + 1) * TJ) > 0 ? SWE_F64_THREADS_PER_SM / ((TI + 1) * TJ) : 1;
+}
+constexpr int ens_min_blocks(int TI, int TJ) {
+    return SWE_ENS_F64_THREADS_PER_SM / ((TI + 1) * TJ) > 0
+               ? SWE_ENS_F64_THREADS_PER_SM / ((TI + 1) * TJ) : 1;
+}
+
 // Single grid: one CTA per tile.
 template <int TI, int TJ, int STAGE>
-__global__ void __launch_bounds__((TI + 1) * TJ) k_stage_f64(const StageParams p) {
+__global__ void __launch_bounds__((TI + 1) * TJ, min_blocks(TI, TJ)) k_stage_f64(const StageParams p) {
     const double dt = stage_dt(p);
     const double speed = stage_tile_f64<TI, TJ, STAGE>(p, blockIdx.y * TI, blockIdx.x * TJ, dt);
     if (STAGE == 1 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
@@ -371,7 +403,7 @@ __global__ void __launch_bounds__((TI + 1) * TJ) k_stage_f64(const StageParams p
 // costs the same, so static striding balances.  Each instance has its own dt, max-speed
 // slots and time (per-instance CFL).
 template <int TI, int TJ, int STAGE>
-__global__ void __launch_bounds__((TI + 1) * TJ) k_ens_stage_f64(const EnsParams e) {
+__global__ void __launch_bounds__((TI + 1) * TJ, ens_min_blocks(TI, TJ)) k_ens_stage_f64(const EnsParams e) {
     for (int T = blockIdx.x; T < e.total_tiles; T += gridDim.x) {
         const int q = e.tile_inst[T];
         const StageParams p = ens_view(e, q);

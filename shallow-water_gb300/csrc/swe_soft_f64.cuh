@@ -154,34 +154,9 @@ SWE_HD u64 unpack_normalised(u64 b, int &e) {
     return m << lz;
 }
 
-// x / y, round to nearest even.
-SWE_HD double div_rn(double x, double y) {
-    const u64 bx = ubits(x), by = ubits(y);
-    const u64 sign = (bx ^ by) & SIGN_BIT;
-    const u64 ax = bx & ~SIGN_BIT, ay = by & ~SIGN_BIT;
-    u64 mx, my;
-    int ex, ey;
-    if (ax - HIDDEN >= INF - HIDDEN || ay - HIDDEN >= INF - HIDDEN) {
-        // some operand is zero, subnormal, infinite or NaN
-        if (ax > INF || ay > INF) return ufrom(QNAN);
-        if (ax == INF) return ufrom(ay == INF ? QNAN : (sign | INF));
-        if (ay == INF) return ufrom(sign);
-        if (ay == 0) return ufrom(ax == 0 ? QNAN : (sign | INF));
-        if (ax == 0) return ufrom(sign);
-        mx = unpack_normalised(ax, ex);
-        my = unpack_normalised(ay, ey);
-    } else {
-        ex = (int)(ax >> 52);
-        ey = (int)(ay >> 52);
-        mx = (ax & MANT_BITS) | HIDDEN;
-        my = (ay & MANT_BITS) | HIDDEN;
-    }
-    int e = ex - ey + 1023;
-    if (mx < my) {  // quotient significand in [1, 2)
-        mx <<= 1;
-        e -= 1;
-    }
-    // Y ~ 2^63 / d, d = my / 2^52 in [1, 2)
+// Y ~ 2^63 / d for the significand my (d = my / 2^52 in [1, 2)): an FP32 seed and two
+// fixed-point Newton steps, relative error about 2^-59.
+SWE_HD u64 recip_q63(u64 my) {
     const float f = f_from(0x3F800000u | (u32)((my >> 29) & 0x7FFFFFu));
     u64 Y = seed_q63(rcp_seed(f));
     const u64 D = my << 11;  // d * 2^63
@@ -189,6 +164,16 @@ SWE_HD double div_rn(double x, double y) {
     for (int it = 0; it < 2; ++it) {
         const i64 E = (i64)((1ull << 62) - umulhi(D, Y));  // 2^62 (1 - d y)
         Y = E >= 0 ? Y + (umulhi(Y, (u64)E) << 2) : Y - (umulhi(Y, (u64)(-E)) << 2);
+    }
+    return Y;
+}
+
+// The correctly rounded quotient of significands mx / my (both in [2^52, 2^53)) with
+// exponent e = ex - ey + 1023 and sign, given Y = recip_q63(my).
+SWE_HD double quotient(u64 sign, int e, u64 mx, u64 my, u64 Y) {
+    if (mx < my) {  // quotient significand in [1, 2)
+        mx <<= 1;
+        e -= 1;
     }
     // Q = floor(mx 2^52 / my) to within one unit
     u64 Q = umulhi(mx << 10, Y) >> 9;
@@ -206,6 +191,63 @@ SWE_HD double div_rn(double x, double y) {
         return ufrom(sign | (((u64)(e - 1) << 52) + Q));
     }
     return round_pack(sign, e, (Q << 10) | (u64)(R != 0));
+}
+
+SWE_COLD double div_special(double x, double y);
+
+// x / y for a normal y and an x that is zero, subnormal, infinite or NaN: zero
+// numerators (frequent: fluid at rest) inline, the rest out of line.
+SWE_HD double div_by_normal_special(double x, double y) {
+    const u64 bx = ubits(x);
+    return (bx & ~SIGN_BIT) == 0 ? ufrom((bx ^ ubits(y)) & SIGN_BIT) : div_special(x, y);
+}
+
+// x / y, round to nearest even.
+SWE_HD double div_rn(double x, double y) {
+    const u64 bx = ubits(x), by = ubits(y);
+    const u64 ax = bx & ~SIGN_BIT, ay = by & ~SIGN_BIT;
+    if (ay - HIDDEN >= INF - HIDDEN) return div_special(x, y);
+    if (ax - HIDDEN >= INF - HIDDEN) return div_by_normal_special(x, y);
+    const u64 my = (ay & MANT_BITS) | HIDDEN;
+    return quotient((bx ^ by) & SIGN_BIT, (int)(ax >> 52) - (int)(ay >> 52) + 1023,
+                    (ax & MANT_BITS) | HIDDEN, my, recip_q63(my));
+}
+
+// x1 / y and x2 / y, each round to nearest even, sharing the reciprocal of y.
+SWE_HD void div2_rn(double x1, double x2, double y, double &q1, double &q2) {
+    const u64 b1 = ubits(x1), b2 = ubits(x2), by = ubits(y);
+    const u64 a1 = b1 & ~SIGN_BIT, a2 = b2 & ~SIGN_BIT, ay = by & ~SIGN_BIT;
+    if (ay - HIDDEN >= INF - HIDDEN) {
+        q1 = div_special(x1, y);
+        q2 = div_special(x2, y);
+        return;
+    }
+    const u64 my = (ay & MANT_BITS) | HIDDEN;
+    const u64 Y = recip_q63(my);
+    const int ey = (int)(ay >> 52);
+    q1 = a1 - HIDDEN >= INF - HIDDEN
+             ? div_by_normal_special(x1, y)
+             : quotient((b1 ^ by) & SIGN_BIT, (int)(a1 >> 52) - ey + 1023,
+                        (a1 & MANT_BITS) | HIDDEN, my, Y);
+    q2 = a2 - HIDDEN >= INF - HIDDEN
+             ? div_by_normal_special(x2, y)
+             : quotient((b2 ^ by) & SIGN_BIT, (int)(a2 >> 52) - ey + 1023,
+                        (a2 & MANT_BITS) | HIDDEN, my, Y);
+}
+
+// Some operand zero, subnormal, infinite or NaN.
+SWE_COLD double div_special(double x, double y) {
+    const u64 bx = ubits(x), by = ubits(y);
+    const u64 sign = (bx ^ by) & SIGN_BIT;
+    const u64 ax = bx & ~SIGN_BIT, ay = by & ~SIGN_BIT;
+    if (ax > INF || ay > INF) return ufrom(QNAN);
+    if (ax == INF) return ufrom(ay == INF ? QNAN : (sign | INF));
+    if (ay == INF) return ufrom(sign);
+    if (ay == 0) return ufrom(ax == 0 ? QNAN : (sign | INF));
+    if (ax == 0) return ufrom(sign);
+    int ex, ey;
+    const u64 mx = unpack_normalised(ax, ex), my = unpack_normalised(ay, ey);
+    return quotient(sign, ex - ey + 1023, mx, my, recip_q63(my));
 }
 
 // sqrt(x), round to nearest even.

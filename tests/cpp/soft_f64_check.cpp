@@ -1,4 +1,5 @@
-// Checks the integer-pipe binary64 division, square root, multiplication and addition
+// Checks the integer-pipe binary64 division (single and two numerators sharing a
+// reciprocal), square root, multiplication and addition
 // (shallow-water_gb300/csrc/swe_soft_f64.cuh) bitwise against the host's IEEE
 // operations: edge values of every class, random operands over the whole exponent
 // range and at physical scales, exact quotients and squares and their neighbours,
@@ -45,6 +46,16 @@ static void check_div(double x, double y) {
         std::printf("MISMATCH div(%a, %a): got %a want %a\n", x, y, got, want);
 }
 
+static void check_div2(double x1, double x2, double y) {
+    checked += 2;
+    double q1, q2;
+    swe::sf::div2_rn(x1, x2, y, q1, q2);
+    if (!same(q1, x1 / y) && ++failures <= 20)
+        std::printf("MISMATCH div2(%a, ., %a): got %a want %a\n", x1, y, q1, x1 / y);
+    if (!same(q2, x2 / y) && ++failures <= 20)
+        std::printf("MISMATCH div2(., %a, %a): got %a want %a\n", x2, y, q2, x2 / y);
+}
+
 static void check_mul(double x, double y) {
     ++checked;
     const double want = x * y, got = mul_rn(x, y);
@@ -88,6 +99,8 @@ int main(int argc, char **argv) {
             check_div(a, b);
             check_mul(a, b);
             check_add(a, b);
+            check_div2(a, b, b);
+            check_div2(b, a, a);
         }
     }
 
@@ -112,6 +125,8 @@ int main(int argc, char **argv) {
         // whole exponent range, raw patterns (subnormal, huge, NaN payloads, signs)
         const double r1 = from_bits((int64_t)raw(rng)), r2 = from_bits((int64_t)raw(rng));
         check_div(r1, r2);
+        check_div2(r1, a, r2);
+        check_div2(a, b, std::fabs(r1));
         check_mul(r1, r2);
         check_add(r1, r2);
         check_sqrt(r1);
@@ -128,6 +143,7 @@ int main(int argc, char **argv) {
         const double y = std::ldexp((double)m27(rng), ex(rng) - 27);
         const double x = q * y;  // exact: 26 + 27 bits
         check_div(x, y);
+        check_div2(x, std::nextafter(x, -inf), y);
         check_div(std::nextafter(x, inf), y);
         check_div(std::nextafter(x, -inf), y);
         check_div(x, std::nextafter(y, inf));
