@@ -147,17 +147,15 @@ struct Face {
     double fh, fqt, fqn_m, fqn_p;
 };
 
-__device__ __forceinline__ Face face_flux(double g, double half_g, double eta_m1, double eta_0,
-                                          double eta_p1, double eta_p2, double qn_m1,
-                                          double qn_0, double qn_p1, double qn_p2, double qt_m1,
-                                          double qt_0, double qt_p1, double qt_p2,
-                                          double b_minus, double b_plus) {
-    const double d_eta0 = fsub<0>(eta_0, eta_m1), d_eta1 = fsub<0>(eta_p1, eta_0);
-    const double d_eta2 = fsub<0>(eta_p2, eta_p1);
-    const double d_qn0 = fsub<0>(qn_0, qn_m1), d_qn1 = fsub<0>(qn_p1, qn_0);
-    const double d_qn2 = fsub<0>(qn_p2, qn_p1);
-    const double d_qt0 = fsub<0>(qt_0, qt_m1), d_qt1 = fsub<0>(qt_p1, qt_0);
-    const double d_qt2 = fsub<0>(qt_p2, qt_p1);
+// The stencil differences (d0 = x0 - x_m1, d1 = x_p1 - x0, d2 = x_p2 - x_p1 of eta, qn,
+// qt) are computed once per cell pair in shared memory and shared by the three
+// interfaces that use each of them; the values are the reference's own differences.
+__device__ __forceinline__ Face face_flux(double g, double half_g, double eta_0, double eta_p1,
+                                          double d_eta0, double d_eta1, double d_eta2,
+                                          double qn_0, double qn_p1, double d_qn0,
+                                          double d_qn1, double d_qn2, double qt_0,
+                                          double qt_p1, double d_qt0, double d_qt1,
+                                          double d_qt2, double b_minus, double b_plus) {
     const double eta_minus = fadd<1>(eta_0, x64::halve(x64::minmod(d_eta0, d_eta1)));
     const double eta_plus = fsub<1>(eta_p1, x64::halve(x64::minmod(d_eta1, d_eta2)));
     const double qn_minus = fadd<1>(qn_0, x64::halve(x64::minmod(d_qn0, d_qn1)));
@@ -237,14 +235,28 @@ __device__ __forceinline__ double stage_dt(const StageParams &p) {
 // coordinates) plus a 2-cell halo, compute its interfaces, and update its cells.
 // Returns the thread's cell wave speed of the new state (stage 3), else 0.
 // (TI + 1) * TJ threads; the caller provides dt (same for the whole block).
+// Shared memory of one tile (dynamic: up to 53 KB for the 4x64 shape).
+template <int TI, int TJ>
+struct TileF64 {
+    static constexpr int RI = TI + 4, RJ = TJ + 4;
+    double hu[RI][RJ], hv[RI][RJ], B[RI][RJ], eta[RI][RJ];  // tile + 2-cell halo
+    double dx[3][RI - 1][TJ];  // eta, hu, hv: row r minus row r - 1 (r = 1..RI-1), tile columns
+    double dy[3][TI][RJ - 1];  // eta, hu, hv: column c minus column c - 1, tile rows
+    double xf[4][TI + 1][TJ];  // x-interfaces: fh, fhv, fhu_m, fhu_p
+    double yf[4][TI][TJ + 1];  // y-interfaces: gh, ghu, ghv_m, ghv_p
+};
+
+// One tile of one RK stage: stage the TI x TJ tile (origin i0, j0 in interior
+// coordinates) plus a 2-cell halo, compute its interfaces, and update its cells.
+// Returns the thread's cell wave speed of the new state (stage 3), else 0.
+// (TI + 1) * TJ threads; the caller provides dt (same for the whole block).
 template <int TI, int TJ, int STAGE>
 __device__ __forceinline__ double stage_tile_f64(const StageParams &p, int i0, int j0,
                                                  double dt) {
     constexpr int NT = (TI + 1) * TJ, RI = TI + 4, RJ = TJ + 4;
     static_assert(TI * (TJ + 1) <= NT, "one thread per y-face");
-    __shared__ double s_h[RI][RJ], s_hu[RI][RJ], s_hv[RI][RJ], s_B[RI][RJ], s_eta[RI][RJ];
-    __shared__ double s_xf[4][TI + 1][TJ];  // fh, fhv, fhu_m, fhu_p
-    __shared__ double s_yf[4][TI][TJ + 1];  // gh, ghu, ghv_m, ghv_p
+    extern __shared__ __align__(16) unsigned char smem_f64[];
+    TileF64<TI, TJ> &S = *reinterpret_cast<TileF64<TI, TJ> *>(smem_f64);
 
     const int tid = threadIdx.x;
     const long long P = p.pitch;
@@ -266,40 +278,63 @@ __device__ __forceinline__ double stage_tile_f64(const StageParams &p, int i0, i
         const int bi = clamp_int(ii + NG, 0, p.Nx + 2 * NG - 1);
         const int bj = clamp_int(jj + NG, 0, p.Ny + 2 * NG - 1);
         const double b_ = Bg[(long long)bi * P + bj];
-        s_h[r][c] = h_;
-        s_hu[r][c] = fx ? x64::neg(hu_) : hu_;
-        s_hv[r][c] = fy ? x64::neg(hv_) : hv_;
-        s_B[r][c] = b_;
-        s_eta[r][c] = h_ + b_;
+        S.hu[r][c] = fx ? x64::neg(hu_) : hu_;
+        S.hv[r][c] = fy ? x64::neg(hv_) : hv_;
+        S.B[r][c] = b_;
+        S.eta[r][c] = h_ + b_;
+    }
+    __syncthreads();
+
+    // Stencil differences: x along the tile columns, y along the tile rows.
+    constexpr int NDX = (RI - 1) * TJ, NDY = TI * (RJ - 1);
+    for (int t = tid; t < NDX + NDY; t += NT) {
+        if (t < NDX) {
+            const int r = t / TJ + 1, c = t - (t / TJ) * TJ;
+            S.dx[0][r - 1][c] = S.eta[r][c + NG] - S.eta[r - 1][c + NG];
+            S.dx[1][r - 1][c] = S.hu[r][c + NG] - S.hu[r - 1][c + NG];
+            S.dx[2][r - 1][c] = S.hv[r][c + NG] - S.hv[r - 1][c + NG];
+        } else {
+            const int u = t - NDX;
+            const int r = u / (RJ - 1), c = u - (u / (RJ - 1)) * (RJ - 1) + 1;
+            S.dy[0][r][c - 1] = S.eta[r + NG][c] - S.eta[r + NG][c - 1];
+            S.dy[1][r][c - 1] = S.hu[r + NG][c] - S.hu[r + NG][c - 1];
+            S.dy[2][r][c - 1] = S.hv[r + NG][c] - S.hv[r + NG][c - 1];
+        }
     }
     __syncthreads();
 
     const double g = p.g, half_g = p.half_g;
     // x-faces: between tile rows a = fr + 1 and a + 1, for fr in [0, TI]: one per thread.
+    // Differences: row a minus a - 1 is dx[.][a - 1] = dx[.][fr].
     {
         const int fr = tid / TJ, fc = tid - (tid / TJ) * TJ;
         const int a = fr + 1, c = fc + NG;
-        const Face F = face_flux(g, half_g, s_eta[a - 1][c], s_eta[a][c], s_eta[a + 1][c],
-                                 s_eta[a + 2][c], s_hu[a - 1][c], s_hu[a][c], s_hu[a + 1][c],
-                                 s_hu[a + 2][c], s_hv[a - 1][c], s_hv[a][c], s_hv[a + 1][c],
-                                 s_hv[a + 2][c], s_B[a][c], s_B[a + 1][c]);
-        s_xf[0][fr][fc] = F.fh;
-        s_xf[1][fr][fc] = F.fqt;
-        s_xf[2][fr][fc] = F.fqn_m;
-        s_xf[3][fr][fc] = F.fqn_p;
+        const Face F = face_flux(g, half_g, S.eta[a][c], S.eta[a + 1][c], S.dx[0][fr][fc],
+                                 S.dx[0][fr + 1][fc], S.dx[0][fr + 2][fc], S.hu[a][c],
+                                 S.hu[a + 1][c], S.dx[1][fr][fc], S.dx[1][fr + 1][fc],
+                                 S.dx[1][fr + 2][fc], S.hv[a][c], S.hv[a + 1][c],
+                                 S.dx[2][fr][fc], S.dx[2][fr + 1][fc], S.dx[2][fr + 2][fc],
+                                 S.B[a][c], S.B[a + 1][c]);
+        S.xf[0][fr][fc] = F.fh;
+        S.xf[1][fr][fc] = F.fqt;
+        S.xf[2][fr][fc] = F.fqn_m;
+        S.xf[3][fr][fc] = F.fqn_p;
     }
     // y-faces: between tile columns a = fc + 1 and a + 1, for fc in [0, TJ].
+    // Differences: column a minus a - 1 is dy[.][fr][a - 1] = dy[.][fr][fc].
     if (tid < TI * (TJ + 1)) {
         const int fr = tid / (TJ + 1), fc = tid - (tid / (TJ + 1)) * (TJ + 1);
         const int r = fr + NG, a = fc + 1;
-        const Face F = face_flux(g, half_g, s_eta[r][a - 1], s_eta[r][a], s_eta[r][a + 1],
-                                 s_eta[r][a + 2], s_hv[r][a - 1], s_hv[r][a], s_hv[r][a + 1],
-                                 s_hv[r][a + 2], s_hu[r][a - 1], s_hu[r][a], s_hu[r][a + 1],
-                                 s_hu[r][a + 2], s_B[r][a], s_B[r][a + 1]);
-        s_yf[0][fr][fc] = F.fh;
-        s_yf[1][fr][fc] = F.fqt;
-        s_yf[2][fr][fc] = F.fqn_m;
-        s_yf[3][fr][fc] = F.fqn_p;
+        const Face F = face_flux(g, half_g, S.eta[r][a], S.eta[r][a + 1], S.dy[0][fr][fc],
+                                 S.dy[0][fr][fc + 1], S.dy[0][fr][fc + 2], S.hv[r][a],
+                                 S.hv[r][a + 1], S.dy[2][fr][fc], S.dy[2][fr][fc + 1],
+                                 S.dy[2][fr][fc + 2], S.hu[r][a], S.hu[r][a + 1],
+                                 S.dy[1][fr][fc], S.dy[1][fr][fc + 1], S.dy[1][fr][fc + 2],
+                                 S.B[r][a], S.B[r][a + 1]);
+        S.yf[0][fr][fc] = F.fh;
+        S.yf[1][fr][fc] = F.fqt;
+        S.yf[2][fr][fc] = F.fqn_m;
+        S.yf[3][fr][fc] = F.fqn_p;
     }
     __syncthreads();
 
@@ -312,18 +347,18 @@ __device__ __forceinline__ double stage_tile_f64(const StageParams &p, int i0, i
         // fluxes against left/bottom face plus-side fluxes.
         // -inv_dx * (a - b) - inv_dy * (c - d); (-c) * x == -(c * x) exactly.
         const double rh =
-            fsub<4>(x64::neg(mul_const(p.inv_dx, p.kx, fsub<4>(s_xf[0][ty + 1][tx], s_xf[0][ty][tx]))),
-                    mul_const(p.inv_dy, p.ky, fsub<4>(s_yf[0][ty][tx + 1], s_yf[0][ty][tx])));
+            fsub<4>(x64::neg(mul_const(p.inv_dx, p.kx, fsub<4>(S.xf[0][ty + 1][tx], S.xf[0][ty][tx]))),
+                    mul_const(p.inv_dy, p.ky, fsub<4>(S.yf[0][ty][tx + 1], S.yf[0][ty][tx])));
         const double rhu =
-            fsub<4>(x64::neg(mul_const(p.inv_dx, p.kx, fsub<4>(s_xf[2][ty + 1][tx], s_xf[3][ty][tx]))),
-                    mul_const(p.inv_dy, p.ky, fsub<4>(s_yf[1][ty][tx + 1], s_yf[1][ty][tx])));
+            fsub<4>(x64::neg(mul_const(p.inv_dx, p.kx, fsub<4>(S.xf[2][ty + 1][tx], S.xf[3][ty][tx]))),
+                    mul_const(p.inv_dy, p.ky, fsub<4>(S.yf[1][ty][tx + 1], S.yf[1][ty][tx])));
         const double rhv =
-            fsub<4>(x64::neg(mul_const(p.inv_dx, p.kx, fsub<4>(s_xf[1][ty + 1][tx], s_xf[1][ty][tx]))),
-                    mul_const(p.inv_dy, p.ky, fsub<4>(s_yf[2][ty][tx + 1], s_yf[3][ty][tx])));
+            fsub<4>(x64::neg(mul_const(p.inv_dx, p.kx, fsub<4>(S.xf[1][ty + 1][tx], S.xf[1][ty][tx]))),
+                    mul_const(p.inv_dy, p.ky, fsub<4>(S.yf[2][ty][tx + 1], S.yf[3][ty][tx])));
         const long long k = (long long)(ii + NG) * P + (jj + NG);
-        const double sh = s_h[ty + NG][tx + NG];
-        const double shu = s_hu[ty + NG][tx + NG];
-        const double shv = s_hv[ty + NG][tx + NG];
+        const double sh = hs[k];  // interior cell: no ghost mapping
+        const double shu = S.hu[ty + NG][tx + NG];
+        const double shv = S.hv[ty + NG][tx + NG];
         // U + dt * L(U)
         const double eh = fadd<4>(sh, fmul<4>(dt, rh));
         const double ehu = fadd<4>(shu, fmul<4>(dt, rhu));
@@ -474,26 +509,62 @@ __global__ void k_fill_ghosts_f64(double *h, double *hu, double *hv, int Nx, int
 
 }  // namespace
 
-cudaError_t launch_stage_f64(int stage, const StageParams &p, cudaStream_t s) {
-    constexpr int TI = 8, TJ = 32, NT = (TI + 1) * TJ;
+// Once per kernel and device: the largest shared-memory carveout (four tiles of up to
+// 47 KB per SM) and, above 48 KB, the opt-in to that much dynamic shared memory.
+// `done` is the caller's per-kernel, per-device flag array.
+template <class K>
+static cudaError_t smem_opt_in(K kernel, size_t bytes, bool (&done)[64]) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (done[dev]) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e == cudaSuccess && bytes > 48 * 1024)
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return e;
+    done[dev] = true;
+    return cudaSuccess;
+}
+
+template <int TI, int TJ, int STAGE>
+static cudaError_t single_launch_f64(const StageParams &p, cudaStream_t s) {
+    constexpr int NT = (TI + 1) * TJ;
+    constexpr size_t smem = sizeof(TileF64<TI, TJ>);
+    static bool done[64];  // one per kernel instantiation
+    const cudaError_t e = smem_opt_in(k_stage_f64<TI, TJ, STAGE>, smem, done);
+    if (e != cudaSuccess) return e;
     const dim3 grid((p.Ny + TJ - 1) / TJ, (p.Nx + TI - 1) / TI);
+    k_stage_f64<TI, TJ, STAGE><<<grid, NT, smem, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stage_f64(int stage, const StageParams &p, cudaStream_t s) {
     switch (stage) {
-        case 1: k_stage_f64<TI, TJ, 1><<<grid, NT, 0, s>>>(p); break;
-        case 2: k_stage_f64<TI, TJ, 2><<<grid, NT, 0, s>>>(p); break;
-        default: k_stage_f64<TI, TJ, 3><<<grid, NT, 0, s>>>(p); break;
+        case 1: return single_launch_f64<8, 32, 1>(p, s);
+        case 2: return single_launch_f64<8, 32, 2>(p, s);
+        default: return single_launch_f64<8, 32, 3>(p, s);
     }
+}
+
+template <int TI, int TJ, int STAGE>
+static cudaError_t ens_launch_stage(const EnsParams &e, int grid, cudaStream_t s) {
+    constexpr int NT = (TI + 1) * TJ;
+    constexpr size_t smem = sizeof(TileF64<TI, TJ>);
+    static bool done[64];  // one per kernel instantiation
+    const cudaError_t err = smem_opt_in(k_ens_stage_f64<TI, TJ, STAGE>, smem, done);
+    if (err != cudaSuccess) return err;
+    k_ens_stage_f64<TI, TJ, STAGE><<<grid, NT, smem, s>>>(e);
     return cudaGetLastError();
 }
 
 template <int TI, int TJ>
 static cudaError_t ens_launch_f64(int stage, const EnsParams &e, int grid, cudaStream_t s) {
-    constexpr int NT = (TI + 1) * TJ;
     switch (stage) {
-        case 1: k_ens_stage_f64<TI, TJ, 1><<<grid, NT, 0, s>>>(e); break;
-        case 2: k_ens_stage_f64<TI, TJ, 2><<<grid, NT, 0, s>>>(e); break;
-        default: k_ens_stage_f64<TI, TJ, 3><<<grid, NT, 0, s>>>(e); break;
+        case 1: return ens_launch_stage<TI, TJ, 1>(e, grid, s);
+        case 2: return ens_launch_stage<TI, TJ, 2>(e, grid, s);
+        default: return ens_launch_stage<TI, TJ, 3>(e, grid, s);
     }
-    return cudaGetLastError();
 }
 
 cudaError_t launch_ens_stage_f64(int shape, int stage, const EnsParams &e, int grid,
