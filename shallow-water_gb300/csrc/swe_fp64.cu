@@ -105,8 +105,16 @@ __device__ __forceinline__ void hll_normal(double g, double half_g, double hL, d
     const double utL = wetL ? x64::redivide(qtL, hL, utm) : 0.0;
     const double unR = wetR ? x64::redivide(qnR, hR, unp) : 0.0;
     const double utR = wetR ? x64::redivide(qtR, hR, utp) : 0.0;
-    const double cL = sf::sqrt_rn(fmul<3>(g, hL));
-    const double cR = sf::sqrt_rn(fmul<3>(g, hR));
+    // Wave speeds of both sides through one inlined copy of the square root.
+    double cL = 0.0, cR = 0.0;
+#pragma unroll 1
+    for (int side = 0; side < 2; ++side) {
+        const double c = sf::sqrt_rn(fmul<3>(g, side ? hR : hL));
+        if (side)
+            cR = c;
+        else
+            cL = c;
+    }
     const double sL = dmin(fsub<2>(unL, cL), fsub<2>(unR, cR));
     const double sR = dmax(fadd<2>(unL, cL), fadd<2>(unR, cR));
     const double FL_h = qnL;
@@ -170,9 +178,21 @@ __device__ __forceinline__ Face face_flux(double g, double half_g, double eta_0,
     const double b_star = m_star ? b_minus : b_plus;
     const double h_minus = x64::positive_part(fsub<1>(eta_minus, b_minus));
     const double h_plus = x64::positive_part(fsub<1>(eta_plus, b_plus));
-    double un_minus, ut_minus, un_plus, ut_plus;
-    safe_velocity2(qn_minus, qt_minus, h_minus, un_minus, ut_minus);
-    safe_velocity2(qn_plus, qt_plus, h_plus, un_plus, ut_plus);
+    // Velocities of both sides through one inlined copy of the division.
+    double un_minus = 0.0, ut_minus = 0.0, un_plus = 0.0, ut_plus = 0.0;
+#pragma unroll 1
+    for (int side = 0; side < 2; ++side) {
+        double a, b;
+        safe_velocity2(side ? qn_plus : qn_minus, side ? qt_plus : qt_minus,
+                       side ? h_plus : h_minus, a, b);
+        if (side) {
+            un_plus = a;
+            ut_plus = b;
+        } else {
+            un_minus = a;
+            ut_minus = b;
+        }
+    }
     const double h_o = m_star ? h_plus : h_minus;  // the side b_star is not taken from
     const double hs_o = x64::positive_part(fsub<1>(m_star ? eta_plus : eta_minus, b_star));
     const double hs_minus = m_star ? h_minus : hs_o;
@@ -304,37 +324,42 @@ __device__ __forceinline__ double stage_tile_f64(const StageParams &p, int i0, i
     __syncthreads();
 
     const double g = p.g, half_g = p.half_g;
-    // x-faces: between tile rows a = fr + 1 and a + 1, for fr in [0, TI]: one per thread.
-    // Differences: row a minus a - 1 is dx[.][a - 1] = dx[.][fr].
-    {
-        const int fr = tid / TJ, fc = tid - (tid / TJ) * TJ;
-        const int a = fr + 1, c = fc + NG;
-        const Face F = face_flux(g, half_g, S.eta[a][c], S.eta[a + 1][c], S.dx[0][fr][fc],
-                                 S.dx[0][fr + 1][fc], S.dx[0][fr + 2][fc], S.hu[a][c],
-                                 S.hu[a + 1][c], S.dx[1][fr][fc], S.dx[1][fr + 1][fc],
-                                 S.dx[1][fr + 2][fc], S.hv[a][c], S.hv[a + 1][c],
-                                 S.dx[2][fr][fc], S.dx[2][fr + 1][fc], S.dx[2][fr + 2][fc],
-                                 S.B[a][c], S.B[a + 1][c]);
-        S.xf[0][fr][fc] = F.fh;
-        S.xf[1][fr][fc] = F.fqt;
-        S.xf[2][fr][fc] = F.fqn_m;
-        S.xf[3][fr][fc] = F.fqn_p;
-    }
-    // y-faces: between tile columns a = fc + 1 and a + 1, for fc in [0, TJ].
-    // Differences: column a minus a - 1 is dy[.][fr][a - 1] = dy[.][fr][fc].
-    if (tid < TI * (TJ + 1)) {
-        const int fr = tid / (TJ + 1), fc = tid - (tid / (TJ + 1)) * (TJ + 1);
-        const int r = fr + NG, a = fc + 1;
-        const Face F = face_flux(g, half_g, S.eta[r][a], S.eta[r][a + 1], S.dy[0][fr][fc],
-                                 S.dy[0][fr][fc + 1], S.dy[0][fr][fc + 2], S.hv[r][a],
-                                 S.hv[r][a + 1], S.dy[2][fr][fc], S.dy[2][fr][fc + 1],
-                                 S.dy[2][fr][fc + 2], S.hu[r][a], S.hu[r][a + 1],
-                                 S.dy[1][fr][fc], S.dy[1][fr][fc + 1], S.dy[1][fr][fc + 2],
-                                 S.B[r][a], S.B[r][a + 1]);
-        S.yf[0][fr][fc] = F.fh;
-        S.yf[1][fr][fc] = F.fqt;
-        S.yf[2][fr][fc] = F.fqn_m;
-        S.yf[3][fr][fc] = F.fqn_p;
+    // Interfaces, one code path for both directions (a single inlined copy of the flux
+    // keeps the kernel within the instruction cache):
+    //  pass 0, x-faces between tile rows a = fr + 1 and a + 1, fr in [0, TI], one per
+    //    thread; the difference of rows a and a - 1 is dx[.][fr];
+    //  pass 1, y-faces between tile columns a = fc + 1 and a + 1, fc in [0, TJ]; the
+    //    difference of columns a and a - 1 is dy[.][fr][fc].
+#pragma unroll 1
+    for (int pass = 0; pass < 2; ++pass) {
+        const bool xp = pass == 0;
+        if (!xp && tid >= TI * (TJ + 1)) break;
+        const int W = xp ? TJ : TJ + 1;
+        const int fr = tid / W, fc = tid - (tid / W) * W;
+        // cells c0 and p1 of the stencil and the three differences of each field
+        const int r0 = xp ? fr + 1 : fr + NG, c0 = xp ? fc + NG : fc + 1;
+        const int r1 = xp ? r0 + 1 : r0, c1 = xp ? c0 : c0 + 1;
+        const double *D0 = xp ? &S.dx[0][fr][fc] : &S.dy[0][fr][fc];
+        const double *Dn = xp ? &S.dx[1][fr][fc] : &S.dy[2][fr][fc];  // normal momentum
+        const double *Dt = xp ? &S.dx[2][fr][fc] : &S.dy[1][fr][fc];  // tangential
+        const int st = xp ? TJ : 1;  // stride to the next difference
+        const double(*N)[TileF64<TI, TJ>::RJ] = xp ? S.hu : S.hv;
+        const double(*T)[TileF64<TI, TJ>::RJ] = xp ? S.hv : S.hu;
+        const Face F = face_flux(g, half_g, S.eta[r0][c0], S.eta[r1][c1], D0[0], D0[st],
+                                 D0[2 * st], N[r0][c0], N[r1][c1], Dn[0], Dn[st], Dn[2 * st],
+                                 T[r0][c0], T[r1][c1], Dt[0], Dt[st], Dt[2 * st], S.B[r0][c0],
+                                 S.B[r1][c1]);
+        if (xp) {
+            S.xf[0][fr][fc] = F.fh;
+            S.xf[1][fr][fc] = F.fqt;
+            S.xf[2][fr][fc] = F.fqn_m;
+            S.xf[3][fr][fc] = F.fqn_p;
+        } else {
+            S.yf[0][fr][fc] = F.fh;
+            S.yf[1][fr][fc] = F.fqt;
+            S.yf[2][fr][fc] = F.fqn_m;
+            S.yf[3][fr][fc] = F.fqn_p;
+        }
     }
     __syncthreads();
 
