@@ -294,15 +294,15 @@ cudaError_t forward_step_into(Adj &A, double *const *W, double *const *out, doub
     sp.hs = W[0]; sp.hus = W[1]; sp.hvs = W[2];
     sp.ho = U1[0]; sp.huo = U1[1]; sp.hvo = U1[2];
     sp.mask = mk[0];
-    ACK(launch_stage_f64(1, sp, c->stream));
+    ACK(launch_stage_f64(1, sp, nullptr, c->stream));
     sp.hs = U1[0]; sp.hus = U1[1]; sp.hvs = U1[2];
     sp.ho = U2[0]; sp.huo = U2[1]; sp.hvo = U2[2];
     sp.mask = mk[1];
-    ACK(launch_stage_f64(2, sp, c->stream));
+    ACK(launch_stage_f64(2, sp, nullptr, c->stream));
     sp.hs = U2[0]; sp.hus = U2[1]; sp.hvs = U2[2];
     sp.ho = out[0]; sp.huo = out[1]; sp.hvo = out[2];
     sp.mask = mk[2];
-    ACK(launch_stage_f64(3, sp, c->stream));
+    ACK(launch_stage_f64(3, sp, nullptr, c->stream));
     c->launches += 3;
     ++A.fwd_steps;
     return cudaSuccess;

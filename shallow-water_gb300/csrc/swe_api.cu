@@ -56,8 +56,8 @@ int set_device(swe_ctx *c) {
 
 }  // namespace
 
-bool swe::encode_tile_map_f32(CUtensorMap *m, const void *base, int rows, int cols,
-                              long long pitch, int box_rows, int box_cols) {
+bool swe::encode_tile_map(CUtensorMap *m, const void *base, int rows, int cols,
+                          long long pitch, int box_rows, int box_cols, int elem) {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     if (!encode) {
         void *fn = nullptr;
@@ -71,10 +71,12 @@ bool swe::encode_tile_map_f32(CUtensorMap *m, const void *base, int rows, int co
         encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
     }
     const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-    const cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float)};
+    const cuuint64_t strides[1] = {(cuuint64_t)pitch * (cuuint64_t)elem};
     const cuuint32_t box[2] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows};
     const cuuint32_t estr[2] = {1, 1};
-    return encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void *>(base), dims, strides,
+    const CUtensorMapDataType type =
+        elem == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    return encode(m, type, 2, const_cast<void *>(base), dims, strides,
                   box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
@@ -139,24 +141,27 @@ int refresh_speed(swe_ctx *c) {
 cudaError_t launch_stage(swe_ctx *c, int stage, const StageParams &sp) {
     if (fp32(c))
         return launch_stage_f32(stage, sp, c->maps_ok ? &c->maps[stage - 1] : nullptr, c->stream);
-    return launch_stage_f64(stage, sp, c->stream);
+    return launch_stage_f64(stage, sp, c->maps_ok ? &c->maps[stage - 1] : nullptr, c->stream);
 }
 
-// TMA maps of the three stage sources of an FP32 context (box = tile + 2-cell halo).
-// Any failure leaves maps_ok false and every tile on the mirrored-index loader.
+// TMA maps of the three stage sources of a context (box = tile + 2-cell halo): the FP32
+// form's (eta, hu, hv, B) or the FP64 form's (h, hu, hv, B).  Any failure leaves maps_ok
+// false and every tile on the mirrored-index loader.
 void build_maps(swe_ctx *c) {
     c->maps_ok = false;
     const char *off = std::getenv("SWE_GB300_NO_TMA");
     if (off && off[0] == '1') return;
     const int rows = c->p.Nx + 4, cols = c->p.Ny + 4;
-    const int bi = TILE_I_F32 + 4, bj = TILE_J_F32 + 4;
+    const bool f32 = fp32(c);
+    const int bi = (f32 ? TILE_I_F32 : TILE_I_F64) + 4, bj = (f32 ? TILE_J_F32 : TILE_J_F64) + 4;
+    const int el = f32 ? 4 : 8;
     void *const *src[3] = {c->Un, c->U1, c->U2};
     for (int s = 0; s < 3; ++s) {
         StageMaps &m = c->maps[s];
-        if (!encode_tile_map_f32(&m.e, src[s][0], rows, cols, c->pitch, bi, bj) ||
-            !encode_tile_map_f32(&m.u, src[s][1], rows, cols, c->pitch, bi, bj) ||
-            !encode_tile_map_f32(&m.v, src[s][2], rows, cols, c->pitch, bi, bj) ||
-            !encode_tile_map_f32(&m.b, c->B, rows, cols, c->pitch, bi, bj))
+        if (!encode_tile_map(&m.e, src[s][0], rows, cols, c->pitch, bi, bj, el) ||
+            !encode_tile_map(&m.u, src[s][1], rows, cols, c->pitch, bi, bj, el) ||
+            !encode_tile_map(&m.v, src[s][2], rows, cols, c->pitch, bi, bj, el) ||
+            !encode_tile_map(&m.b, c->B, rows, cols, c->pitch, bi, bj, el))
             return;
     }
     c->maps_ok = true;
@@ -275,7 +280,7 @@ int swe_create(const swe_params *pin, swe_ctx **out) {
     e = cudaMemsetAsync(c->base, 0, 10 * fb + aux + staging, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cleanup(SWE_ERR_CUDA);
-    if (p.precision == SWE_PRECISION_FP32_MIXED) build_maps(c);
+    build_maps(c);
     *out = c;
     return SWE_OK;
 }
@@ -423,6 +428,8 @@ int swe_step(swe_ctx *c, int n_steps, double dt, double *t_inout) {
     c->last_ms = ms;
     c->last_steps = n_steps;
     if (t_inout) *t_inout = t1;
+    if (flags & FLAG_TIMEOUT)
+        return fail(c, SWE_ERR_TIMEOUT, "a tile's TMA copy did not complete (state undefined)");
     if (flags & FLAG_NONFINITE)
         return fail(c, SWE_ERR_NONFINITE, "non-finite state detected in GB300 solver");
     return SWE_OK;
@@ -451,6 +458,8 @@ int swe_stage(swe_ctx *c, int stage, double dt) {
     int flags = 0;
     CK(cudaMemcpyAsync(&flags, c->flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    if (flags & FLAG_TIMEOUT)
+        return fail(c, SWE_ERR_TIMEOUT, "a tile's TMA copy did not complete (state undefined)");
     if (flags & FLAG_NONFINITE)
         return fail(c, SWE_ERR_NONFINITE, "non-finite state detected in GB300 solver");
     return SWE_OK;

@@ -25,6 +25,7 @@
 #include "swe_f64_exact.cuh"
 #include "swe_soft_f64.cuh"
 #include "swe_launch.h"
+#include "swe_tma.cuh"
 
 namespace swe {
 namespace {
@@ -264,7 +265,18 @@ struct TileF64 {
     double dy[3][TI][RJ - 1];  // eta, hu, hv: column c minus column c - 1, tile rows
     double xf[4][TI + 1][TJ];  // x-interfaces: fh, fhv, fhu_m, fhu_p
     double yf[4][TI][TJ + 1];  // y-interfaces: gh, ghu, ghv_m, ghv_p
+    uint64_t bar;              // TMA transaction barrier
 };
+// The halo arrays are multiples of 128 bytes, so with the struct 128-byte aligned every
+// TMA destination is too.
+static_assert(sizeof(double) * (8 + 4) * (32 + 4) % 128 == 0, "TMA destinations aligned");
+
+template <int TI, int TJ>
+__device__ __forceinline__ TileF64<TI, TJ> &tile_smem() {
+    extern __shared__ unsigned char smem_f64[];  // sizeof(TileF64) + 128 bytes
+    const uint32_t a = tma::smem_u32(smem_f64);
+    return *reinterpret_cast<TileF64<TI, TJ> *>(smem_f64 + ((128u - (a & 127u)) & 127u));
+}
 
 // One tile of one RK stage: stage the TI x TJ tile (origin i0, j0 in interior
 // coordinates) plus a 2-cell halo, compute its interfaces, and update its cells.
@@ -272,11 +284,10 @@ struct TileF64 {
 // (TI + 1) * TJ threads; the caller provides dt (same for the whole block).
 template <int TI, int TJ, int STAGE>
 __device__ __forceinline__ double stage_tile_f64(const StageParams &p, int i0, int j0,
-                                                 double dt) {
+                                                 double dt, const tma::TileMaps *tm) {
     constexpr int NT = (TI + 1) * TJ, RI = TI + 4, RJ = TJ + 4;
     static_assert(TI * (TJ + 1) <= NT, "one thread per y-face");
-    extern __shared__ __align__(16) unsigned char smem_f64[];
-    TileF64<TI, TJ> &S = *reinterpret_cast<TileF64<TI, TJ> *>(smem_f64);
+    TileF64<TI, TJ> &S = tile_smem<TI, TJ>();
 
     const int tid = threadIdx.x;
     const long long P = p.pitch;
@@ -285,23 +296,50 @@ __device__ __forceinline__ double stage_tile_f64(const StageParams &p, int i0, i
     const double *hvs = static_cast<const double *>(p.hvs);
     const double *Bg = static_cast<const double *>(p.B);
 
-    // Stage the tile + halo; ghosts come from the wall boundary condition.
-    for (int t = tid; t < RI * RJ; t += NT) {
-        const int r = t / RJ, c = t - (t / RJ) * RJ;
-        const int ii = i0 - NG + r, jj = j0 - NG + c;
-        bool fx, fy;
-        const int mi = map_row(ii, p.Nx, p.bc, p.halo_lo, p.halo_hi, fx);
-        const int mj = map_coord(jj, p.Ny, p.bc, fy);
-        const long long k = (long long)(mi + NG) * P + (mj + NG);
-        const double hv_ = hvs[k], hu_ = hus[k], h_ = hs[k];
-        // B is read where it lies, ghosts included (clamped in overhanging tiles).
-        const int bi = clamp_int(ii + NG, 0, p.Nx + 2 * NG - 1);
-        const int bj = clamp_int(jj + NG, 0, p.Ny + 2 * NG - 1);
-        const double b_ = Bg[(long long)bi * P + bj];
-        S.hu[r][c] = fx ? x64::neg(hu_) : hu_;
-        S.hv[r][c] = fy ? x64::neg(hv_) : hv_;
-        S.B[r][c] = b_;
-        S.eta[r][c] = h_ + b_;
+    // Stage the tile + halo.  Tiles whose halo lies inside the interior are copied by
+    // TMA (h lands in eta and becomes h + B in place); tiles that touch a wall or a slab
+    // interface read through mirrored indices, ghosts from the wall rule.
+    const bool interior = tm != nullptr && i0 >= NG && j0 >= NG && i0 + TI + NG <= p.Nx &&
+                          j0 + TJ + NG <= p.Ny;
+    if (interior) {
+        if (tid == 0) tma::mbar_init(&S.bar, 1);
+        __syncthreads();
+        if (tid == 0) {
+            tma::mbar_arrive_expect_tx(&S.bar, 4u * RI * RJ * sizeof(double));
+            // halo origin (i0 - 2, j0 - 2) in interior coordinates = (i0, j0) in the
+            // ghosted array; j0 is a multiple of TJ, so x * 8 bytes is 16-byte aligned
+            tma::load_2d(&S.eta[0][0], tm->e, j0, i0, &S.bar);
+            tma::load_2d(&S.hu[0][0], tm->u, j0, i0, &S.bar);
+            tma::load_2d(&S.hv[0][0], tm->v, j0, i0, &S.bar);
+            tma::load_2d(&S.B[0][0], tm->b, j0, i0, &S.bar);
+        }
+        const bool timed_out = !tma::mbar_wait(&S.bar, 0);
+        if (__syncthreads_or(timed_out)) {
+            if (tid == 0) atomicOr(p.flags, FLAG_TIMEOUT);
+            return 0.0;
+        }
+        for (int t = tid; t < RI * RJ; t += NT) {
+            const int r = t / RJ, c = t - (t / RJ) * RJ;
+            S.eta[r][c] = S.eta[r][c] + S.B[r][c];  // h + B
+        }
+    } else {
+        for (int t = tid; t < RI * RJ; t += NT) {
+            const int r = t / RJ, c = t - (t / RJ) * RJ;
+            const int ii = i0 - NG + r, jj = j0 - NG + c;
+            bool fx, fy;
+            const int mi = map_row(ii, p.Nx, p.bc, p.halo_lo, p.halo_hi, fx);
+            const int mj = map_coord(jj, p.Ny, p.bc, fy);
+            const long long k = (long long)(mi + NG) * P + (mj + NG);
+            const double hv_ = hvs[k], hu_ = hus[k], h_ = hs[k];
+            // B is read where it lies, ghosts included (clamped in overhanging tiles).
+            const int bi = clamp_int(ii + NG, 0, p.Nx + 2 * NG - 1);
+            const int bj = clamp_int(jj + NG, 0, p.Ny + 2 * NG - 1);
+            const double b_ = Bg[(long long)bi * P + bj];
+            S.hu[r][c] = fx ? x64::neg(hu_) : hu_;
+            S.hv[r][c] = fy ? x64::neg(hv_) : hv_;
+            S.B[r][c] = b_;
+            S.eta[r][c] = h_ + b_;
+        }
     }
     __syncthreads();
 
@@ -445,9 +483,15 @@ constexpr int ens_min_blocks(int TI, int TJ) {
 
 // Single grid: one CTA per tile.
 template <int TI, int TJ, int STAGE>
-__global__ void __launch_bounds__((TI + 1) * TJ, min_blocks(TI, TJ)) k_stage_f64(const StageParams p) {
+__global__ void __launch_bounds__((TI + 1) * TJ, min_blocks(TI, TJ))
+    k_stage_f64(const StageParams p, const __grid_constant__ CUtensorMap tm_h,
+                const __grid_constant__ CUtensorMap tm_u,
+                const __grid_constant__ CUtensorMap tm_v,
+                const __grid_constant__ CUtensorMap tm_b, int use_tma) {
     const double dt = stage_dt(p);
-    const double speed = stage_tile_f64<TI, TJ, STAGE>(p, blockIdx.y * TI, blockIdx.x * TJ, dt);
+    const tma::TileMaps maps{&tm_h, &tm_u, &tm_v, &tm_b};
+    const double speed = stage_tile_f64<TI, TJ, STAGE>(p, blockIdx.y * TI, blockIdx.x * TJ, dt,
+                                                       use_tma ? &maps : nullptr);
     if (STAGE == 1 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
         p.speed[p.slot_write] = 0ull;  // read by nobody until stage 3 of this step
         if (p.dt_log) p.dt_log[p.log_index] = dt;
@@ -471,7 +515,7 @@ __global__ void __launch_bounds__((TI + 1) * TJ, ens_min_blocks(TI, TJ)) k_ens_s
         const int t = T - I.tile_base;
         const int ti = t / I.tiles_j, tj = t - (t / I.tiles_j) * I.tiles_j;
         const double dt = stage_dt(p);
-        const double speed = stage_tile_f64<TI, TJ, STAGE>(p, ti * TI, tj * TJ, dt);
+        const double speed = stage_tile_f64<TI, TJ, STAGE>(p, ti * TI, tj * TJ, dt, nullptr);
         if (STAGE == 1 && t == 0 && threadIdx.x == 0) {
             p.speed[p.slot_write] = 0ull;
             if (e.dt_last) e.dt_last[q] = dt;
@@ -553,29 +597,34 @@ static cudaError_t smem_opt_in(K kernel, size_t bytes, bool (&done)[64]) {
 }
 
 template <int TI, int TJ, int STAGE>
-static cudaError_t single_launch_f64(const StageParams &p, cudaStream_t s) {
+static cudaError_t single_launch_f64(const StageParams &p, const StageMaps *maps,
+                                     cudaStream_t s) {
     constexpr int NT = (TI + 1) * TJ;
-    constexpr size_t smem = sizeof(TileF64<TI, TJ>);
+    constexpr size_t smem = sizeof(TileF64<TI, TJ>) + 128;  // + alignment slack
     static bool done[64];  // one per kernel instantiation
     const cudaError_t e = smem_opt_in(k_stage_f64<TI, TJ, STAGE>, smem, done);
     if (e != cudaSuccess) return e;
     const dim3 grid((p.Ny + TJ - 1) / TJ, (p.Nx + TI - 1) / TI);
-    k_stage_f64<TI, TJ, STAGE><<<grid, NT, smem, s>>>(p);
+    static const StageMaps none{};  // unused when use_tma is 0
+    const StageMaps &m = maps ? *maps : none;
+    k_stage_f64<TI, TJ, STAGE><<<grid, NT, smem, s>>>(p, m.e, m.u, m.v, m.b, maps ? 1 : 0);
     return cudaGetLastError();
 }
 
-cudaError_t launch_stage_f64(int stage, const StageParams &p, cudaStream_t s) {
+cudaError_t launch_stage_f64(int stage, const StageParams &p, const StageMaps *maps,
+                             cudaStream_t s) {
+    static_assert(TILE_I_F64 == 8 && TILE_J_F64 == 32, "tile of the TMA maps");
     switch (stage) {
-        case 1: return single_launch_f64<8, 32, 1>(p, s);
-        case 2: return single_launch_f64<8, 32, 2>(p, s);
-        default: return single_launch_f64<8, 32, 3>(p, s);
+        case 1: return single_launch_f64<8, 32, 1>(p, maps, s);
+        case 2: return single_launch_f64<8, 32, 2>(p, maps, s);
+        default: return single_launch_f64<8, 32, 3>(p, maps, s);
     }
 }
 
 template <int TI, int TJ, int STAGE>
 static cudaError_t ens_launch_stage(const EnsParams &e, int grid, cudaStream_t s) {
     constexpr int NT = (TI + 1) * TJ;
-    constexpr size_t smem = sizeof(TileF64<TI, TJ>);
+    constexpr size_t smem = sizeof(TileF64<TI, TJ>) + 128;  // + alignment slack
     static bool done[64];  // one per kernel instantiation
     const cudaError_t err = smem_opt_in(k_ens_stage_f64<TI, TJ, STAGE>, smem, done);
     if (err != cudaSuccess) return err;

@@ -9,7 +9,10 @@
 namespace swe {
 
 // FP64 drop-in (swe_fp64.cu, compiled with --fmad=false).
-cudaError_t launch_stage_f64(int stage, const StageParams &p, cudaStream_t s);
+// maps (optional): TMA maps of the stage source (h, hu, hv, B) for interior tiles.
+cudaError_t launch_stage_f64(int stage, const StageParams &p, const StageMaps *maps,
+                             cudaStream_t s);
+constexpr int TILE_I_F64 = 8, TILE_J_F64 = 32;
 // Ensemble stage over the work list; shape is SHAPE_* (8x32, 8x16, 4x64 for FP64).
 cudaError_t launch_ens_stage_f64(int shape, int stage, const EnsParams &e, int grid,
                                  cudaStream_t s);

@@ -76,9 +76,10 @@ struct StageMaps {
     CUtensorMap e, u, v, b;
 };
 
-// Encodes a 2-D tiled map over a ghosted (rows x cols) FP32 field with row pitch
-// `pitch` elements and a (box_rows x box_cols) box (host; defined in swe_api.cu).
-bool encode_tile_map_f32(CUtensorMap *m, const void *base, int rows, int cols,
-                         long long pitch, int box_rows, int box_cols);
+// Encodes a 2-D tiled map over a ghosted (rows x cols) field of FP32 (elem 4) or FP64
+// (elem 8) values with row pitch `pitch` elements and a (box_rows x box_cols) box
+// (host; defined in swe_api.cu).
+bool encode_tile_map(CUtensorMap *m, const void *base, int rows, int cols, long long pitch,
+                     int box_rows, int box_cols, int elem);
 
 }  // namespace swe
