@@ -40,7 +40,7 @@ NCU_TRAFFIC_BYTES_PER_CELL_LAUNCH = 71.7
 # FP64-pipe lane operations (DADD + DMUL + DFMA) per cell update, three stages, from the
 # ncu thread-level instruction counts of the stage kernel; the pipe executes 2 per clock
 # per SM, so its peak is 2 x SMs x clock.
-FP64_OPS_PER_CELL_UPDATE = 559.8
+FP64_OPS_PER_CELL_UPDATE = 484.9
 
 
 def parse():

@@ -99,6 +99,15 @@ SWE_HD void face_forward(const FaceIn<T> &in, T g, T eps, FaceOut<T> &out) {
     out.fqn_p = F[1] + half * g * (h_p * h_p - hR * hR);
 }
 
+template <class T>
+SWE_HD T trsqrt(T x) {
+#if defined(__CUDA_ARCH__)
+    return rsqrt(x);
+#else
+    return T(1) / sqrt(x);
+#endif
+}
+
 // Branch tests and reciprocals of face_vjp.  For double they work on the bit patterns
 // (the same decisions as the IEEE comparisons for every non-NaN operand) and the
 // reciprocal is the correctly rounded integer-pipe division, so the GPU spends its
@@ -127,6 +136,22 @@ SWE_HD T half_(T a) {  // 0.5 * a, exact
     if constexpr (std::is_same<T, double>::value) return x64::halve(a);
     else return T(0.5) * a;
 }
+// c = sqrt(x) and rc = 1 / c for x > 0, both 0 otherwise; for double from one
+// integer-pipe root (c correctly rounded, rc to about 1 ulp).
+template <class T>
+SWE_HD void speed_(T x, T &c, T &rc) {
+    if (!pos_(x)) {
+        c = rc = T(0);
+        return;
+    }
+    if constexpr (std::is_same<T, double>::value) {
+        sf::sqrt_rsqrt(x, c, rc);
+    } else {
+        rc = trsqrt(x);
+        c = x * rc;
+    }
+}
+
 // minmod_sel with the sign and magnitude tests on the bit patterns for double.
 template <class T>
 SWE_HD T msel_(T a, T b, int &sel) {
@@ -148,14 +173,6 @@ SWE_HD T msel_(T a, T b, int &sel) {
     }
 }
 
-template <class T>
-SWE_HD T trsqrt(T x) {
-#if defined(__CUDA_ARCH__)
-    return rsqrt(x);
-#else
-    return T(1) / sqrt(x);
-#endif
-}
 
 // Adjoint of face_forward: given d = dJ/d(out), returns a = dJ/d(in) (overwritten).
 //
@@ -196,8 +213,9 @@ SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceI
     const T unL = wL ? un_m : T(0), utL = wL ? ut_m : T(0);
     const T unR = wR ? un_p : T(0), utR = wR ? ut_p : T(0);
     const T ghL = g * hL, ghR = g * hR;
-    const T rcL = pos_(ghL) ? trsqrt(ghL) : T(0), rcR = pos_(ghR) ? trsqrt(ghR) : T(0);
-    const T cL = ghL * rcL, cR = ghR * rcR;
+    T cL, rcL, cR, rcR;
+    speed_(ghL, cL, rcL);
+    speed_(ghR, cR, rcR);
     const T a1 = unL - cL, a2 = unR - cR, b1 = unL + cL, b2 = unR + cR;
     const bool sL_is2 = lt_(a2, a1), sR_is2 = lt_(b1, b2);
     const T sL = sL_is2 ? a2 : a1, sR = sR_is2 ? b2 : b1;

@@ -293,6 +293,50 @@ SWE_HD double sqrt_rn(double x) {
     return ufrom(((u64)((E >> 1) + 1022) << 52) + S);
 }
 
+// sqrt(x) rounded to nearest even and 1/sqrt(x) to about 2^-58 relative (the Newton
+// iterate of the root, truncated to 53 bits), for a positive normal x; other operands
+// give (sqrt_rn(x), 1 / sqrt_rn(x)) through the rare branch.  For callers that need a
+// wave speed and its reciprocal together (the adjoint's dc/dh = g / (2 c)).
+SWE_HD void sqrt_rsqrt(double x, double &s, double &r) {
+    const u64 bx = ubits(x);
+    if (bx - HIDDEN >= INF - HIDDEN) {
+        s = sqrt_rn(x);
+        r = div_rn(1.0, s);
+        return;
+    }
+    u64 mx = (bx & MANT_BITS) | HIDDEN;
+    int E = (int)(bx >> 52) - 1023;
+    if (E & 1) {
+        mx <<= 1;
+        E -= 1;
+    }
+    const float f = (float)(u32)(mx >> 22) * 9.31322574615478515625e-10f;  // * 2^-30
+    u64 Y = seed_q63(rsqrt_seed(f));
+    const u64 M = mx << 10;
+#pragma unroll
+    for (int it = 0; it < 2; ++it) {
+        const u64 T = umulhi(umulhi(Y, Y), M);
+        const i64 E1 = (i64)((1ull << 60) - T);
+        Y = E1 >= 0 ? Y + (umulhi(Y, (u64)E1) << 3) : Y - (umulhi(Y, (u64)(-E1)) << 3);
+    }
+    u64 S = umulhi(M, Y) >> 9;
+    i64 R = (i64)((mx << 52) - S * S);
+    if (R < 0) {
+        S -= 1;
+        R += (i64)(2 * S + 1);
+    } else if (R > (i64)(2 * S)) {
+        R -= (i64)(2 * S + 1);
+        S += 1;
+    }
+    S += (u64)(R > (i64)S);
+    s = ufrom(((u64)((E >> 1) + 1022) << 52) + S);
+    // Y ~ 2^63 / sqrt(m), m = mx / 2^52 in [1, 4): Y in (2^61, 2^63]; 1/sqrt(x) = Y 2^-63
+    // 2^(-E/2)
+    const int lz = clz64(Y);
+    const u64 q = (Y << lz) >> 11;  // 53 bits, leading one at bit 52
+    r = ufrom(((u64)(1022 - lz - (E >> 1)) << 52) + q);
+}
+
 // Rare operands of mul_rn: zeros, subnormals, infinities, NaN.
 SWE_COLD double mul_special(u64 ax, u64 ay, u64 sign);
 

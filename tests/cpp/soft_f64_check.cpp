@@ -73,11 +73,22 @@ static void check_add(double x, double y) {
         std::printf("MISMATCH sub(%a, %a): got %a want %a\n", x, y, gots, wants);
 }
 
+static double worst_rsqrt = 0.0;
+
 static void check_sqrt(double x) {
     ++checked;
     const double want = std::sqrt(x), got = sqrt_rn(x);
     if (!same(got, want) && ++failures <= 20)
         std::printf("MISMATCH sqrt(%a): got %a want %a\n", x, got, want);
+    if (x > 0.0 && std::isfinite(x)) {
+        double s, r;
+        swe::sf::sqrt_rsqrt(x, s, r);
+        const long double exact = 1.0L / std::sqrt((long double)x);
+        const double rel = (double)std::fabs(((long double)r - exact) / exact);
+        if (rel > worst_rsqrt) worst_rsqrt = rel;
+        if ((!same(s, want) || rel > 0x1p-51) && ++failures <= 20)
+            std::printf("MISMATCH sqrt_rsqrt(%a): s %a r %a rel %g\n", x, s, r, rel);
+    }
 }
 
 int main(int argc, char **argv) {
@@ -181,6 +192,7 @@ int main(int argc, char **argv) {
         check_add(sub, -from_bits((int64_t)(raw(rng) >> 11)));
         check_add(std::ldexp(u1(rng), 1023), std::ldexp(u1(rng), 1023));
     }
+    std::printf("worst 1/sqrt relative error %.3g\n", worst_rsqrt);
     std::printf("checked %ld operations, %ld mismatches\n", checked, failures);
     return failures ? 1 : 0;
 }
