@@ -76,6 +76,10 @@ struct EnsParams {
     double *dt_last;          // per-instance dt of the last step
     int *flags;
     int elem;                 // element size (8: FP64, 4: FP32)
+    // FP32 form: TMA maps of the current tile shape, per instance and stage source:
+    // maps[(q * 3 + s) * 4 + f], s = 0 U^n, 1 U^(1), 2 U^(2); f = eta, hu, hv, B (null:
+    // every tile uses the mirrored-index loader).  CUtensorMap is 128 bytes.
+    const void *maps;
 };
 
 enum : int { SHAPE_8x32 = 0, SHAPE_8x16 = 1, SHAPE_4x64 = 2, SHAPE_16x32 = 3, SHAPE_8x64 = 4 };
@@ -84,7 +88,7 @@ enum : int { SHAPE_8x32 = 0, SHAPE_8x16 = 1, SHAPE_4x64 = 2, SHAPE_16x32 = 3, SH
 __device__ __forceinline__ StageParams ens_view(const EnsParams &e, int q) {
     const EnsInst &I = e.inst[q];
     const long long off = I.off * e.elem;
-    StageParams p;
+    StageParams p{};  // every field defined (halo sides, mask, log: none)
     p.hs = static_cast<const char *>(e.src[0]) + off;
     p.hus = static_cast<const char *>(e.src[1]) + off;
     p.hvs = static_cast<const char *>(e.src[2]) + off;

@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -39,6 +40,7 @@ struct swe_ens {
     EnsInst *d_inst = nullptr;
     int *d_tile_inst = nullptr;
     int total_tiles = 0;
+    CUtensorMap *d_maps = nullptr;  // FP32: per instance and stage source, current shape
     unsigned long long *d_speed = nullptr;  // 2 per instance
     double *d_t = nullptr, *d_dt = nullptr;
     int *d_flags = nullptr;
@@ -110,6 +112,50 @@ void destroy_graphs(swe_ens *c) {
     c->graph_shape = -1;
 }
 
+// FP32 form: TMA maps of every instance's three stage sources for a TI x TJ tile (box
+// (TI + 4) x (TJ + 4)).  Instances too small for an interior tile never use theirs (a
+// failed encode leaves it zero); any other failure, or SWE_GB300_NO_TMA=1, leaves every
+// tile on the mirrored-index loader.
+void build_maps(swe_ens *c, int TI, int TJ) {
+    if (c->d_maps) cudaFree(c->d_maps);
+    c->d_maps = nullptr;
+    const char *off = std::getenv("SWE_GB300_NO_TMA");
+    if (off && off[0] == '1') return;
+    std::vector<CUtensorMap> maps((size_t)c->n * 12);
+    std::memset(maps.data(), 0, maps.size() * sizeof(CUtensorMap));
+    void *const *src[3] = {c->Un, c->U1, c->U2};
+    for (int q = 0; q < c->n; ++q) {
+        const EnsInst &I = c->inst[q];
+        const bool used = I.Nx >= TI + 4 && I.Ny >= TJ + 4;  // can hold an interior tile
+        const size_t o = (size_t)I.off * c->elem;
+        for (int s = 0; s < 3; ++s) {
+            const void *base[4] = {static_cast<char *>(src[s][0]) + o,
+                                   static_cast<char *>(src[s][1]) + o,
+                                   static_cast<char *>(src[s][2]) + o,
+                                   static_cast<char *>(c->B) + o};
+            for (int f = 0; f < 4; ++f) {
+                CUtensorMap &m = maps[((size_t)q * 3 + s) * 4 + f];
+                if (!encode_tile_map(&m, base[f], I.Nx + 4, I.Ny + 4, I.pitch, TI + 4, TJ + 4,
+                                     (int)c->elem)) {
+                    if (used) return;
+                    std::memset(&m, 0, sizeof m);
+                }
+            }
+        }
+    }
+    if (cudaMalloc(&c->d_maps, maps.size() * sizeof(CUtensorMap)) != cudaSuccess) {
+        cudaGetLastError();
+        c->d_maps = nullptr;
+        return;
+    }
+    if (cudaMemcpy(c->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap),
+                   cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        cudaFree(c->d_maps);
+        c->d_maps = nullptr;
+    }
+}
+
 // Work list for the current tile shape (instances in order, tiles row-major).
 int build_tiles(swe_ens *c) {
     int TI, TJ;
@@ -140,6 +186,7 @@ int build_tiles(swe_ens *c) {
     ECK(cudaStreamSynchronize(c->stream));
     c->total_tiles = (int)total;
     destroy_graphs(c);
+    if (c->f32) build_maps(c, TI, TJ);
     return SWE_OK;
 }
 
@@ -169,6 +216,7 @@ EnsParams stage_params(const swe_ens *c, int stage, int slot_read, double dt_fix
     e.dt_last = c->d_dt;
     e.flags = c->d_flags;
     e.elem = (int)c->elem;
+    e.maps = c->d_maps;
     return e;
 }
 
@@ -341,7 +389,8 @@ void swe_ens_destroy(swe_ens *c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     destroy_graphs(c);
     for (void *p : {(void *)c->base_ptr, (void *)c->snap, (void *)c->d_inst, (void *)c->d_tile_inst,
-                    (void *)c->d_speed, (void *)c->d_t, (void *)c->d_dt, (void *)c->d_flags})
+                    (void *)c->d_speed, (void *)c->d_t, (void *)c->d_dt, (void *)c->d_flags,
+                    (void *)c->d_maps})
         if (p) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);

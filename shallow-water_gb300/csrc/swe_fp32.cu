@@ -183,6 +183,7 @@ __device__ __forceinline__ float stage_tile_f32(const StageParams &p, int i0, in
         if (tid == 0) tma::mbar_init(&s_bar, 1);
         __syncthreads();
         if (tid == 0) {
+            tma::fence_proxy_async();  // the previous tile's reads of these buffers
             tma::mbar_arrive_expect_tx(&s_bar, 4u * RI * RJ * sizeof(float));
             // halo origin (i0 - 2, j0 - 2) in interior coordinates = (i0, j0) in the
             // ghosted array; j0 is a multiple of TJ, so x * 4 bytes is 16-byte aligned
@@ -319,17 +320,44 @@ __global__ void __launch_bounds__((TI + 1) * TJ)
     }
 }
 
+#ifndef SWE_ENS_F32_THREADS_PER_SM
+#define SWE_ENS_F32_THREADS_PER_SM 2016  // seven 8x32 tiles, the single-grid occupancy
+#endif
+constexpr int ens_min_blocks_f32(int TI, int TJ) {
+    return SWE_ENS_F32_THREADS_PER_SM / ((TI + 1) * TJ) > 0
+               ? SWE_ENS_F32_THREADS_PER_SM / ((TI + 1) * TJ) : 1;
+}
+
 template <int TI, int TJ, int STAGE>
-__global__ void __launch_bounds__((TI + 1) * TJ) k_ens_stage_f32(const EnsParams e) {
+__global__ void __launch_bounds__((TI + 1) * TJ, ens_min_blocks_f32(TI, TJ))
+    k_ens_stage_f32(const EnsParams e) {
+    // The instance's view lives in shared memory, read where used, as the single-grid
+    // kernel reads its parameters from the constant bank (held in registers it halves
+    // the resident CTAs).
+    __shared__ StageParams s_p;
+    __shared__ int s_t;
     for (int T = blockIdx.x; T < e.total_tiles; T += gridDim.x) {
+        if (threadIdx.x == 0) {
+            const int q = e.tile_inst[T];
+            s_p = ens_view(e, q);
+            s_t = T - e.inst[q].tile_base;
+        }
+        __syncthreads();
+        const StageParams &p = s_p;
         const int q = e.tile_inst[T];
-        const StageParams p = ens_view(e, q);
-        const EnsInst &I = e.inst[q];
-        const int t = T - I.tile_base;
-        const int ti = t / I.tiles_j, tj = t - (t / I.tiles_j) * I.tiles_j;
+        const int t = s_t;
+        const int tiles_j = e.inst[q].tiles_j;
+        const int ti = t / tiles_j, tj = t - (t / tiles_j) * tiles_j;
         const BlockDt bd = stage_dt_f32(p);
         const float dt = bd.f;
-        const float speed = stage_tile_f32<TI, TJ, STAGE>(p, ti * TI, tj * TJ, dt);
+        tma::TileMaps tm{};
+        if (e.maps) {
+            const CUtensorMap *m =
+                static_cast<const CUtensorMap *>(e.maps) + ((size_t)q * 3 + (STAGE - 1)) * 4;
+            tm = tma::TileMaps{m, m + 1, m + 2, m + 3};
+        }
+        const float speed =
+            stage_tile_f32<TI, TJ, STAGE>(p, ti * TI, tj * TJ, dt, e.maps ? &tm : nullptr);
         if (STAGE == 1 && t == 0 && threadIdx.x == 0) {
             p.speed[p.slot_write] = 0ull;
             if (e.dt_last) e.dt_last[q] = (double)dt;

@@ -305,6 +305,7 @@ __device__ __forceinline__ double stage_tile_f64(const StageParams &p, int i0, i
         if (tid == 0) tma::mbar_init(&S.bar, 1);
         __syncthreads();
         if (tid == 0) {
+            tma::fence_proxy_async();
             tma::mbar_arrive_expect_tx(&S.bar, 4u * RI * RJ * sizeof(double));
             // halo origin (i0 - 2, j0 - 2) in interior coordinates = (i0, j0) in the
             // ghosted array; j0 is a multiple of TJ, so x * 8 bytes is 16-byte aligned
@@ -508,12 +509,21 @@ __global__ void __launch_bounds__((TI + 1) * TJ, min_blocks(TI, TJ))
 // slots and time (per-instance CFL).
 template <int TI, int TJ, int STAGE>
 __global__ void __launch_bounds__((TI + 1) * TJ, ens_min_blocks(TI, TJ)) k_ens_stage_f64(const EnsParams e) {
+    // The instance's view lives in shared memory, read where used (see k_ens_stage_f32).
+    __shared__ StageParams s_p;
+    __shared__ int s_t;
     for (int T = blockIdx.x; T < e.total_tiles; T += gridDim.x) {
+        if (threadIdx.x == 0) {
+            const int q = e.tile_inst[T];
+            s_p = ens_view(e, q);
+            s_t = T - e.inst[q].tile_base;
+        }
+        __syncthreads();
+        const StageParams &p = s_p;
         const int q = e.tile_inst[T];
-        const StageParams p = ens_view(e, q);
-        const EnsInst &I = e.inst[q];
-        const int t = T - I.tile_base;
-        const int ti = t / I.tiles_j, tj = t - (t / I.tiles_j) * I.tiles_j;
+        const int t = s_t;
+        const int tiles_j = e.inst[q].tiles_j;
+        const int ti = t / tiles_j, tj = t - (t / tiles_j) * tiles_j;
         const double dt = stage_dt(p);
         const double speed = stage_tile_f64<TI, TJ, STAGE>(p, ti * TI, tj * TJ, dt, nullptr);
         if (STAGE == 1 && t == 0 && threadIdx.x == 0) {

@@ -52,6 +52,13 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
     return false;
 }
 
+// Orders this thread's earlier generic-proxy shared-memory accesses, and those of the
+// block ordered before them by a barrier, before its following TMA writes (the async
+// proxy): issued by the thread that starts the copies when the buffers are being reused.
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
 // 2-D tile (x = innermost coordinate, y = row) of `map` into shared memory at dst
 // (128-byte aligned); completes `bytes` on bar.  x times the element size must be a
 // multiple of 16 bytes.
