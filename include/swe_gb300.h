@@ -141,6 +141,16 @@ int swe_stable_dt(swe_ctx *ctx, double *out);
  * (tests/sanity_checks/mass_conservation.hpp:45-56); this is the device-side twin. */
 int swe_totals(swe_ctx *ctx, double *mass, double *momentum_x, double *momentum_y);
 
+/* Sanity reductions of the current state on the device, the quantities the reference's
+ * sanity checks compute from a downloaded state (tests/sanity_checks/): mass =
+ * sum h dx dy (MassConservation, mass_conservation.hpp:45-56; compensated here), h_min
+ * = min h over the interior (Debug, debug.hpp:40-57), first_negative = i * Ny + j of the
+ * first interior cell in row-major order with h < 0, or -1 (the cell Positivity reports,
+ * positivity.hpp:28-40), and energy = sum [ (hu^2 + hv^2) / (2h) (0 where h <= 1e-8)
+ * + g h^2 / 2 + g h B ] dx dy (no reference counterpart).  FP32 form: h = eta - B. */
+int swe_sanity(swe_ctx *ctx, double *mass, double *h_min, long long *first_negative,
+               double *energy);
+
 /* Capacity, in partial-sum blocks, of the fixed scratch used by swe_totals_noalloc. */
 #define SWE_TOTALS_NOALLOC_MAX_BLOCKS 1024
 

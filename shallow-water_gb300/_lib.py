@@ -34,7 +34,7 @@ EXPORTS = (
     "swe_ens_times", "swe_ens_last_dt", "swe_ens_last_step_ms", "swe_ens_kernel_launches",
     "swe_ens_set_schedule", "swe_ens_get_schedule", "swe_ens_tune", "swe_ens_last_error",
     "swe_totals_noalloc", "swe_adjoint_gauge", "swe_selftest_soft_f64", "swe_stage",
-    "swe_halo",
+    "swe_halo", "swe_sanity",
 )
 TOTALS_NOALLOC_MAX_BLOCKS = 1024
 ADJ_TAPE_ALL = -1  # n_snapshots value of swe_adjoint_gauge's tape mode
@@ -137,6 +137,8 @@ def lib(path: str = LIB_PATH):
     L.swe_adjoint_gauge.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ip, ip, dp,
                                     ctypes.c_int, dp, dp, dp, dp, dp, dp]
     L.swe_adjoint_gauge.restype = ctypes.c_int
+    L.swe_sanity.argtypes = [vp, dp, dp, ctypes.POINTER(ctypes.c_longlong), dp]
+    L.swe_sanity.restype = ctypes.c_int
     L.swe_stage.argtypes = [vp, ctypes.c_int, ctypes.c_double]
     L.swe_stage.restype = ctypes.c_int
     L.swe_halo.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp]

@@ -530,6 +530,29 @@ int swe_totals(swe_ctx *c, double *mass, double *mx, double *my) {
     return SWE_OK;
 }
 
+int swe_sanity(swe_ctx *c, double *mass, double *h_min, long long *first_negative,
+               double *energy) {
+    if (!c || !mass || !h_min || !first_negative || !energy)
+        return fail(c, SWE_ERR_BAD_ARG, "swe_sanity: null argument");
+    if (!c->uploaded) return fail(c, SWE_ERR_BAD_ARG, "swe_sanity: no state uploaded");
+    int st = set_device(c);
+    if (st) return st;
+    if (!c->partial)
+        CK(cudaMalloc(&c->partial, (6 * (size_t)totals_blocks(c->num_sms) + 4) * sizeof(double)));
+    double *out = c->partial + 6 * totals_blocks(c->num_sms);
+    CK(launch_sanity(c->Un[0], c->Un[1], c->Un[2], c->B, fp32(c), c->p.Nx, c->p.Ny, c->pitch,
+                     c->p.g, c->dx * c->dy, c->partial, out, c->num_sms, c->stream));
+    c->launches += 2;
+    double r[4];
+    CK(cudaMemcpyAsync(r, out, sizeof r, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    *mass = r[0];
+    *energy = r[1];
+    *h_min = r[2];
+    std::memcpy(first_negative, &r[3], sizeof(long long));
+    return SWE_OK;
+}
+
 int swe_last_step_ms(const swe_ctx *c, double *ms) {
     if (!c || !ms) return SWE_ERR_BAD_ARG;
     *ms = c->last_ms;

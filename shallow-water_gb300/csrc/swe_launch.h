@@ -51,6 +51,11 @@ int totals_blocks(int num_sms);
 cudaError_t launch_totals_blocks(const void *h, const void *hu, const void *hv, const void *B,
                                  bool f32, int Nx, int Ny, long long pitch, double dxdy,
                                  double *partial, double *out, int blocks, cudaStream_t s);
+// Sanity reductions (mass, energy, h_min, first negative index) into out[0..3];
+// partial holds 6 doubles per block, num_sms * 4 blocks.
+cudaError_t launch_sanity(const void *h, const void *hu, const void *hv, const void *B, bool f32,
+                          int Nx, int Ny, long long pitch, double g, double dxdy,
+                          double *partial, double *out, int num_sms, cudaStream_t s);
 cudaError_t launch_totals(const void *h, const void *hu, const void *hv, const void *B, bool f32,
                           int Nx, int Ny, long long pitch, double dxdy, double *partial,
                           double *out, int num_sms, cudaStream_t s);

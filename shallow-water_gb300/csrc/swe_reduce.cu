@@ -8,6 +8,7 @@
 // result is deterministic (fixed assignment and order) and accurate to about one
 // rounding of the total.  Works on both forms (FP32 eta - B is exact in FP64).
 #include <algorithm>
+#include <climits>
 #include <mutex>
 
 #include "../../include/swe_gb300.h"
@@ -97,7 +98,122 @@ __global__ void k_totals_final(const double *partial, int blocks, double scale, 
     out[threadIdx.x] = (x.s + x.c) * scale;
 }
 
+// Sanity reductions of one state in one pass (the reference's MassConservation,
+// Positivity and Debug checks, tests/sanity_checks/*.hpp, computed on the device):
+// compensated sums of h and of the energy density
+//   e = (hu^2 + hv^2) / (2 h) (h > 1e-8, else 0) + g h^2 / 2 + g h B,
+// the minimum h (NaN ignored, as `h < h_min` never selects it) and the smallest
+// row-major interior index i * Ny + j with h < 0 (the cell Positivity reports first).
+// Per block: mass pair, energy pair, h_min, first index (as a double's bits).
+template <bool F32>
+__global__ void __launch_bounds__(BT) k_sanity_partial(const void *h, const void *hu,
+                                                       const void *hv, const void *B, int Nx,
+                                                       int Ny, long long P, double g,
+                                                       double *partial) {
+    Comp mass{0, 0}, energy{0, 0};
+    double hmin = __longlong_as_double(0x7FF0000000000000LL);  // +inf
+    long long first = LLONG_MAX;
+    const long long n = (long long)Nx * Ny;
+    for (long long t = blockIdx.x * (long long)BT + threadIdx.x; t < n;
+         t += (long long)gridDim.x * BT) {
+        const int i = (int)(t / Ny), j = (int)(t - (t / Ny) * Ny);
+        const long long k = (long long)(i + NG) * P + (j + NG);
+        double hh, u, v, b;
+        if (F32) {
+            b = static_cast<const float *>(B)[k];
+            hh = (double)static_cast<const float *>(h)[k] - b;
+            u = static_cast<const float *>(hu)[k];
+            v = static_cast<const float *>(hv)[k];
+        } else {
+            hh = static_cast<const double *>(h)[k];
+            u = static_cast<const double *>(hu)[k];
+            v = static_cast<const double *>(hv)[k];
+            b = static_cast<const double *>(B)[k];
+        }
+        add(mass, hh);
+        const double kin = hh > 1.0e-8 ? 0.5 * (u * u + v * v) / hh : 0.0;
+        add(energy, kin + 0.5 * g * hh * hh + g * hh * b);
+        hmin = fmin(hmin, hh);
+        if (hh < 0.0 && t < first) first = t;
+    }
+    __shared__ Comp red[2][BT / 32];
+    __shared__ double rmin[BT / 32];
+    __shared__ long long rfirst[BT / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        Comp y;
+        y.s = __shfl_down_sync(0xffffffffu, mass.s, o);
+        y.c = __shfl_down_sync(0xffffffffu, mass.c, o);
+        mass = merge(mass, y);
+        y.s = __shfl_down_sync(0xffffffffu, energy.s, o);
+        y.c = __shfl_down_sync(0xffffffffu, energy.c, o);
+        energy = merge(energy, y);
+        hmin = fmin(hmin, __shfl_down_sync(0xffffffffu, hmin, o));
+        const long long f2 = __shfl_down_sync(0xffffffffu, first, o);
+        first = f2 < first ? f2 : first;
+    }
+    if (lane == 0) {
+        red[0][warp] = mass;
+        red[1][warp] = energy;
+        rmin[warp] = hmin;
+        rfirst[warp] = first;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Comp m = red[0][0], e = red[1][0];
+        double hm = rmin[0];
+        long long f = rfirst[0];
+        for (int w = 1; w < BT / 32; ++w) {
+            m = merge(m, red[0][w]);
+            e = merge(e, red[1][w]);
+            hm = fmin(hm, rmin[w]);
+            f = rfirst[w] < f ? rfirst[w] : f;
+        }
+        double *o = partial + (size_t)blockIdx.x * 6;
+        o[0] = m.s;
+        o[1] = m.c;
+        o[2] = e.s;
+        o[3] = e.c;
+        o[4] = hm;
+        o[5] = __longlong_as_double(f);
+    }
+}
+
+// out: mass * dxdy, energy * dxdy, h_min, first index (-1: none; as a double's bits).
+__global__ void k_sanity_final(const double *partial, int blocks, double dxdy, double *out) {
+    if (threadIdx.x != 0) return;
+    Comp m{0, 0}, e{0, 0};
+    double hm = __longlong_as_double(0x7FF0000000000000LL);
+    long long f = LLONG_MAX;
+    for (int b = 0; b < blocks; ++b) {
+        const double *o = partial + (size_t)b * 6;
+        m = merge(m, Comp{o[0], o[1]});
+        e = merge(e, Comp{o[2], o[3]});
+        hm = fmin(hm, o[4]);
+        const long long fb = __double_as_longlong(o[5]);
+        f = fb < f ? fb : f;
+    }
+    out[0] = (m.s + m.c) * dxdy;
+    out[1] = (e.s + e.c) * dxdy;
+    out[2] = hm;
+    out[3] = __longlong_as_double(f == LLONG_MAX ? -1LL : f);
+}
+
 }  // namespace
+
+cudaError_t launch_sanity(const void *h, const void *hu, const void *hv, const void *B, bool f32,
+                          int Nx, int Ny, long long pitch, double g, double dxdy,
+                          double *partial, double *out, int num_sms, cudaStream_t s) {
+    const int blocks = num_sms * 4;
+    if (f32)
+        k_sanity_partial<true><<<blocks, BT, 0, s>>>(h, hu, hv, B, Nx, Ny, pitch, g, partial);
+    else
+        k_sanity_partial<false><<<blocks, BT, 0, s>>>(h, hu, hv, B, Nx, Ny, pitch, g, partial);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_sanity_final<<<1, 32, 0, s>>>(partial, blocks, dxdy, out);
+    return cudaGetLastError();
+}
 
 int totals_blocks(int num_sms) { return num_sms * 4; }
 

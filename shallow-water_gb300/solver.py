@@ -152,6 +152,17 @@ class Solver:
         self._check(self._lib.swe_totals(self._ctx, *(ctypes.byref(x) for x in v)), "swe_totals")
         return tuple(x.value for x in v)
 
+    def sanity(self):
+        """On-device sanity reductions of the current state: mass (sum h dx dy), h_min,
+        first_negative (row-major interior index i * Ny + j of the first h < 0, or -1, the
+        cell the reference's Positivity check reports) and energy."""
+        m, hmin, e = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        first = ctypes.c_longlong()
+        self._check(self._lib.swe_sanity(self._ctx, ctypes.byref(m), ctypes.byref(hmin),
+                                         ctypes.byref(first), ctypes.byref(e)), "swe_sanity")
+        return {"mass": m.value, "h_min": hmin.value, "first_negative": first.value,
+                "energy": e.value}
+
     def kernel_launches(self) -> int:
         return int(self._lib.swe_kernel_launches(self._ctx))
 
