@@ -108,3 +108,18 @@ def test_nonfinite_reports_status(gpu_lib, sw, problems):
         with pytest.raises(sw.SweError) as e:
             s.step(1, 1e-4)
         assert e.value.status == 3
+
+
+def test_config2_16384_matches_fp64_gpu(gpu_lib, sw, problems):
+    """The precision form at its own size (16384^2 dam break over the seeded 16-Gaussian
+    bathymetry, transmissive walls) against an FP64 run of the same grid on the GPU,
+    over a reduced step count: relative L1(h) within the stated budget."""
+    n, steps = 16384, 20
+    B, _ = problems.gaussian_sum_bathymetry(n, n, n=16, seed=2026, bc="transmissive")
+    h, hu, hv = problems.dam_break(B)
+    with sw.Solver(n, n, bc="transmissive") as s:
+        s.upload(h, hu, hv, B)
+        s.step(steps)
+        ref = s.download()
+    out, _, _ = run_fp32(sw, h, hu, hv, B, n, n, steps, bc=1)
+    assert rel_l1(out[0], ref[0]) <= L1_H_TOL

@@ -164,3 +164,29 @@ def test_totals_are_compensated_sums(gpu_lib, sw, problems, precision):
     for got, a in zip((mass, mx, my), out):
         want = math.fsum(a[2:-2, 2:-2].ravel()) * dxdy
         assert abs(got - want) <= 4e-16 * max(abs(want), math.fsum(np.abs(a[2:-2, 2:-2]).ravel()) * dxdy)
+
+
+def test_config1_8192_dambreak_bitwise_two_steps(gpu_lib, sw, port, problems):
+    """The headline workload at its own size (8192^2 dam break over 16 seeded Gaussians,
+    transmissive walls, adaptive dt) against the CPU oracle over a reduced step count."""
+    n = 8192
+    B, _ = problems.gaussian_sum_bathymetry(n, n, n=16, seed=2026, bc="transmissive")
+    h, hu, hv = problems.dam_break(B)
+    ref, out, dts, t, _ = run_both(sw, port, h, hu, hv, B, n, n, 2, bc=1)
+    assert_bitwise(ref, out, dts, t)
+
+
+def test_config1_8192_lake_at_rest_stays_at_rest(gpu_lib, sw, problems):
+    """The lake-at-rest run of the 8192^2 configuration (eta = 1 over the same
+    bathymetry, u = v = 0): velocities stay at rounding level where the lake is wet."""
+    n = 8192
+    B, _ = problems.gaussian_sum_bathymetry(n, n, n=16, seed=2026, bc="transmissive")
+    h, hu, hv = problems.lake_at_rest(B)
+    with sw.Solver(n, n, bc="transmissive") as s:
+        s.upload(h, hu, hv, B)
+        s.step(20)
+        oh, ohu, ohv = s.download()
+    wet = h[2:-2, 2:-2] > 1e-3
+    assert wet.mean() > 0.5
+    assert np.abs(ohu[2:-2, 2:-2][wet]).max() < 1e-12
+    assert np.abs(ohv[2:-2, 2:-2][wet]).max() < 1e-12
