@@ -111,7 +111,10 @@ def config(n, form="fp64_dropin"):
         "workload": f"{n}x{n} dam break over seeded 16-Gaussian bathymetry, transmissive "
                     "walls, adaptive CFL dt 0.45, MUSCL+hydrostatic+HLL+SSP-RK3",
         "grid": [n, n], "form": form, "bc": "transmissive", "dt": "adaptive (cfl 0.45)",
-        "l2": "inputs larger than L2 (each step streams ~3.7 GB of state vs 129 MB L2)",
+        "l2": (f"no flush: each stage launch streams {BYTES_PER_CELL_FP64 / 3 * n * n / 1e9:.2f} GB "
+               "(algorithmic bytes) against the 129 MB L2"
+               if BYTES_PER_CELL_FP64 / 3 * n * n > 4 * 129e6 else
+               "grid smaller than 4x L2: rates include L2 reuse (a parity or tuning size)"),
         "parallelism": "replicas (one grid per GPU)",
     }
 

@@ -13,7 +13,10 @@
 namespace swe {
 namespace tma {
 
-constexpr uint32_t kSpinLimit = 1u << 26;
+// Each failed try_wait may itself suspend for a hardware-defined time (about a
+// microsecond), so 2^20 polls bound a copy that never lands near a second per tile,
+// far above the microseconds a copy takes.
+constexpr uint32_t kSpinLimit = 1u << 20;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
