@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the FP32-mixed, ensemble and adjoint measurements")
-    ap.add_argument("--forms", default="fp32_mixed,ensemble,adjoint",
+    ap.add_argument("--forms", default="fp32_mixed,ensemble,adjoint,sanity,slabs",
                     help="comma list of the extra forms to measure")
     ap.add_argument("--fp32-n", type=int, default=16384)
     ap.add_argument("--ens-count", type=int, default=512)
@@ -331,12 +331,54 @@ def form_adjoint(args, sw):
             "tape_bytes": int((75 * K + 400) * (n + 4) * (n + 4))}
 
 
+def form_sanity(args, sw):
+    """swe_sanity (mass, energy, h_min, first negative cell in one device pass) on the
+    headline grid: its bandwidth against the HBM roofline (reads h, hu, hv, B: 32 B per
+    cell), per synchronous call (launch, reduction and the copy of four numbers back)."""
+    n = args.n
+    h, hu, hv, B = workload(n, args.seed)
+    with sw.Solver(n, n, bc="transmissive") as s:
+        s.upload(h, hu, hv, B)
+        s.sanity()
+        reps = 10
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            r = s.sanity()
+        wall = (time.perf_counter() - t0) / reps
+    gbs = 32.0 * n * n / wall / 1e9
+    return {"grid": [n, n], "ms_per_call_wall": wall * 1e3, "bytes_per_cell": 32,
+            "achieved_gbs": gbs, "hbm_frac_of_measured": gbs / peaks()[0],
+            "mass": r["mass"], "h_min": r["h_min"], "first_negative": r["first_negative"]}
+
+
+def form_slabs(args, sw):
+    """The headline grid as two x-slabs on this one GPU (slabs.SlabGrid: per-stage
+    interface exchange through host memory, one global CFL dt per step) against one
+    context: the cost of the decomposition's exchange and stage-by-stage stepping."""
+    n, K = args.n, 3
+    h, hu, hv, B = workload(n, args.seed)
+    grid = sw.slabs.SlabGrid(n, n, bc="transmissive", parts=2)
+    try:
+        grid.upload(h, hu, hv, B)
+        grid.step(1)
+        t0 = time.perf_counter()
+        grid.step(K)
+        secs = time.perf_counter() - t0
+    finally:
+        grid.close()
+    return {"grid": [n, n], "parts": 2, "steps": K, "ms_per_step_wall": secs * 1e3 / K,
+            "gcups": n * n * K / secs / 1e9,
+            "exchange": "2 rows x 3 fields per interface per stage, through host memory"}
+
+
 def run_forms(args, sw, fp64_gcups):
     forms = {}
     wanted = set(args.forms.split(","))
     for name, fn in (("fp32_mixed", lambda: form_fp32(args, sw, fp64_gcups)),
                      ("ensemble", lambda: form_ensemble(args, sw)),
-                     ("adjoint", lambda: form_adjoint(args, sw))):
+                     ("adjoint", lambda: form_adjoint(args, sw)),
+                     ("sanity", lambda: form_sanity(args, sw)),
+                     ("slabs", lambda: form_slabs(args, sw))):
         if name not in wanted:
             continue
         try:

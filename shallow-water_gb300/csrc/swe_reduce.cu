@@ -2,10 +2,13 @@
 // sum hv dx dy over the interior (the quantity the reference's MassConservation check
 // accumulates naively, tests/sanity_checks/mass_conservation.hpp:45-56).
 //
-// Each thread keeps Neumaier-compensated FP64 sums over a fixed grid-stride set of
-// cells; warps and blocks combine (sum, compensation) pairs with the error-free
-// TwoSum; a second one-block kernel adds the per-block pairs in block order.  The
-// result is deterministic (fixed assignment and order) and accurate to about one
+// Each thread sums a fixed grid-stride set of cells in chunks of CHUNK cells: a plain
+// FP64 sum per chunk, then an error-free TwoSum of the chunk into the thread's
+// compensated (sum, compensation) pair - one FP64 add per value plus 6/CHUNK, where a
+// TwoSum per value would make the reduction FP64-bound on GB300.  Warps and blocks
+// combine pairs with TwoSum; a second one-block kernel adds the per-block pairs in
+// block order.  The result is deterministic (fixed assignment and order); its error is
+// that of the CHUNK-term chunk sums, about CHUNK roundings of a chunk, plus one
 // rounding of the total.  Works on both forms (FP32 eta - B is exact in FP64).
 #include <algorithm>
 #include <climits>
@@ -13,6 +16,7 @@
 
 #include "../../include/swe_gb300.h"
 #include "swe_common.cuh"
+#include "swe_soft_f64.cuh"
 #include "swe_launch.h"
 
 namespace swe {
@@ -44,12 +48,15 @@ __device__ __forceinline__ Comp merge(Comp x, Comp y) {
 }
 
 constexpr int BT = 256;
+constexpr int CHUNK = 8;
 
 template <bool F32>
 __global__ void __launch_bounds__(BT) k_totals_partial(const void *h, const void *hu,
                                                        const void *hv, const void *B, int Nx,
                                                        int Ny, long long P, double *partial) {
     Comp acc[3] = {{0, 0}, {0, 0}, {0, 0}};
+    double part[3] = {0.0, 0.0, 0.0};
+    int in_chunk = 0;
     const long long n = (long long)Nx * Ny;
     for (long long t = blockIdx.x * (long long)BT + threadIdx.x; t < n;
          t += (long long)gridDim.x * BT) {
@@ -65,10 +72,18 @@ __global__ void __launch_bounds__(BT) k_totals_partial(const void *h, const void
             v1 = static_cast<const double *>(hu)[k];
             v2 = static_cast<const double *>(hv)[k];
         }
-        add(acc[0], v0);
-        add(acc[1], v1);
-        add(acc[2], v2);
+        part[0] += v0;
+        part[1] += v1;
+        part[2] += v2;
+        if (++in_chunk == CHUNK) {
+            for (int q = 0; q < 3; ++q) {
+                add(acc[q], part[q]);
+                part[q] = 0.0;
+            }
+            in_chunk = 0;
+        }
     }
+    for (int q = 0; q < 3; ++q) add(acc[q], part[q]);
     __shared__ Comp red[3][BT / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int q = 0; q < 3; ++q) {
@@ -111,8 +126,11 @@ __global__ void __launch_bounds__(BT) k_sanity_partial(const void *h, const void
                                                        int Ny, long long P, double g,
                                                        double *partial) {
     Comp mass{0, 0}, energy{0, 0};
+    double pm = 0.0, pe = 0.0;  // chunk sums
+    int in_chunk = 0;
     double hmin = __longlong_as_double(0x7FF0000000000000LL);  // +inf
     long long first = LLONG_MAX;
+    const double half_g = 0.5 * g;
     const long long n = (long long)Nx * Ny;
     for (long long t = blockIdx.x * (long long)BT + threadIdx.x; t < n;
          t += (long long)gridDim.x * BT) {
@@ -130,12 +148,22 @@ __global__ void __launch_bounds__(BT) k_sanity_partial(const void *h, const void
             v = static_cast<const double *>(hv)[k];
             b = static_cast<const double *>(B)[k];
         }
-        add(mass, hh);
-        const double kin = hh > 1.0e-8 ? 0.5 * (u * u + v * v) / hh : 0.0;
-        add(energy, kin + 0.5 * g * hh * hh + g * hh * b);
-        hmin = fmin(hmin, hh);
-        if (hh < 0.0 && t < first) first = t;
+        // the division and the comparisons run on the integer pipe (correctly rounded /
+        // exact), the rest is one FP64 chunk sum per quantity
+        const double kin = x64::lt(1.0e-8, hh) ? sf::div_rn(x64::halve(u * u + v * v), hh) : 0.0;
+        pm += hh;
+        pe += kin + half_g * hh * hh + g * hh * b;
+        if (++in_chunk == CHUNK) {
+            add(mass, pm);
+            add(energy, pe);
+            pm = pe = 0.0;
+            in_chunk = 0;
+        }
+        if (x64::lt(hh, hmin)) hmin = hh;  // NaN never selected, as `h < h_min`
+        if (x64::lt(hh, 0.0) && t < first) first = t;
     }
+    add(mass, pm);
+    add(energy, pe);
     __shared__ Comp red[2][BT / 32];
     __shared__ double rmin[BT / 32];
     __shared__ long long rfirst[BT / 32];
@@ -148,7 +176,8 @@ __global__ void __launch_bounds__(BT) k_sanity_partial(const void *h, const void
         y.s = __shfl_down_sync(0xffffffffu, energy.s, o);
         y.c = __shfl_down_sync(0xffffffffu, energy.c, o);
         energy = merge(energy, y);
-        hmin = fmin(hmin, __shfl_down_sync(0xffffffffu, hmin, o));
+        const double hm2 = __shfl_down_sync(0xffffffffu, hmin, o);
+        if (x64::lt(hm2, hmin)) hmin = hm2;
         const long long f2 = __shfl_down_sync(0xffffffffu, first, o);
         first = f2 < first ? f2 : first;
     }
@@ -166,7 +195,7 @@ __global__ void __launch_bounds__(BT) k_sanity_partial(const void *h, const void
         for (int w = 1; w < BT / 32; ++w) {
             m = merge(m, red[0][w]);
             e = merge(e, red[1][w]);
-            hm = fmin(hm, rmin[w]);
+            if (x64::lt(rmin[w], hm)) hm = rmin[w];
             f = rfirst[w] < f ? rfirst[w] : f;
         }
         double *o = partial + (size_t)blockIdx.x * 6;
@@ -189,7 +218,7 @@ __global__ void k_sanity_final(const double *partial, int blocks, double dxdy, d
         const double *o = partial + (size_t)b * 6;
         m = merge(m, Comp{o[0], o[1]});
         e = merge(e, Comp{o[2], o[3]});
-        hm = fmin(hm, o[4]);
+        if (x64::lt(o[4], hm)) hm = o[4];
         const long long fb = __double_as_longlong(o[5]);
         f = fb < f ? fb : f;
     }

@@ -152,7 +152,9 @@ def test_run_snapshots_match_oracle(gpu_lib, sw, port, problems):
 
 @pytest.mark.parametrize("precision", ["fp64", "fp32_mixed"])
 def test_totals_are_compensated_sums(gpu_lib, sw, problems, precision):
-    """swe_totals equals the exactly rounded sum (math.fsum) of the downloaded state."""
+    """swe_totals is within its error bound of the exactly rounded sum (math.fsum) of the
+    downloaded state: plain sums of 8-cell chunks (7 roundings each) merged with
+    error-free TwoSum, so |error| <= about 9 eps times the sum of magnitudes."""
     import math
     h, hu, hv, B = problems.random_state(300, 257, seed=3, q_scale=0.2, b_scale=0.05)
     with sw.Solver(300, 257, 1.0, 1.3, precision=precision) as s:
@@ -163,7 +165,7 @@ def test_totals_are_compensated_sums(gpu_lib, sw, problems, precision):
     dxdy = (1.0 / 300) * (1.3 / 257)
     for got, a in zip((mass, mx, my), out):
         want = math.fsum(a[2:-2, 2:-2].ravel()) * dxdy
-        assert abs(got - want) <= 4e-16 * max(abs(want), math.fsum(np.abs(a[2:-2, 2:-2]).ravel()) * dxdy)
+        assert abs(got - want) <= 1e-15 * max(abs(want), math.fsum(np.abs(a[2:-2, 2:-2]).ravel()) * dxdy)
 
 
 def test_config1_8192_dambreak_bitwise_two_steps(gpu_lib, sw, port, problems):
