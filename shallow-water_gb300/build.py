@@ -46,7 +46,7 @@ def _stale(target: str, deps) -> bool:
 
 def build(verbose: bool = False, force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h", ".map"))]
     headers.append(os.path.join(HERE, "..", "include", "swe_gb300.h"))
     objs, procs = [], []
     cc = nvcc()
@@ -65,7 +65,9 @@ def build(verbose: bool = False, force: bool = False) -> str:
         if verbose:
             sys.stderr.write(open(o + ".log").read())
     if force or _stale(LIB, objs):
-        cmd = [cc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+        # the C ABI only (swe_*); the kernels' C++ launchers stay internal
+        cmd = [cc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart",
+               "-Xlinker", "--version-script=" + os.path.join(CSRC, "swe_gb300.map")]
         subprocess.run(cmd, check=True)
     return LIB
 
