@@ -219,15 +219,16 @@ SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceI
     const T a1 = unL - cL, a2 = unR - cR, b1 = unL + cL, b2 = unR + cR;
     const bool sL_is2 = lt_(a2, a1), sR_is2 = lt_(b1, b2);
     const T sL = sL_is2 ? a2 : a1, sR = sR_is2 ? b2 : b1;
-    const T FL[3] = {qnL, qnL * unL + half * g * hL * hL, qnL * utL};
-    const T FR[3] = {qnR, qnR * unR + half * g * hR * hR, qnR * utR};
+    const T hg = half * g;
+    const T FL[3] = {qnL, qnL * unL + hg * hL * hL, qnL * utL};
+    const T FR[3] = {qnR, qnR * unR + hg * hR * hR, qnR * utR};
     const T UL[3] = {hL, qnL, qtL}, UR[3] = {hR, qnR, qtR};
     const int regime = !lt_(sL, T(0)) ? 0 : (!lt_(T(0), sR) ? 1 : 2);
 
     // ---- reverse sweep ----
     const T dF[3] = {d.fh, d.fqn_m + d.fqn_p, d.fqt};
     T dh_m = g * h_m * d.fqn_m, dh_p = g * h_p * d.fqn_p;
-    T dhL = -g * hL * d.fqn_m, dhR = -g * hR * d.fqn_p;
+    T dhL = -ghL * d.fqn_m, dhR = -ghR * d.fqn_p;
     T dFL[3] = {0, 0, 0}, dFR[3] = {0, 0, 0}, dUL[3] = {0, 0, 0}, dUR[3] = {0, 0, 0};
     T dsL = 0, dsR = 0;
     if (regime == 0) {
@@ -267,19 +268,19 @@ SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceI
         dunL += dsR;
         dcL += dsR;
     }
-    dhL += dcL * half * g * rcL;  // dc/dh = g / (2 c)
-    dhR += dcR * half * g * rcR;
+    dhL += dcL * hg * rcL;  // dc/dh = g / (2 c)
+    dhR += dcR * hg * rcR;
     // physical fluxes FL = (qnL, qnL unL + g/2 hL^2, qnL utL); U = (h, qn, qt)
     const T dqnL = dFL[0] + dFL[1] * unL + dFL[2] * utL + dUL[1];
     const T dqtL = dUL[2];
     dunL += dFL[1] * qnL;
     T dutL = dFL[2] * qnL;
-    dhL += dFL[1] * g * hL + dUL[0];
+    dhL += dFL[1] * ghL + dUL[0];
     const T dqnR = dFR[0] + dFR[1] * unR + dFR[2] * utR + dUR[1];
     const T dqtR = dUR[2];
     dunR += dFR[1] * qnR;
     T dutR = dFR[2] * qnR;
-    dhR += dFR[1] * g * hR + dUR[0];
+    dhR += dFR[1] * ghR + dUR[0];
     // unL = un_m (wet L), qnL = hL un_m, ...
     T dun_m = dqnL * hL + (wL ? dunL : T(0)), dut_m = dqtL * hL + (wL ? dutL : T(0));
     T dun_p = dqnR * hR + (wR ? dunR : T(0)), dut_p = dqtR * hR + (wR ? dutR : T(0));
