@@ -64,6 +64,10 @@ def parse():
     ap.add_argument("--adj-steps", type=int, default=200)
     ap.add_argument("--acc-n", type=int, default=2048)
     ap.add_argument("--acc-steps", type=int, default=500)
+    ap.add_argument("--snap-steps", type=int, default=30)
+    ap.add_argument("--snap-every", type=int, default=10)
+    ap.add_argument("--snap-dir", default="",
+                    help="directory for the snapshot form's files (default: a temporary one)")
     ap.add_argument("--seed", type=int, default=2026)
     return ap.parse_args()
 
@@ -371,6 +375,81 @@ def form_slabs(args, sw):
             "exchange": "2 rows x 3 fields per interface per stage, through host memory"}
 
 
+def form_snapshots(args, sw):
+    """NetCDF snapshots of the headline grid every snap_every steps, two ways: through the
+    device path (pack kernel + writer thread, overlapped with stepping) and the
+    reference's way (synchronous download of the ghosted state, then packing and writing
+    on the host, cuda_solver.hpp:211-219).  Reports ms per step of each against plain
+    stepping; the files are deleted afterwards."""
+    import shutil
+    import tempfile
+    n, K, every = args.n, args.snap_steps, args.snap_every
+    h, hu, hv, B = workload(n, args.seed)
+    root = tempfile.mkdtemp(prefix="swe_snap_", dir=args.snap_dir or None)
+    out = {"grid": [n, n], "steps": K, "save_every": every, "records": K // every + 1,
+           "record_bytes": 3 * n * n * 8 + 8, "dir_fs": _fs_type(root)}
+    try:
+        with sw.Solver(n, n, bc="transmissive") as s:
+            s.upload(h, hu, hv, B)
+            s.step(1)
+            ms = {}
+            for mode in ("none", "device", "host"):
+                s.upload(h, hu, hv)
+                s.time = 0.0
+                path = os.path.join(root, f"{mode}.nc")
+                w = None if mode == "none" else sw.output.NetCDFWriter(path, s, save_every=every)
+                if w:
+                    w.write_bathymetry(B)
+                t0 = time.perf_counter()
+                for k in range(K + 1):
+                    if w and k % every == 0:
+                        if mode == "device":
+                            w.write_snapshot(s, s.time)
+                        else:
+                            w.write_snapshot(s.download(), s.time)
+                    if k < K:
+                        s.step(1)
+                t_loop = time.perf_counter() - t0
+                if w:
+                    w.flush()
+                t_all = time.perf_counter() - t0
+                ms[mode] = {"ms_per_step_loop": t_loop * 1e3 / K, "ms_per_step_with_flush": t_all * 1e3 / K}
+                if mode == "device":
+                    c, wr, nb = w.stats()
+                    ms[mode].update({"writer_copy_s": c, "writer_write_s": wr, "writer_bytes": nb,
+                                     "file_write_gbs": nb / wr / 1e9 if wr > 0 else None})
+                if w:
+                    w.close()
+                    os.remove(path)
+            out.update(ms)
+            base = ms["none"]["ms_per_step_loop"]
+            for mode in ("device", "host"):
+                # the stall the stepping loop sees per record, and the wait for the last
+                # records to reach the file after the loop
+                out[mode]["stall_ms_per_record"] = (
+                    (ms[mode]["ms_per_step_loop"] - base) * K / out["records"])
+                out[mode]["final_flush_ms"] = (
+                    (ms[mode]["ms_per_step_with_flush"] - ms[mode]["ms_per_step_loop"]) * K)
+    finally:
+        shutil.rmtree(root, ignore_errors=True)
+    return out
+
+
+def _fs_type(path):
+    """Filesystem type of path's mount (from /proc/mounts), for the record."""
+    try:
+        best, fs = "", "unknown"
+        real = os.path.realpath(path)
+        with open("/proc/mounts") as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) > 2 and real.startswith(parts[1]) and len(parts[1]) > len(best):
+                    best, fs = parts[1], parts[2]
+        return fs
+    except OSError:
+        return "unknown"
+
+
 def run_forms(args, sw, fp64_gcups):
     forms = {}
     wanted = set(args.forms.split(","))
@@ -378,7 +457,8 @@ def run_forms(args, sw, fp64_gcups):
                      ("ensemble", lambda: form_ensemble(args, sw)),
                      ("adjoint", lambda: form_adjoint(args, sw)),
                      ("sanity", lambda: form_sanity(args, sw)),
-                     ("slabs", lambda: form_slabs(args, sw))):
+                     ("slabs", lambda: form_slabs(args, sw)),
+                     ("snapshots", lambda: form_snapshots(args, sw))):
         if name not in wanted:
             continue
         try:

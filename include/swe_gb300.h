@@ -37,7 +37,9 @@ typedef enum swe_status {
     SWE_ERR_CFL = 4,         /* fixed dt above the CFL limit (HPC_solver.hpp:142-145) */
     SWE_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
     SWE_ERR_NO_DEVICE = 6,   /* no usable CUDA device */
-    SWE_ERR_UNSUPPORTED = 7  /* option not available in this build */
+    SWE_ERR_UNSUPPORTED = 7, /* option not available in this build */
+    SWE_ERR_IO = 8           /* an output file could not be created or written (the
+                                reference's netCDF::exceptions, netCDF_writer.cpp:20) */
 } swe_status;
 
 typedef enum swe_bc {
@@ -267,6 +269,101 @@ int swe_ens_get_schedule(const swe_ens *ens, int *shape, int *grid, int *total_t
 int swe_ens_tune(swe_ens *ens, int steps, double *best_ms);
 
 const char *swe_ens_last_error(const swe_ens *ens);
+
+/* ---- Snapshot output (NetCDF) ---------------------------------------------------------
+ * Replaces NetCDFWriter (include/io/netCDF_writer.hpp:12-55, netCDF_writer.cpp:10-149):
+ * the same data model - dimensions time (unlimited), x = Nx, y = Ny; double variables
+ * time(time), x(x), y(y), h, hu, hv (time, x, y) and B (x, y); "units" attributes on x,
+ * y, h, B and time when their unit is non-empty; the global int save_every; and, set by
+ * the first swe_snapshot_metadata call, the global dt, backend, riemann_solver,
+ * reconstruction, time_integrator, boundary_condition and bathymetry.  Cell centres are
+ * x = (i + 0.5) dx, y = (j + 0.5) dy (include/core/grid.hpp:22-23); fields hold the
+ * interior only, x slow and y contiguous (pack_interior_into, netCDF_writer.cpp:73-83).
+ *
+ * The file is written in the netCDF classic encoding (CDF-2, or CDF-5 when a variable
+ * reaches 4 GiB), which netCDF readers open like the reference's netCDF-4 files; no
+ * netCDF or HDF5 library is used.
+ *
+ * swe_snapshot_write takes the state from a context's device memory without stopping
+ * it: a kernel on the context's stream packs U^n's interior (byte-swapped to the file's
+ * big-endian order) into one of two device staging buffers, and a writer thread copies
+ * it to pinned host memory on its own stream, in chunks, and writes the record while
+ * the context keeps stepping.  A write blocks only while both staging buffers are
+ * still being written out. */
+typedef struct swe_snapshot swe_snapshot; /* opaque */
+
+typedef struct swe_snapshot_params {
+    int Nx, Ny;           /* interior cells */
+    double dx, dy;        /* cell sizes (Lx / Nx, Ly / Ny) */
+    const char *unit_x;   /* mesh.spatial_unit_x; NULL or "": no attribute */
+    const char *unit_y;   /* mesh.spatial_unit_y */
+    const char *unit_h;   /* mesh.spatial_unit_h (h and B) */
+    const char *unit_time;/* time.time_unit */
+    int save_every;       /* time.save_every, stored as a global attribute */
+    int format;           /* 0: CDF-2 when every variable fits it, else CDF-5; 2 or 5 */
+} swe_snapshot_params;
+
+/* Creates (replaces) the file, making missing directories, and writes the coordinates
+ * (the NetCDFWriter constructor, netCDF_writer.cpp:10-27). */
+int swe_snapshot_open(const char *path, const swe_snapshot_params *p, swe_snapshot **out);
+
+/* Writes B's interior from a ghosted host array, once (write_bathymetry, :85-98). */
+int swe_snapshot_bathymetry(swe_snapshot *s, const double *B);
+
+/* The run metadata write_snapshot attaches once (:100-133): dt unless NaN, and each
+ * string unless NULL or empty.  Applied only by the first call that carries dt or one of
+ * the strings after backend, as in the reference; later calls are ignored. */
+int swe_snapshot_metadata(swe_snapshot *s, double dt, const char *backend,
+                          const char *riemann_solver, const char *reconstruction,
+                          const char *time_integrator, const char *boundary_condition,
+                          const char *bathymetry);
+
+/* Appends one record from ghosted host arrays, synchronously (write_snapshot, :135-149),
+ * after every pending device record. */
+int swe_snapshot_write_host(swe_snapshot *s, double time, const double *h, const double *hu,
+                            const double *hv);
+
+/* Appends one record of ctx's current state (FP64 as stored; FP32-mixed as
+ * swe_download converts it) asynchronously; ctx must match the file's Nx and Ny. */
+int swe_snapshot_write(swe_snapshot *s, swe_ctx *ctx, double time);
+
+/* Waits until every record is on disk (in the file); returns the first write error. */
+int swe_snapshot_flush(swe_snapshot *s);
+
+/* Records appended so far (written or pending). */
+long long swe_snapshot_records(const swe_snapshot *s);
+
+/* Seconds the writer thread spent in device-to-host copies and file writes, and the
+ * bytes it wrote, over all device records so far. */
+int swe_snapshot_stats(const swe_snapshot *s, double *copy_s, double *write_s,
+                       long long *bytes);
+
+/* Flushes and closes the file; the object stays valid for swe_snapshot_last_error. */
+int swe_snapshot_close(swe_snapshot *s);
+void swe_snapshot_destroy(swe_snapshot *s); /* closes if open, frees; NULL is ignored */
+const char *swe_snapshot_last_error(const swe_snapshot *s);
+
+/* ---- Sanity-check records (NetCDF) ----------------------------------------------------
+ * Replaces SanityCheckNetCDFWriter (include/io/sanity_checks_netdcdf_writer.hpp,
+ * sanity_checks_netcdf_writer.cpp:6-71): dimension record (unlimited); variables
+ * step (uint64), time, mass_rel_err, h_min (double) with the reference's long_name and
+ * units attributes; globals save_every, dt, backend, riemann_solver, reconstruction,
+ * time_integrator, boundary_condition, bathymetry, mass_conservation_enabled = 1 and
+ * positivity_enabled = 1.  CDF-5 (the encoding that has uint64).  Pairs with
+ * swe_sanity, which computes the mass and h_min on the device. */
+typedef struct swe_sanity_log swe_sanity_log; /* opaque */
+
+int swe_sanity_log_open(const char *path, const char *time_unit, const char *h_unit,
+                        int save_every, double dt, const char *backend,
+                        const char *riemann_solver, const char *reconstruction,
+                        const char *time_integrator, const char *boundary_condition,
+                        const char *bathymetry, swe_sanity_log **out);
+/* One record (SanityCheckNetCDFWriter::write, :61-71). */
+int swe_sanity_log_write(swe_sanity_log *l, unsigned long long step, double time,
+                         double rel_err, double h_min);
+int swe_sanity_log_close(swe_sanity_log *l);
+void swe_sanity_log_destroy(swe_sanity_log *l);
+const char *swe_sanity_log_last_error(const swe_sanity_log *l);
 
 /* ---- Self-test (no counterpart in the reference) ------------------------------------
  * The FP64 kernels compute double division, square root and part of the multiplications

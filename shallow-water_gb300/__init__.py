@@ -12,5 +12,6 @@ from .solver import Solver, SweError  # noqa: F401
 from .ensemble import Ensemble  # noqa: F401
 from . import adjoint  # noqa: F401
 from . import slabs  # noqa: F401
+from . import output  # noqa: F401
 
-__all__ = ["Solver", "SweError", "Ensemble", "adjoint", "slabs", "problems", "lib"]
+__all__ = ["Solver", "SweError", "Ensemble", "adjoint", "slabs", "output", "problems", "lib"]

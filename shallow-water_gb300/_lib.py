@@ -19,6 +19,7 @@ SWE_ERR_CFL = 4
 SWE_ERR_TIMEOUT = 5
 SWE_ERR_NO_DEVICE = 6
 SWE_ERR_UNSUPPORTED = 7
+SWE_ERR_IO = 8
 
 SWE_BC_REFLECTING = 0
 SWE_BC_TRANSMISSIVE = 1
@@ -35,6 +36,11 @@ EXPORTS = (
     "swe_ens_set_schedule", "swe_ens_get_schedule", "swe_ens_tune", "swe_ens_last_error",
     "swe_totals_noalloc", "swe_adjoint_gauge", "swe_selftest_soft_f64", "swe_stage",
     "swe_halo", "swe_sanity",
+    "swe_snapshot_open", "swe_snapshot_bathymetry", "swe_snapshot_metadata",
+    "swe_snapshot_write_host", "swe_snapshot_write", "swe_snapshot_flush",
+    "swe_snapshot_records", "swe_snapshot_stats", "swe_snapshot_close", "swe_snapshot_destroy",
+    "swe_snapshot_last_error", "swe_sanity_log_open", "swe_sanity_log_write",
+    "swe_sanity_log_close", "swe_sanity_log_destroy", "swe_sanity_log_last_error",
 )
 TOTALS_NOALLOC_MAX_BLOCKS = 1024
 ADJ_TAPE_ALL = -1  # n_snapshots value of swe_adjoint_gauge's tape mode
@@ -59,6 +65,21 @@ class SweParams(ctypes.Structure):
         ("reserved", ctypes.c_int),
         ("dx", ctypes.c_double),
         ("dy", ctypes.c_double),
+    ]
+
+
+class SnapshotParams(ctypes.Structure):
+    _fields_ = [
+        ("Nx", ctypes.c_int),
+        ("Ny", ctypes.c_int),
+        ("dx", ctypes.c_double),
+        ("dy", ctypes.c_double),
+        ("unit_x", ctypes.c_char_p),
+        ("unit_y", ctypes.c_char_p),
+        ("unit_h", ctypes.c_char_p),
+        ("unit_time", ctypes.c_char_p),
+        ("save_every", ctypes.c_int),
+        ("format", ctypes.c_int),
     ]
 
 
@@ -148,5 +169,40 @@ def lib(path: str = LIB_PATH):
     L.swe_selftest_soft_f64.restype = ctypes.c_int
     L.swe_ens_last_error.argtypes = [vp]
     L.swe_ens_last_error.restype = ctypes.c_char_p
+    cp = ctypes.c_char_p
+    L.swe_snapshot_open.argtypes = [cp, ctypes.POINTER(SnapshotParams), ctypes.POINTER(vp)]
+    L.swe_snapshot_open.restype = ctypes.c_int
+    L.swe_snapshot_bathymetry.argtypes = [vp, dp]
+    L.swe_snapshot_bathymetry.restype = ctypes.c_int
+    L.swe_snapshot_metadata.argtypes = [vp, ctypes.c_double, cp, cp, cp, cp, cp, cp]
+    L.swe_snapshot_metadata.restype = ctypes.c_int
+    L.swe_snapshot_write_host.argtypes = [vp, ctypes.c_double, dp, dp, dp]
+    L.swe_snapshot_write_host.restype = ctypes.c_int
+    L.swe_snapshot_write.argtypes = [vp, vp, ctypes.c_double]
+    L.swe_snapshot_write.restype = ctypes.c_int
+    L.swe_snapshot_flush.argtypes = [vp]
+    L.swe_snapshot_flush.restype = ctypes.c_int
+    L.swe_snapshot_records.argtypes = [vp]
+    L.swe_snapshot_records.restype = ctypes.c_longlong
+    L.swe_snapshot_stats.argtypes = [vp, dp, dp, ctypes.POINTER(ctypes.c_longlong)]
+    L.swe_snapshot_stats.restype = ctypes.c_int
+    L.swe_snapshot_close.argtypes = [vp]
+    L.swe_snapshot_close.restype = ctypes.c_int
+    L.swe_snapshot_destroy.argtypes = [vp]
+    L.swe_snapshot_destroy.restype = None
+    L.swe_snapshot_last_error.argtypes = [vp]
+    L.swe_snapshot_last_error.restype = cp
+    L.swe_sanity_log_open.argtypes = [cp, cp, cp, ctypes.c_int, ctypes.c_double, cp, cp, cp,
+                                      cp, cp, cp, ctypes.POINTER(vp)]
+    L.swe_sanity_log_open.restype = ctypes.c_int
+    L.swe_sanity_log_write.argtypes = [vp, ctypes.c_ulonglong, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_double]
+    L.swe_sanity_log_write.restype = ctypes.c_int
+    L.swe_sanity_log_close.argtypes = [vp]
+    L.swe_sanity_log_close.restype = ctypes.c_int
+    L.swe_sanity_log_destroy.argtypes = [vp]
+    L.swe_sanity_log_destroy.restype = None
+    L.swe_sanity_log_last_error.argtypes = [vp]
+    L.swe_sanity_log_last_error.restype = cp
     _lib = L
     return L

@@ -26,6 +26,8 @@ UNITS = {
     "swe_ensemble.cu": [],
     "swe_adjoint.cu": [],
     "swe_selftest.cu": [],
+    "swe_output.cu": [],
+    "swe_ncfile.cpp": [],
     "swe_api.cu": [],
 }
 
@@ -52,7 +54,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
     cc = nvcc()
     for src, extra in UNITS.items():
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
             cmd = [cc, *ARCH, *COMMON, *extra, "-c", s, "-o", o]

@@ -193,6 +193,7 @@ const char *swe_status_string(int s) {
         case SWE_ERR_TIMEOUT: return "device wait timed out";
         case SWE_ERR_NO_DEVICE: return "no CUDA device";
         case SWE_ERR_UNSUPPORTED: return "unsupported option";
+        case SWE_ERR_IO: return "output file error";
         default: return "unknown status";
     }
 }

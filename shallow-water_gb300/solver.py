@@ -174,10 +174,13 @@ class Solver:
 
     # -- FastHLLMUSCLBathySolver::run (HPC_solver.hpp:130-200) -----------------------
     def run(self, end_time: float, time_steps: int, save_every: int | None = None,
-            on_snapshot=None):
+            on_snapshot=None, writer=None, bathymetry_name: str = ""):
         """Fixed-dt run as the reference: dt = end_time / time_steps, the CFL guard once
         before stepping, a snapshot (time, h, hu, hv) at t = 0 and every save_every
-        steps and at the end, passed to ``on_snapshot``."""
+        steps and at the end, passed to ``on_snapshot`` and/or appended to ``writer``
+        (an ``output.NetCDFWriter``; the first record carries the run metadata as
+        cuda_solver.hpp:178-183 writes it, and records are written from the device while
+        the run continues)."""
         dt = end_time / float(time_steps)
         dt_stable = self.stable_dt()
         if dt > dt_stable:
@@ -186,11 +189,20 @@ class Solver:
         save_every = save_every or time_steps
         if on_snapshot:
             on_snapshot(0, self.time, *self.download())
+        if writer is not None:
+            bc = "Reflecting Walls" if self.params.bc == L.SWE_BC_REFLECTING else "Transmissive"
+            writer.write_snapshot(self, self.time, dt, "GB300", "HLL", "MUSCL", "SSPRK3", bc,
+                                  bathymetry_name)
         done = 0
         while done < time_steps:
             n = min(save_every - done % save_every, time_steps - done)
             self.step(n, dt)
             done += n
-            if on_snapshot and (done % save_every == 0 or done == time_steps):
-                on_snapshot(done, self.time, *self.download())
+            if done % save_every == 0 or done == time_steps:
+                if writer is not None:
+                    writer.write_snapshot(self, self.time)
+                if on_snapshot:
+                    on_snapshot(done, self.time, *self.download())
+        if writer is not None:
+            writer.flush()
         return self.time
