@@ -16,7 +16,18 @@
 //     fixed dt = end_time / time_steps, a snapshot and the sanity checks every save_every
 //     steps and at the end, the ETA line, a timing summary.
 //   * non-copyable, RAII device memory, errors as std::runtime_error.
+//
+// With SWE_GB300_NATIVE_OUTPUT=1 the snapshots go through the library's own NetCDF
+// writer (swe_snapshot_*) instead of the reference's NetCDFWriter: each record is packed
+// on the GPU and written by a background thread while the run continues, so an output
+// step no longer stops the solver for a download.  The file holds the same dimensions,
+// variables, attributes and values (classic encoding instead of netCDF-4).  The state
+// is then downloaded only for the sanity checks, when any are configured.
 #pragma once
+
+#ifndef SWE_GB300_NATIVE_OUTPUT
+#define SWE_GB300_NATIVE_OUTPUT 0
+#endif
 
 #include "configs/config.hpp"
 #include "configs/parse_config_helper.hpp"
@@ -52,8 +63,10 @@ class FastHLLMUSCLBathyGB300Solver {
                    static_cast<std::size_t>(grid_.Ny_total())),
           h_(n_total_), hu_(n_total_), hv_(n_total_), B_(n_total_), io_state_(grid_),
           io_bathy_(grid_.Nx_total(), grid_.Ny_total()),
+#if !SWE_GB300_NATIVE_OUTPUT
           writer_(cfg.output.path.string(), grid_, cfg.mesh.spatial_unit_x, cfg.mesh.spatial_unit_y,
                   cfg.mesh.spatial_unit_h, cfg.time.time_unit, cfg.time.save_every),
+#endif
           sanity_checks_(make_sanity_checks(cfg)), sanity_writer_(make_sanity_writer(cfg, dt_)) {
         if (grid_.nG() != 2) {
             throw std::runtime_error("FastHLLMUSCLBathyGB300Solver requires nG == 2 for MUSCL.");
@@ -77,7 +90,11 @@ class FastHLLMUSCLBathyGB300Solver {
         scalar_wall_ghosts(B_tmp.data());
         std::copy(B_tmp.data(), B_tmp.data() + B_tmp.size(), B_.begin());
         std::copy(B_.begin(), B_.end(), io_bathy_.data());
+#if SWE_GB300_NATIVE_OUTPUT
+        open_native_output();
+#else
         writer_.write_bathymetry(io_bathy_);
+#endif
 
         State U_tmp(grid_);
         apply_initial_condition(cfg_, grid_, U_tmp);
@@ -96,7 +113,12 @@ class FastHLLMUSCLBathyGB300Solver {
         }
     }
 
-    ~FastHLLMUSCLBathyGB300Solver() { swe_destroy(ctx_); }
+    ~FastHLLMUSCLBathyGB300Solver() {
+#if SWE_GB300_NATIVE_OUTPUT
+        swe_snapshot_destroy(snap_);
+#endif
+        swe_destroy(ctx_);
+    }
 
     FastHLLMUSCLBathyGB300Solver(const FastHLLMUSCLBathyGB300Solver &) = delete;
     FastHLLMUSCLBathyGB300Solver &operator=(const FastHLLMUSCLBathyGB300Solver &) = delete;
@@ -148,6 +170,13 @@ class FastHLLMUSCLBathyGB300Solver {
                 sanity(time, done);
             }
         }
+#if SWE_GB300_NATIVE_OUTPUT
+        {
+            const auto start = Clock::now();
+            check_snap(swe_snapshot_close(snap_), "swe_snapshot_close");
+            output_s_ += seconds_since(start);
+        }
+#endif
         print_summary(done);
     }
 
@@ -188,6 +217,50 @@ class FastHLLMUSCLBathyGB300Solver {
         std::copy(hv_.begin(), hv_.end(), io_state_.hv().data());
     }
 
+#if SWE_GB300_NATIVE_OUTPUT
+    void check_snap(int status, const char *what) const {
+        if (status == SWE_OK) return;
+        throw std::runtime_error(std::string("GB300 backend: ") + what + ": " +
+                                 swe_status_string(status) + " (" +
+                                 swe_snapshot_last_error(snap_) + ")");
+    }
+
+    // The NetCDFWriter constructor and write_bathymetry (netCDF_writer.cpp:10-27,85-98).
+    void open_native_output() {
+        swe_snapshot_params sp{};
+        sp.Nx = grid_.Nx();
+        sp.Ny = grid_.Ny();
+        sp.dx = grid_.dx();
+        sp.dy = grid_.dy();
+        sp.unit_x = cfg_.mesh.spatial_unit_x.c_str();
+        sp.unit_y = cfg_.mesh.spatial_unit_y.c_str();
+        sp.unit_h = cfg_.mesh.spatial_unit_h.c_str();
+        sp.unit_time = cfg_.time.time_unit.c_str();
+        sp.save_every = cfg_.time.save_every;
+        const std::string path = cfg_.output.path.string();
+        const int st = swe_snapshot_open(path.c_str(), &sp, &snap_);
+        if (st != SWE_OK)
+            throw std::runtime_error("GB300 backend: cannot create " + path + ": " +
+                                     swe_status_string(st));
+        check_snap(swe_snapshot_bathymetry(snap_, B_.data()), "swe_snapshot_bathymetry");
+    }
+
+    // The device state goes to the file from the GPU; the host copy is refreshed only when
+    // a sanity check needs it.
+    void snapshot(double time, bool first) {
+        const auto start = Clock::now();
+        if (first) {
+            const std::string backend = backend_name_from_cfg(cfg_);
+            const std::string bathy = bathymetry_name_from_cfg(cfg_);
+            check_snap(swe_snapshot_metadata(snap_, dt_, backend.c_str(), "HLL", "MUSCL",
+                                             "SSPRK3", "Reflecting Walls", bathy.c_str()),
+                       "swe_snapshot_metadata");
+        }
+        check_snap(swe_snapshot_write(snap_, ctx_, time), "swe_snapshot_write");
+        host_stale_ = !first;
+        output_s_ += seconds_since(start);
+    }
+#else
     void snapshot(double time, bool first) {
         const auto start = Clock::now();
         if (!first) check(swe_download(ctx_, h_.data(), hu_.data(), hv_.data()), "swe_download");
@@ -201,10 +274,15 @@ class FastHLLMUSCLBathyGB300Solver {
         }
         output_s_ += seconds_since(start);
     }
+#endif
 
     void sanity(double time, std::size_t step) {
         if (sanity_checks_.empty()) return;
         const auto start = Clock::now();
+        if (host_stale_) {
+            check(swe_download(ctx_, h_.data(), hu_.data(), hv_.data()), "swe_download");
+            host_stale_ = false;
+        }
         fill_io_state();
         for (auto &c : sanity_checks_) c->evaluate(io_state_, grid_, time, step, sanity_writer_.get());
         sanity_s_ += seconds_since(start);
@@ -250,7 +328,12 @@ class FastHLLMUSCLBathyGB300Solver {
     std::vector<double> h_, hu_, hv_, B_;
     State io_state_;
     Array2D io_bathy_;
+#if SWE_GB300_NATIVE_OUTPUT
+    swe_snapshot *snap_ = nullptr;
+#else
     NetCDFWriter writer_;
+#endif
+    bool host_stale_ = false;  // h_, hu_, hv_ behind the device state
     std::vector<std::unique_ptr<SanityCheck>> sanity_checks_;
     std::unique_ptr<SanityCheckNetCDFWriter> sanity_writer_;
     swe_ctx *ctx_ = nullptr;

@@ -78,24 +78,33 @@ path = "output/simulation.nc"
 """
 
 
-@pytest.fixture(scope="module")
-def patched_app(tmp_path_factory, sw):
-    from importlib import import_module
-    integ = import_module("shallow-water_gb300.integration")
-    tree = tmp_path_factory.mktemp("ref") / "shallow-water"
-    shutil.copytree(REF, tree, ignore=shutil.ignore_patterns("docs", "python", ".git"))
-    integ.patch_reference_tree(str(tree))
+def build_app(tree, name, extra=()):
     libdir = os.path.join(ROOT, "shallow-water_gb300")
-    exe = tree / "swe_solver_gb300"
+    exe = tree / name
     cmd = ["g++", "-std=c++17", "-O1", "-DUSE_OPENMP=0", "-DUSE_CUDA=0", "-DUSE_CUDA_4=0",
-           "-DUSE_GB300=1", "-include", "iostream", f"-I{tree}", f"-I{ROOT}/include",
+           "-DUSE_GB300=1", *extra, "-include", "iostream", f"-I{tree}", f"-I{ROOT}/include",
            f"-I{ROOT}/oracle/ref/stub", "-w",
            str(tree / "apps/main.cpp"), str(tree / "configs/simulation_config.cpp"),
            str(tree / "tests/sanity_checks/sanity_checks.cpp"),
            os.path.join(ROOT, "oracle/ref/netcdf_noop.cpp"),
            f"-L{libdir}", "-lswe_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)]
     subprocess.run(cmd, check=True, capture_output=True, text=True)
-    return tree, exe
+    return exe
+
+
+@pytest.fixture(scope="module")
+def patched_tree(tmp_path_factory, sw):
+    from importlib import import_module
+    integ = import_module("shallow-water_gb300.integration")
+    tree = tmp_path_factory.mktemp("ref") / "shallow-water"
+    shutil.copytree(REF, tree, ignore=shutil.ignore_patterns("docs", "python", ".git"))
+    integ.patch_reference_tree(str(tree))
+    return tree
+
+
+@pytest.fixture(scope="module")
+def patched_app(patched_tree):
+    return patched_tree, build_app(patched_tree, "swe_solver_gb300")
 
 
 def run_app(tree, exe, backend):
@@ -129,6 +138,21 @@ def test_gb300_backend_dispatches(patched_app):
     if torch.cuda.is_available():
         assert r.returncode == 0, r.stderr
         assert "GB300 fused-stage solver active" in r.stdout
+    else:
+        assert r.returncode != 0
+        assert "GB300 backend: swe_create: no CUDA device" in r.stderr
+
+
+def test_gb300_backend_with_native_output(patched_tree):
+    """The class built with SWE_GB300_NATIVE_OUTPUT=1 (snapshots through the library's
+    own NetCDF writer) compiles and dispatches the same way."""
+    exe = build_app(patched_tree, "swe_solver_gb300_native", ["-DSWE_GB300_NATIVE_OUTPUT=1"])
+    r = run_app(patched_tree, exe, "GB300")
+    import torch
+    if torch.cuda.is_available():
+        assert r.returncode == 0, r.stderr
+        out = patched_tree / "output" / "simulation.nc"
+        assert out.exists() and out.read_bytes()[:4] == b"CDF\x02"
     else:
         assert r.returncode != 0
         assert "GB300 backend: swe_create: no CUDA device" in r.stderr
