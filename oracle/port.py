@@ -70,6 +70,11 @@ def lib():
         L.swe_oracle_fill_ghosts.restype = None
         L.swe_oracle_fill_scalar_ghosts.argtypes = [gp, dp]
         L.swe_oracle_fill_scalar_ghosts.restype = None
+        i = ctypes.c_int
+        L.swe_oracle_modular_run.argtypes = [gp, i, i, i, i, ctypes.c_double, dp, dp, dp, dp, dp]
+        L.swe_oracle_modular_run.restype = ctypes.c_int
+        L.swe_oracle_modular_stable_dt.argtypes = [gp, dp, dp, dp, dp]
+        L.swe_oracle_modular_stable_dt.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -147,3 +152,27 @@ def fill_ghosts(p: _Grid, h, hu, hv):
 
 def fill_scalar_ghosts(p: _Grid, a):
     lib().swe_oracle_fill_scalar_ghosts(ctypes.byref(p), _p(a))
+
+
+RECON = {"PiecewiseConst": 0, "MUSCL": 1}
+RIEMANN = {"HLL": 0, "Rusanov": 1, "ROE": 2}
+
+
+def modular_run(p: _Grid, recon, riemann, bathy, h, hu, hv, B, steps, dt):
+    """SerialSolver<ReflectingWalls, recon, riemann, SSPRK3, bathymetry on/off> for
+    ``steps`` fixed-dt steps on copies; returns (h, hu, hv, t, status)."""
+    h, hu, hv = (np.array(a, dtype=np.float64, order="C", copy=True) for a in (h, hu, hv))
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    t = ctypes.c_double(0.0)
+    st = lib().swe_oracle_modular_run(ctypes.byref(p), RECON.get(recon, recon),
+                                      RIEMANN.get(riemann, riemann), int(bool(bathy)), steps, dt,
+                                      _p(h), _p(hu), _p(hv), _p(B), ctypes.byref(t))
+    return h, hu, hv, t.value, st
+
+
+def modular_stable_dt(p: _Grid, h, hu, hv):
+    """(dt, status) of the modular solver's CFL guard (time_utils.hpp:14-38)."""
+    out = ctypes.c_double(0.0)
+    st = lib().swe_oracle_modular_stable_dt(ctypes.byref(p), _p(h), _p(hu), _p(hv),
+                                            ctypes.byref(out))
+    return out.value, st

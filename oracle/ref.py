@@ -36,6 +36,10 @@ def lib(variant="g980665"):
         L.ref_stable_dt.restype = ctypes.c_double
         L.ref_gravity.argtypes = []
         L.ref_gravity.restype = ctypes.c_double
+        L.ref_modular_run.argtypes = [i, i, d, d, d, i, i, i, i, d, dp, dp, dp, dp]
+        L.ref_modular_run.restype = ctypes.c_int
+        L.ref_modular_stable_dt.argtypes = [i, i, d, d, d, dp, dp, dp, dp]
+        L.ref_modular_stable_dt.restype = ctypes.c_int
         _libs[variant] = L
     return _libs[variant]
 
@@ -62,3 +66,21 @@ def stable_dt(Nx, Ny, h, hu, hv, Lx=1.0, Ly=1.0, cfl=0.45, variant="g980665") ->
 
 def gravity(variant="g980665") -> float:
     return lib(variant).ref_gravity()
+
+
+def modular_run(Nx, Ny, recon, riemann, bathy, h, hu, hv, B, steps, dt, Lx=1.0, Ly=1.0,
+                cfl=0.45, variant="g980665"):
+    """The reference's SerialSolver on copies (recon 0/1, riemann 0/1/2 as
+    oracle.port.RECON / RIEMANN); returns (h, hu, hv, status)."""
+    h, hu, hv = (np.array(a, dtype=np.float64, order="C", copy=True) for a in (h, hu, hv))
+    B = np.ascontiguousarray(B, dtype=np.float64)
+    st = lib(variant).ref_modular_run(Nx, Ny, Lx, Ly, cfl, recon, riemann, int(bool(bathy)),
+                                      steps, dt, _p(h), _p(hu), _p(hv), _p(B))
+    return h, hu, hv, st
+
+
+def modular_stable_dt(Nx, Ny, h, hu, hv, Lx=1.0, Ly=1.0, cfl=0.45, variant="g980665"):
+    out = ctypes.c_double(0.0)
+    st = lib(variant).ref_modular_stable_dt(Nx, Ny, Lx, Ly, cfl, _p(h), _p(hu), _p(hv),
+                                            ctypes.byref(out))
+    return out.value, st

@@ -77,6 +77,28 @@ void swe_oracle_fill_ghosts(const swe_oracle_grid *p, double *h, double *hu, dou
  * HPC_solver.hpp:373-404), or zero-gradient copies for transmissive walls. */
 void swe_oracle_fill_scalar_ghosts(const swe_oracle_grid *p, double *a);
 
+/* ---- The modular solver (oracle/swe_modular.c) -------------------------------------
+ * SerialSolver<ReflectingWalls, Recon, Riemann, SSPRK3, Bathymetry>
+ * (include/backend/serial/serial_solver.hpp:140-291), restated for every
+ * reconstruction and Riemann solver it composes. */
+enum { SWE_ORACLE_RECON_PIECEWISE_CONST = 0, SWE_ORACLE_RECON_MUSCL = 1 };
+enum { SWE_ORACLE_RIEMANN_HLL = 0, SWE_ORACLE_RIEMANN_RUSANOV = 1, SWE_ORACLE_RIEMANN_ROE = 2 };
+
+/* `steps` fixed-dt steps in place on h, hu, hv (reflecting walls; ghosts refreshed on
+ * return).  bathy != 0: FluxAssemblyBathy, FiniteVolumeBathy and enforce_positivity (the
+ * Flat / GaussHill instantiations); 0: FluxAssembly and FiniteVolume (None).  B is read
+ * only when bathy != 0.  *t_inout accumulates time += dt.  Returns 0; 1 where the
+ * reference throws "non-finite state detected in positivity correction"; 2 where HLL
+ * throws "HLL could not provide dissipation speed."; -1 on allocation failure. */
+int swe_oracle_modular_run(const swe_oracle_grid *p, int recon, int riemann, int bathy,
+                           int steps, double dt, double *h, double *hu, double *hv,
+                           const double *B, double *t_inout);
+
+/* The modular solver's CFL guard, compute_stable_dt of time_utils.hpp:14-38.  Returns 0,
+ * or 1 where the reference throws on h < 0. */
+int swe_oracle_modular_stable_dt(const swe_oracle_grid *p, const double *h, const double *hu,
+                                 const double *hv, double *out);
+
 #ifdef __cplusplus
 }
 #endif

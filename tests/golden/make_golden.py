@@ -6,7 +6,7 @@ shallow-water_gb300/problems.py; they are stored in the fixtures (small cases) o
 pinned by their SHA-256 (the full 256^2 parity case), so the fixtures do not depend
 on the platform's exp().
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--modular-only]
 """
 from __future__ import annotations
 
@@ -75,8 +75,43 @@ def small_cases():
     return out
 
 
+def modular_cases():
+    """The modular SerialSolver (every reconstruction x Riemann solver, with and without
+    bathymetry) on a wet and a partly dry random state, 8 fixed-dt steps at half the
+    modular CFL limit; reflecting walls (the only ones it has)."""
+    from oracle import port
+    Nx, Ny, Lx, Ly = 20, 14, 1.1, 0.8
+    out = {}
+    for tag, dry in (("wet", 0.0), ("dry", 0.1)):
+        h, hu, hv, B = (np.array(a) for a in P.random_state(Nx, Ny, seed=17, dry_frac=dry))
+        p = port.grid(Nx, Ny, Lx, Ly)
+        port.fill_ghosts(p, h, hu, hv)
+        port.fill_scalar_ghosts(p, B)
+        m = h < 1e-7
+        hu[m] = 0.0
+        hv[m] = 0.0
+        dt_guard, st = ref.modular_stable_dt(Nx, Ny, h, hu, hv, Lx, Ly)
+        assert st == 0
+        dt = 0.5 * dt_guard
+        out[f"{tag}_h"], out[f"{tag}_hu"], out[f"{tag}_hv"], out[f"{tag}_B"] = h, hu, hv, B
+        out[f"{tag}_dt"] = np.array([dt, dt_guard])
+        for recon in (0, 1):
+            for riemann in (0, 1, 2):
+                for bathy in (0, 1):
+                    o = ref.modular_run(Nx, Ny, recon, riemann, bathy, h, hu, hv, B, 8, dt,
+                                        Lx, Ly)
+                    key = f"{tag}_r{recon}_s{riemann}_b{bathy}"
+                    out[key] = np.stack(o[:3])
+                    out[key + "_status"] = np.array([o[3]])
+    meta = dict(Nx=Nx, Ny=Ny, Lx=Lx, Ly=Ly, steps=8, cfl=0.45)
+    np.savez_compressed(os.path.join(HERE, "modular_20x14.npz"), meta=json.dumps(meta), **out)
+
+
 def main():
     assert ref.available() and ref.available("g981"), "build oracle/_ref first: make -C oracle ref"
+    if "--modular-only" in sys.argv:
+        modular_cases()
+        return
     meta = {"config0_g980665": case_config0("g980665"), "config0_g981": case_config0("g981")}
     with open(os.path.join(HERE, "config0_256.json"), "w") as f:
         json.dump(meta, f, indent=1)
@@ -84,6 +119,7 @@ def main():
         arrays = {k: v for k, v in c.items() if isinstance(v, np.ndarray)}
         scalars = {k: v for k, v in c.items() if not isinstance(v, np.ndarray)}
         np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(scalars), **arrays)
+    modular_cases()
     print("wrote", sorted(os.listdir(HERE)))
 
 
