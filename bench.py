@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the FP32-mixed, ensemble and adjoint measurements")
-    ap.add_argument("--forms", default="fp32_mixed,ensemble,adjoint,sanity,slabs",
+    ap.add_argument("--forms", default="fp32_mixed,ensemble,adjoint,sanity,slabs,modular",
                     help="comma list of the extra forms to measure")
     ap.add_argument("--fp32-n", type=int, default=16384)
     ap.add_argument("--ens-count", type=int, default=512)
@@ -435,6 +435,43 @@ def form_snapshots(args, sw):
     return out
 
 
+def form_modular(args, sw):
+    """The modular scheme (SerialSolver's arithmetic, every reconstruction x Riemann
+    solver, with and without bathymetry) on a 4096^2 wet state over seeded bathymetry:
+    GCUPS per combination, fixed dt at half the Serial backend's CFL guard."""
+    n, K = 4096, 3
+    P = importlib.import_module("shallow-water_gb300.problems")
+    B, _ = P.gaussian_sum_bathymetry(n, n, n=16, seed=args.seed)
+    h, hu, hv = P.dam_break(B)
+    out = {"grid": [n, n], "steps": K, "bytes_per_cell_update": 216, "gcups": {}}
+    for recon in ("PiecewiseConst", "MUSCL"):
+        for riemann in ("HLL", "Rusanov", "ROE"):
+            for bathy in (True, False):
+                with sw.Solver(n, n, scheme="modular", reconstruction=recon, riemann=riemann,
+                               bathymetry=bathy) as s:
+                    s.upload(h, hu, hv, B)
+                    dt = 0.5 * s.stable_dt()
+                    s.step(1, dt)
+                    s.step(K, dt)
+                    ms = s.last_step_ms()
+                key = f"{recon}+{riemann}+{'bathymetry' if bathy else 'none'}"
+                out["gcups"][key] = n * n * K / (ms * 1e-3) / 1e9
+    if not args.no_cpu_baseline:
+        # the oracle's C restatement of SerialSolver, one core, MUSCL + HLL + bathymetry
+        from oracle import port
+        m = 512
+        Bm, _ = P.gaussian_sum_bathymetry(m, m, n=16, seed=args.seed)
+        hm, hum, hvm = P.dam_break(Bm)
+        g = port.grid(m, m)
+        dtm = 0.5 * port.modular_stable_dt(g, hm, hum, hvm)[0]
+        t0 = time.perf_counter()
+        port.modular_run(g, 1, 0, 1, hm, hum, hvm, Bm, 2, dtm)
+        secs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": m * m * 2 / secs / 1e9, "unit": "GCUPS", "cores": 1,
+                               "kind": "port", "sample": "512^2, 2 steps, MUSCL+HLL+bathymetry"}
+    return out
+
+
 def _fs_type(path):
     """Filesystem type of path's mount (from /proc/mounts), for the record."""
     try:
@@ -458,7 +495,8 @@ def run_forms(args, sw, fp64_gcups):
                      ("adjoint", lambda: form_adjoint(args, sw)),
                      ("sanity", lambda: form_sanity(args, sw)),
                      ("slabs", lambda: form_slabs(args, sw)),
-                     ("snapshots", lambda: form_snapshots(args, sw))):
+                     ("snapshots", lambda: form_snapshots(args, sw)),
+                     ("modular", lambda: form_modular(args, sw))):
         if name not in wanted:
             continue
         try:

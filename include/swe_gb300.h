@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define SWE_GB300_ABI_VERSION 1
+#define SWE_GB300_ABI_VERSION 2
 
 typedef enum swe_status {
     SWE_OK = 0,
@@ -52,6 +52,25 @@ typedef enum swe_precision {
     SWE_PRECISION_FP32_MIXED = 1  /* FP32 bulk, FP64 where balance/conservation need it */
 } swe_precision;
 
+typedef enum swe_scheme {
+    SWE_SCHEME_FUSED = 0,    /* FastHLLMUSCLBathySolver's arithmetic (HPC_solver.hpp, the
+                                OptimizedSerial / OpenMP / CUDA backends): the drop-in */
+    SWE_SCHEME_MODULAR = 1   /* SerialSolver<ReflectingWalls, reconstruction, riemann,
+                                SSPRK3, bathymetry>'s arithmetic (serial_solver.hpp, the
+                                Serial backend); FP64, reflecting walls, fixed dt */
+} swe_scheme;
+
+typedef enum swe_reconstruction {
+    SWE_RECON_PIECEWISE_CONST = 0, /* reconstruction/piecewise_const.hpp */
+    SWE_RECON_MUSCL = 1            /* reconstruction/muscl.hpp */
+} swe_reconstruction;
+
+typedef enum swe_riemann {
+    SWE_RIEMANN_HLL = 0,     /* riemann/HLL.hpp */
+    SWE_RIEMANN_RUSANOV = 1, /* riemann/rusanov.hpp */
+    SWE_RIEMANN_ROE = 2      /* riemann/ROE.hpp */
+} swe_riemann;
+
 typedef struct swe_params {
     int Nx, Ny;       /* interior cells, each >= 2 (mesh.Nx/Ny, configs/config.hpp:21-30) */
     int nG;           /* ghost layers; must be 2 (MUSCL, solver_assembly.hpp validate_config) */
@@ -67,11 +86,18 @@ typedef struct swe_params {
     int reserved;     /* must be zero */
     double dx, dy;    /* > 0: cell sizes used instead of Lx / Nx and Ly / Ny, so that an
                          x-slab keeps its grid's dx exactly; 0: derived */
+    int scheme;       /* swe_scheme; the three fields below apply to SWE_SCHEME_MODULAR */
+    int reconstruction; /* swe_reconstruction */
+    int riemann;      /* swe_riemann */
+    int bathymetry;   /* nonzero: FluxAssemblyBathy + FiniteVolumeBathy + positivity (the
+                         Flat / GaussHill instantiations); 0: FluxAssembly + FiniteVolume
+                         (None), B unused */
 } swe_params;
 
 typedef struct swe_ctx swe_ctx; /* opaque */
 
 /* Fills *p with defaults: nG = 2, L = 1, g = 9.80665, cfl = 0.45, reflecting, FP64,
+ * the fused scheme (modular fields: MUSCL, HLL, bathymetry on),
  * device 0.  Nx and Ny must still be set. */
 void swe_params_default(swe_params *p);
 
@@ -102,7 +128,12 @@ int swe_download(swe_ctx *ctx, double *h, double *hu, double *hv);
  * reduced on the device inside the last stage of the previous step.  If t_inout is
  * not NULL, *t_inout += dt for every step, in step order (HPC_solver.hpp:170).
  * Returns SWE_ERR_NONFINITE if any stage produced a non-finite interior value (the
- * state is then undefined), checked once per call. */
+ * state is then undefined), checked once per call.
+ * SWE_SCHEME_MODULAR: the step loop of SerialSolver::run (serial_solver.hpp:183-244 with
+ * bathymetry, 247-306 without); dt must be > 0 (the Serial backend has no adaptive dt),
+ * else SWE_ERR_UNSUPPORTED.  SWE_ERR_NONFINITE then also reports where the reference
+ * throws: a non-finite state after positivity (with bathymetry) or an HLL interface
+ * without a dissipation speed (swe_last_error names which). */
 int swe_step(swe_ctx *ctx, int n_steps, double dt, double *t_inout);
 
 /* ---- Slabs (x-decomposition over several GPUs) ---------------------------------------
@@ -134,7 +165,9 @@ int swe_max_wave_speed(swe_ctx *ctx, double *out);
 
 /* compute_stable_dt of the current state (HPC_kernels.hpp:281-298): 1e100 when the
  * max wave speed is <= 1e-8.  The reference's CFL guard (HPC_solver.hpp:134-145) is
- * this value compared with the fixed dt. */
+ * this value compared with the fixed dt.  SWE_SCHEME_MODULAR: the Serial backend's
+ * guard instead, min over cells of cfl / ((|u| + c) / dx + (|v| + c) / dy)
+ * (solver_assembly/time_utils.hpp:14-38); SWE_ERR_BAD_ARG where it throws (h < 0). */
 int swe_stable_dt(swe_ctx *ctx, double *out);
 
 /* Totals of the current state over the interior, times dx * dy: mass = sum h,

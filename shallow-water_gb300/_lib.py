@@ -25,6 +25,10 @@ SWE_BC_REFLECTING = 0
 SWE_BC_TRANSMISSIVE = 1
 SWE_PRECISION_FP64 = 0
 SWE_PRECISION_FP32_MIXED = 1
+SWE_SCHEME_FUSED = 0
+SWE_SCHEME_MODULAR = 1
+RECONSTRUCTIONS = {"PiecewiseConst": 0, "MUSCL": 1}
+RIEMANN_SOLVERS = {"HLL": 0, "Rusanov": 1, "ROE": 2}
 
 # Every symbol include/swe_gb300.h declares.
 EXPORTS = (
@@ -65,6 +69,10 @@ class SweParams(ctypes.Structure):
         ("reserved", ctypes.c_int),
         ("dx", ctypes.c_double),
         ("dy", ctypes.c_double),
+        ("scheme", ctypes.c_int),
+        ("reconstruction", ctypes.c_int),
+        ("riemann", ctypes.c_int),
+        ("bathymetry", ctypes.c_int),
     ]
 
 

@@ -1,8 +1,9 @@
 """Builds libswe_gb300.so in-tree with nvcc for sm_103a (GB300).
 
 Each translation unit compiles in parallel with its own flags, then one link.
-The FP64 drop-in (swe_fp64.cu) is compiled with --fmad=false so that no a*b+c is
-fused: that keeps its arithmetic bitwise equal to the reference's CPU solver.
+The FP64 drop-in (swe_fp64.cu) and the modular solver (swe_modular.cu) are compiled
+with --fmad=false so that no a*b+c is fused: that keeps their arithmetic bitwise equal
+to the reference's CPU solvers.
 """
 from __future__ import annotations
 
@@ -21,6 +22,7 @@ COMMON = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xptxas", "-
 # source -> extra flags
 UNITS = {
     "swe_fp64.cu": ["--fmad=false"],
+    "swe_modular.cu": ["--fmad=false"],
     "swe_fp32.cu": [],
     "swe_reduce.cu": [],
     "swe_ensemble.cu": [],

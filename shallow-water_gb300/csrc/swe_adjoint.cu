@@ -513,6 +513,10 @@ extern "C" int swe_adjoint_gauge(swe_ctx *c, int n_steps, double dt, int n_gauge
         c->err = "swe_adjoint_gauge: not available on slab contexts";
         return SWE_ERR_UNSUPPORTED;
     }
+    if (c->p.scheme != SWE_SCHEME_FUSED) {
+        c->err = "swe_adjoint_gauge: the adjoint is of the fused scheme";
+        return SWE_ERR_UNSUPPORTED;
+    }
     for (int q = 0; q < n_gauges; ++q)
         if (gauge_i[q] < 0 || gauge_i[q] >= c->p.Nx || gauge_j[q] < 0 || gauge_j[q] >= c->p.Ny) {
             c->err = "swe_adjoint_gauge: gauge outside the interior";

@@ -93,6 +93,64 @@ int swe::pow2_exponent(double x) {
 namespace {
 
 bool fp32(const swe_ctx *c) { return c->p.precision == SWE_PRECISION_FP32_MIXED; }
+bool modular(const swe_ctx *c) { return c->p.scheme == SWE_SCHEME_MODULAR; }
+int refresh_speed(swe_ctx *c);
+
+// One stage of the modular solver from buffer set src into dst (stage 1: U^n -> U^(1),
+// 2: U^(1) -> U^(2), 3: U^(2) -> U^n).
+cudaError_t launch_modular(swe_ctx *c, int stage, double dt, void *const *src, void *const *dst) {
+    ModularStage m{};
+    m.hs = src[0]; m.hus = src[1]; m.hvs = src[2];
+    m.hn = c->Un[0]; m.hun = c->Un[1]; m.hvn = c->Un[2];
+    m.B = c->B;
+    m.ho = dst[0]; m.huo = dst[1]; m.hvo = dst[2];
+    m.Nx = c->p.Nx;
+    m.Ny = c->p.Ny;
+    m.pitch = c->pitch;
+    m.g = c->p.g;
+    m.dx = c->dx;
+    m.dy = c->dy;
+    m.dt = dt;
+    m.recon = c->p.reconstruction;
+    m.riemann = c->p.riemann;
+    m.bathy = c->p.bathymetry;
+    m.flags = c->flags;
+    return launch_stage_modular(stage, m, c->stream);
+}
+
+// swe_step of the modular scheme: SerialSolver::run's step loop with fixed dt; the time
+// accumulates on the host in step order (serial_solver.hpp:220).
+int step_modular(swe_ctx *c, int n_steps, double dt, double *t_inout) {
+    if (!(dt > 0.0))
+        return fail(c, SWE_ERR_UNSUPPORTED, "swe_step: the modular scheme takes a fixed dt > 0");
+    CK(cudaMemsetAsync(c->flags, 0, sizeof(int), c->stream));
+    CK(cudaEventRecord(c->ev0, c->stream));
+    for (int s = 0; s < n_steps; ++s) {
+        CK(launch_modular(c, 1, dt, c->Un, c->U1));
+        CK(launch_modular(c, 2, dt, c->U1, c->U2));
+        CK(launch_modular(c, 3, dt, c->U2, c->Un));
+        c->launches += 3;
+        ++c->steps_done;
+    }
+    CK(cudaEventRecord(c->ev1, c->stream));
+    const int st = refresh_speed(c);  // keeps swe_max_wave_speed current
+    if (st) return st;
+    int flags = 0;
+    CK(cudaMemcpyAsync(&flags, c->flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    c->last_ms = ms;
+    c->last_steps = n_steps;
+    c->modular_dt = dt;
+    if (t_inout)
+        for (int s = 0; s < n_steps; ++s) *t_inout += dt;
+    if (flags & FLAG_MODULAR_HLL)
+        return fail(c, SWE_ERR_NONFINITE, "HLL could not provide dissipation speed.");
+    if (flags & FLAG_NONFINITE)
+        return fail(c, SWE_ERR_NONFINITE, "non-finite state detected in positivity correction");
+    return SWE_OK;
+}
 
 // Launch parameters shared by every stage of a context (buffers set per stage).
 StageParams stage_params(swe_ctx *c, double dt) {
@@ -181,6 +239,10 @@ void swe_params_default(swe_params *p) {
     p->bc = SWE_BC_REFLECTING;
     p->precision = SWE_PRECISION_FP64;
     p->device = 0;
+    p->scheme = SWE_SCHEME_FUSED;
+    p->reconstruction = SWE_RECON_MUSCL;
+    p->riemann = SWE_RIEMANN_HLL;
+    p->bathymetry = 1;
 }
 
 const char *swe_status_string(int s) {
@@ -219,6 +281,16 @@ int swe_create(const swe_params *pin, swe_ctx **out) {
         return SWE_ERR_UNSUPPORTED;
     if ((p.x_halo_lo || p.x_halo_hi) && p.precision != SWE_PRECISION_FP64)
         return SWE_ERR_UNSUPPORTED;  // slabs are an FP64 drop-in feature
+    if (p.scheme != SWE_SCHEME_FUSED && p.scheme != SWE_SCHEME_MODULAR) return SWE_ERR_BAD_ARG;
+    if (p.scheme == SWE_SCHEME_MODULAR) {
+        if (p.reconstruction < 0 || p.reconstruction > 1 || p.riemann < 0 || p.riemann > 2)
+            return SWE_ERR_BAD_ARG;
+        p.bathymetry = p.bathymetry != 0;
+        // SerialSolver: FP64, ReflectingWalls only (the reference has no other boundary)
+        if (p.precision != SWE_PRECISION_FP64 || p.bc != SWE_BC_REFLECTING || p.x_halo_lo ||
+            p.x_halo_hi)
+            return SWE_ERR_UNSUPPORTED;
+    }
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= p.device || p.device < 0) {
         cudaGetLastError();
@@ -384,6 +456,7 @@ int swe_step(swe_ctx *c, int n_steps, double dt, double *t_inout) {
     if (n_steps == 0) return SWE_OK;
     int st = set_device(c);
     if (st) return st;
+    if (modular(c)) return step_modular(c, n_steps, dt, t_inout);
     if (c->dt_log_cap < n_steps) {
         if (c->dt_log) CK(cudaFree(c->dt_log));
         c->dt_log = nullptr;
@@ -440,6 +513,7 @@ int swe_stage(swe_ctx *c, int stage, double dt) {
     if (!c || stage < 1 || stage > 3 || !(dt > 0.0))
         return fail(c, SWE_ERR_BAD_ARG, "swe_stage: stage must be 1..3 and dt > 0");
     if (!c->uploaded) return fail(c, SWE_ERR_BAD_ARG, "swe_stage: no state uploaded");
+    if (modular(c)) return fail(c, SWE_ERR_UNSUPPORTED, "swe_stage: fused scheme only");
     int st = set_device(c);
     if (st) return st;
     StageParams sp = stage_params(c, dt);
@@ -504,6 +578,29 @@ int swe_max_wave_speed(swe_ctx *c, double *out) {
 
 int swe_stable_dt(swe_ctx *c, double *out) {
     if (!out) return fail(c, SWE_ERR_BAD_ARG, "swe_stable_dt: null argument");
+    if (c && modular(c)) {
+        if (!c->uploaded) return fail(c, SWE_ERR_BAD_ARG, "swe_stable_dt: no state uploaded");
+        int st = set_device(c);
+        if (st) return st;
+        unsigned long long *slot = c->speed + (c->steps_done & 1);
+        CK(cudaMemsetAsync(c->flags, 0, sizeof(int), c->stream));
+        CK(launch_modular_stable_dt(c->Un[0], c->Un[1], c->Un[2], c->p.Nx, c->p.Ny, c->pitch,
+                                    c->p.g, c->p.cfl, c->dx, c->dy, slot, c->flags, c->num_sms,
+                                    c->stream));
+        ++c->launches;
+        unsigned long long bits = 0;
+        int flags = 0;
+        CK(cudaMemcpyAsync(&bits, slot, sizeof bits, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(&flags, c->flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        st = refresh_speed(c);  // the slot held the max wave speed
+        if (st) return st;
+        CK(cudaStreamSynchronize(c->stream));
+        if (flags & FLAG_NONFINITE)
+            return fail(c, SWE_ERR_BAD_ARG,
+                        "Could not perform stability check for dt because h <= 0!");
+        std::memcpy(out, &bits, sizeof(double));
+        return SWE_OK;
+    }
     double ms = 0.0;
     int st = swe_max_wave_speed(c, &ms);
     if (st) return st;
@@ -565,6 +662,10 @@ int swe_dt_log(swe_ctx *c, double *out, int n, int *written) {
     const int m = std::min(n, c->last_steps);
     if (written) *written = m;
     if (m == 0) return SWE_OK;
+    if (modular(c)) {  // fixed dt
+        for (int k = 0; k < m; ++k) out[k] = c->modular_dt;
+        return SWE_OK;
+    }
     CK(cudaMemcpyAsync(out, c->dt_log, (size_t)m * sizeof(double), cudaMemcpyDeviceToHost,
                        c->stream));
     CK(cudaStreamSynchronize(c->stream));

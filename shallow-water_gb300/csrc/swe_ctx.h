@@ -31,6 +31,7 @@ struct swe_ctx {
     long long launches = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // bracket the stage launches of swe_step
     double last_ms = 0.0;
+    double modular_dt = 0.0;   // the modular scheme's fixed dt of the last swe_step
     swe::StageMaps maps[3]{};  // FP32 form: TMA maps of U^n, U^(1), U^(2) (stage sources)
     bool maps_ok = false;
     std::string err;

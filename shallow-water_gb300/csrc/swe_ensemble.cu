@@ -303,6 +303,7 @@ int swe_ens_create(const swe_params *base, int n, const int *Nx, const int *Ny, 
     if (b.nG != 2 || !(b.cfl > 0.0) || (b.bc != SWE_BC_REFLECTING && b.bc != SWE_BC_TRANSMISSIVE) ||
         (b.precision != SWE_PRECISION_FP64 && b.precision != SWE_PRECISION_FP32_MIXED))
         return SWE_ERR_BAD_ARG;
+    if (b.scheme != SWE_SCHEME_FUSED) return SWE_ERR_UNSUPPORTED;  // the fused stage only
     for (int q = 0; q < n; ++q) {
         if (Nx[q] < 2 || Ny[q] < 2) return SWE_ERR_BAD_ARG;
         if ((Lx && !(Lx[q] > 0.0)) || (Ly && !(Ly[q] > 0.0))) return SWE_ERR_BAD_ARG;

@@ -51,6 +51,27 @@ int totals_blocks(int num_sms);
 cudaError_t launch_totals_blocks(const void *h, const void *hu, const void *hv, const void *B,
                                  bool f32, int Nx, int Ny, long long pitch, double dxdy,
                                  double *partial, double *out, int blocks, cudaStream_t s);
+// The modular solver (swe_modular.cu, --fmad=false): one fused stage of
+// SerialSolver<ReflectingWalls, recon, riemann, SSPRK3, bathymetry on / off>.
+struct ModularStage {
+    const void *hs, *hus, *hvs;  // stage source
+    const void *hn, *hun, *hvn;  // U^n
+    const void *B;
+    void *ho, *huo, *hvo;
+    int Nx, Ny;
+    long long pitch;
+    double g, dx, dy, dt;
+    int recon, riemann, bathy;  // 0 / 1 PiecewiseConst / MUSCL; 0 / 1 / 2 HLL / Rusanov / ROE
+    int *flags;                 // FLAG_NONFINITE, FLAG_MODULAR_HLL
+};
+constexpr int FLAG_MODULAR_HLL = 4;  // HLL could not provide a dissipation speed
+cudaError_t launch_stage_modular(int stage, const ModularStage &m, cudaStream_t s);
+// time_utils.hpp's compute_stable_dt into *out (as double bits); h < 0 sets FLAG_NONFINITE.
+cudaError_t launch_modular_stable_dt(const void *h, const void *hu, const void *hv, int Nx, int Ny,
+                                     long long pitch, double g, double cfl, double dx, double dy,
+                                     unsigned long long *out, int *flags, int num_sms,
+                                     cudaStream_t s);
+
 // Sanity reductions (mass, energy, h_min, first negative index) into out[0..3];
 // partial holds 6 doubles per block, num_sms * 4 blocks.
 cudaError_t launch_sanity(const void *h, const void *hu, const void *hv, const void *B, bool f32,

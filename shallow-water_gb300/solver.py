@@ -46,9 +46,14 @@ class Solver:
     def __init__(self, Nx: int, Ny: int, Lx: float = 1.0, Ly: float = 1.0,
                  g: float = 9.80665, cfl: float = 0.45, bc="reflecting",
                  precision="fp64", device: int = 0, x_halo=(False, False),
-                 dx: float = 0.0, dy: float = 0.0):
+                 dx: float = 0.0, dy: float = 0.0, scheme: str = "fused",
+                 reconstruction: str = "MUSCL", riemann: str = "HLL", bathymetry: bool = True):
         """``x_halo`` marks the low / high x sides whose ghost rows a neighbour slab
-        supplies, ``dx``/``dy`` > 0 fix the cell sizes (see ``slabs.SlabGrid``)."""
+        supplies, ``dx``/``dy`` > 0 fix the cell sizes (see ``slabs.SlabGrid``).
+
+        ``scheme="modular"`` runs the reference's SerialSolver arithmetic with the given
+        ``reconstruction`` (PiecewiseConst, MUSCL), ``riemann`` (HLL, Rusanov, ROE) and
+        ``bathymetry`` (False: the None instantiation, B unused); fixed dt only."""
         self._lib = L.lib()
         p = L.SweParams()
         self._lib.swe_params_default(ctypes.byref(p))
@@ -58,6 +63,10 @@ class Solver:
         p.device = device
         p.x_halo_lo, p.x_halo_hi = int(bool(x_halo[0])), int(bool(x_halo[1]))
         p.dx, p.dy = float(dx), float(dy)
+        p.scheme = {"fused": L.SWE_SCHEME_FUSED, "modular": L.SWE_SCHEME_MODULAR}[scheme]
+        p.reconstruction = L.RECONSTRUCTIONS[reconstruction]
+        p.riemann = L.RIEMANN_SOLVERS[riemann]
+        p.bathymetry = int(bool(bathymetry))
         self.params = p
         self.Nx, self.Ny = Nx, Ny
         self._ctx = ctypes.c_void_p()
