@@ -17,6 +17,13 @@
 //     steps and at the end, the ETA line, a timing summary.
 //   * non-copyable, RAII device memory, errors as std::runtime_error.
 //
+// Scheme: with [solver] MUSCL + HLL and Flat or GaussHill bathymetry - the combination
+// the reference's optimised backends run - the class uses the fused scheme, bitwise
+// FastHLLMUSCLBathySolver (HPC_solver.hpp).  Every other [solver] reconstruction /
+// riemann and [bathymetry] choice runs the modular scheme, bitwise the reference's
+// SerialSolver for that combination (serial_solver.hpp; the Serial backend's dispatch,
+// solver_assembly.hpp:330-490), where the optimised backends would ignore the setting.
+//
 // With SWE_GB300_NATIVE_OUTPUT=1 the snapshots go through the library's own NetCDF
 // writer (swe_snapshot_*) instead of the reference's NetCDFWriter: each record is packed
 // on the GPU and written by a background thread while the run continues, so an output
@@ -74,6 +81,15 @@ class FastHLLMUSCLBathyGB300Solver {
 
         swe_params p;
         swe_params_default(&p);
+        if (!fused(cfg_)) {
+            p.scheme = SWE_SCHEME_MODULAR;
+            p.reconstruction = cfg_.solver.reconstruction == ReconstructionType::MUSCL
+                                   ? SWE_RECON_MUSCL : SWE_RECON_PIECEWISE_CONST;
+            p.riemann = cfg_.solver.riemann == RiemannType::HLL       ? SWE_RIEMANN_HLL
+                        : cfg_.solver.riemann == RiemannType::Rusanov ? SWE_RIEMANN_RUSANOV
+                                                                      : SWE_RIEMANN_ROE;
+            p.bathymetry = cfg_.bathymetry.type != BathymetryType::None;
+        }
         p.Nx = grid_.Nx();
         p.Ny = grid_.Ny();
         p.nG = grid_.nG();
@@ -126,7 +142,11 @@ class FastHLLMUSCLBathyGB300Solver {
     void run() {
         std::cout << std::unitbuf;
         std::cerr << std::unitbuf;
-        std::cout << "INFO: GB300 fused-stage solver active\n";
+        if (fused(cfg_))
+            std::cout << "INFO: GB300 fused-stage solver active\n";
+        else
+            std::cout << "INFO: GB300 modular solver active (" << reconstruction_name(cfg_)
+                      << " + " << riemann_name(cfg_) << ")\n";
 
         double dt_stable = 0.0;
         {
@@ -252,8 +272,10 @@ class FastHLLMUSCLBathyGB300Solver {
         if (first) {
             const std::string backend = backend_name_from_cfg(cfg_);
             const std::string bathy = bathymetry_name_from_cfg(cfg_);
-            check_snap(swe_snapshot_metadata(snap_, dt_, backend.c_str(), "HLL", "MUSCL",
-                                             "SSPRK3", "Reflecting Walls", bathy.c_str()),
+            check_snap(swe_snapshot_metadata(snap_, dt_, backend.c_str(),
+                                             riemann_name(cfg_).c_str(),
+                                             reconstruction_name(cfg_).c_str(), "SSPRK3",
+                                             "Reflecting Walls", bathy.c_str()),
                        "swe_snapshot_metadata");
         }
         check_snap(swe_snapshot_write(snap_, ctx_, time), "swe_snapshot_write");
@@ -266,9 +288,9 @@ class FastHLLMUSCLBathyGB300Solver {
         if (!first) check(swe_download(ctx_, h_.data(), hu_.data(), hv_.data()), "swe_download");
         fill_io_state();
         if (first) {
-            writer_.write_snapshot(io_state_, time, dt_, backend_name_from_cfg(cfg_), "HLL",
-                                   "MUSCL", "SSPRK3", "Reflecting Walls",
-                                   bathymetry_name_from_cfg(cfg_));
+            writer_.write_snapshot(io_state_, time, dt_, backend_name_from_cfg(cfg_),
+                                   riemann_name(cfg_), reconstruction_name(cfg_), "SSPRK3",
+                                   "Reflecting Walls", bathymetry_name_from_cfg(cfg_));
         } else {
             writer_.write_snapshot(io_state_, time);
         }
@@ -297,8 +319,29 @@ class FastHLLMUSCLBathyGB300Solver {
         }
         return std::make_unique<SanityCheckNetCDFWriter>(
             cfg.sanity_checks.output_path.string(), cfg.time.time_unit, cfg.mesh.spatial_unit_h,
-            cfg.time.save_every, dt, backend_name_from_cfg(cfg), "HLL", "MUSCL", "SSPRK3",
-            "Reflecting Walls", bathymetry_name_from_cfg(cfg));
+            cfg.time.save_every, dt, backend_name_from_cfg(cfg), riemann_name(cfg),
+            reconstruction_name(cfg), "SSPRK3", "Reflecting Walls", bathymetry_name_from_cfg(cfg));
+    }
+
+    // The combination the optimised backends run (solver_assembly.hpp:50-117).
+    static bool fused(const SimulationConfig &cfg) {
+        return cfg.solver.reconstruction == ReconstructionType::MUSCL &&
+               cfg.solver.riemann == RiemannType::HLL &&
+               (cfg.bathymetry.type == BathymetryType::Flat ||
+                cfg.bathymetry.type == BathymetryType::GaussHill);
+    }
+    // SerialSolver's riemann_name_static / reconstruction_name_static (serial_solver.hpp:
+    // 397-418).
+    static std::string riemann_name(const SimulationConfig &cfg) {
+        switch (cfg.solver.riemann) {
+            case RiemannType::Rusanov: return "Rusanov";
+            case RiemannType::HLL: return "HLL";
+            case RiemannType::ROE: return "ROE";
+        }
+        return "UnknownRiemann";
+    }
+    static std::string reconstruction_name(const SimulationConfig &cfg) {
+        return cfg.solver.reconstruction == ReconstructionType::MUSCL ? "MUSCL" : "PiecewiseConst";
     }
 
     void print_summary(std::size_t steps) const {

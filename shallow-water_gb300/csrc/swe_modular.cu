@@ -12,8 +12,8 @@
 //
 // The arithmetic is the reference's own, operation by operation, including the
 // association of its CellState and std::array expressions, so results are bitwise equal
-// to SerialSolver: the file is compiled with --fmad=false and uses IEEE division and
-// square root.  std::min / std::max are written as their definitions
+// to SerialSolver: the file is compiled with --fmad=false, and its divisions and square
+// roots are correctly rounded (on the integer pipes, swe_soft_f64.cuh).  std::min / std::max are written as their definitions
 // ((b < a) ? b : a, (a < b) ? b : a), which fixes their NaN and signed-zero behaviour.
 #include <cuda_runtime.h>
 
@@ -21,6 +21,7 @@
 
 #include "swe_common.cuh"
 #include "swe_launch.h"
+#include "swe_soft_f64.cuh"
 
 namespace swe {
 namespace mod {
@@ -34,47 +35,50 @@ struct CS {
     double h, hu, hv;
 };  // CellState (include/core/cell_state.hpp:6-35)
 
+// A CellState with its u() and v() (cell_state.hpp:18-25), computed once: the reference
+// recomputes them on every call, with the same operands, so the values are the same.
+struct CSV {
+    double h, hu, hv, u, v;
+};
+
 __device__ __forceinline__ double dmin(double a, double b) { return (b < a) ? b : a; }
 __device__ __forceinline__ double dmax(double a, double b) { return (a < b) ? b : a; }
 
-// CellState::u / v (cell_state.hpp:18-25)
-__device__ __forceinline__ double cs_u(const CS &s) { return (s.h > EPS) ? (s.hu / s.h) : 0.0; }
-__device__ __forceinline__ double cs_v(const CS &s) { return (s.h > EPS) ? (s.hv / s.h) : 0.0; }
+// IEEE division and square root, correctly rounded on the integer pipes
+// (swe_soft_f64.cuh): the same results as the FP64 unit's, off the FP64 pipe.
+__device__ __forceinline__ double ddiv(double a, double b) { return sf::div_rn(a, b); }
+__device__ __forceinline__ double dsqrt(double a) { return sf::sqrt_rn(a); }
+
+__device__ __forceinline__ CSV with_velocity(const CS &s) {
+    CSV r{s.h, s.hu, s.hv, 0.0, 0.0};
+    if (s.h > EPS) sf::div2_rn(s.hu, s.hv, s.h, r.u, r.v);
+    return r;
+}
 
 // RiemannSolver::F / G (riemann/riemann.hpp:10-19); half_g = 0.5 * g (exact).
-__device__ __forceinline__ CS flux_F(double half_g, const CS &U) {
-    const double u = cs_u(U);
-    return {U.hu, u * u * U.h + half_g * U.h * U.h, U.hu * cs_v(U)};
-}
-__device__ __forceinline__ CS flux_G(double half_g, const CS &U) {
-    const double v = cs_v(U);
-    return {U.hv, U.hu * v, U.h * v * v + half_g * U.h * U.h};
-}
-
 template <int DIR>
-__device__ __forceinline__ CS phys_flux(double half_g, const CS &U) {
-    return DIR == 0 ? flux_F(half_g, U) : flux_G(half_g, U);
-}
-template <int DIR>
-__device__ __forceinline__ double normal_vel(const CS &U) {
-    return DIR == 0 ? cs_u(U) : cs_v(U);
+__device__ __forceinline__ CS phys_flux(double half_g, const CSV &U) {
+    if (DIR == 0) return {U.hu, U.u * U.u * U.h + half_g * U.h * U.h, U.hu * U.v};
+    return {U.hv, U.hu * U.v, U.h * U.v * U.v + half_g * U.h * U.h};
 }
 
 // HLL (riemann/HLL.hpp:10-45).  Sets *fail where the reference throws "HLL could not
 // provide dissipation speed." (NaN speeds).
 template <int DIR>
-__device__ __forceinline__ CS hll(double g, double half_g, const CS &A, const CS &B, bool *fail) {
-    const double uA = normal_vel<DIR>(A), uB = normal_vel<DIR>(B);
-    const double cA = sqrt(g * A.h), cB = sqrt(g * B.h);
+__device__ __forceinline__ CS hll(double g, double half_g, const CSV &A, const CSV &B, bool *fail) {
+    const double uA = DIR == 0 ? A.u : A.v, uB = DIR == 0 ? B.u : B.v;
+    const double cA = dsqrt(g * A.h), cB = dsqrt(g * B.h);
     const double sR = dmax(uA + cA, uB + cB);
     const double sL = dmin(uA - cA, uB - cB);
     if (sL >= 0.0) return phys_flux<DIR>(half_g, A);
     if (sL < 0.0 && sR > 0.0) {
         const CS FA = phys_flux<DIR>(half_g, A), FB = phys_flux<DIR>(half_g, B);
         const double ss = sL * sR, d = sR - sL;
-        return {(sR * FA.h - sL * FB.h + ss * (B.h - A.h)) / d,
-                (sR * FA.hu - sL * FB.hu + ss * (B.hu - A.hu)) / d,
-                (sR * FA.hv - sL * FB.hv + ss * (B.hv - A.hv)) / d};
+        CS r;
+        sf::div2_rn(sR * FA.h - sL * FB.h + ss * (B.h - A.h),
+                    sR * FA.hu - sL * FB.hu + ss * (B.hu - A.hu), d, r.h, r.hu);
+        r.hv = ddiv(sR * FA.hv - sL * FB.hv + ss * (B.hv - A.hv), d);
+        return r;
     }
     if (sR <= 0.0) return phys_flux<DIR>(half_g, B);
     *fail = true;
@@ -83,35 +87,33 @@ __device__ __forceinline__ CS hll(double g, double half_g, const CS &A, const CS
 
 // Rusanov (riemann/rusanov.hpp:12-30)
 template <int DIR>
-__device__ __forceinline__ CS rusanov(double g, double half_g, const CS &A, const CS &B) {
-    const double uA = normal_vel<DIR>(A), uB = normal_vel<DIR>(B);
+__device__ __forceinline__ CS rusanov(double g, double half_g, const CSV &A, const CSV &B) {
+    const double uA = DIR == 0 ? A.u : A.v, uB = DIR == 0 ? B.u : B.v;
     const double hB = dmax(B.h, 0.0), hA = dmax(A.h, 0.0);
-    const double a = dmax(fabs(uA) + sqrt(g * hA), fabs(uB) + sqrt(g * hB));
+    const double a = dmax(fabs(uA) + dsqrt(g * hA), fabs(uB) + dsqrt(g * hB));
     const CS FA = phys_flux<DIR>(half_g, A), FB = phys_flux<DIR>(half_g, B);
     const double ha = 0.5 * a;
     return {0.5 * (FA.h + FB.h) - ha * (B.h - A.h), 0.5 * (FA.hu + FB.hu) - ha * (B.hu - A.hu),
             0.5 * (FA.hv + FB.hv) - ha * (B.hv - A.hv)};
 }
 
-// ROE::compute_roe_avg (riemann/ROE.hpp:66-69)
-__device__ __forceinline__ double roe_avg(double u1, double h1, double u2, double h2) {
-    return ((sqrt(h1) * u1) + (sqrt(h2) * u2)) / (sqrt(h1) + sqrt(h2));
-}
-
-// ROE (riemann/ROE.hpp:10-63).  The eigenvectors' 0 and 1 entries are multiplied as
+// ROE (riemann/ROE.hpp:10-63), compute_roe_avg (:66-69) for u and v over the one
+// denominator sqrt(h1) + sqrt(h2).  The eigenvectors' 0 and 1 entries are multiplied as
 // written: 0 * x keeps the sign of x and its NaN, as the reference's std::array product.
 template <int DIR>
-__device__ __forceinline__ CS roe(double g, double half_g, const CS &A, const CS &B) {
+__device__ __forceinline__ CS roe(double g, double half_g, const CSV &A, const CSV &B) {
     const double h = (A.h + B.h) / 2.0;
-    const double c = sqrt(g * h);
-    const double u_roe = roe_avg(cs_u(A), A.h, cs_u(B), B.h);
-    const double v_roe = roe_avg(cs_v(A), A.h, cs_v(B), B.h);
+    const double c = dsqrt(g * h);
+    const double sA = dsqrt(A.h), sB = dsqrt(B.h);
+    double u_roe, v_roe;
+    sf::div2_rn((sA * A.u) + (sB * B.u), (sA * A.v) + (sB * B.v), sA + sB, u_roe, v_roe);
     const double vn = DIR == 0 ? u_roe : v_roe, vt = DIR == 0 ? v_roe : u_roe;
     const double l1 = vn - c, l2 = vn, l3 = vn + c;
     const double dh = B.h - A.h, dhu = B.hu - A.hu, dhv = B.hv - A.hv;
     const double dqn = DIR == 0 ? dhu : dhv, dqt = DIR == 0 ? dhv : dhu;
-    const double alpha1 = 0.5 * (dh - ((dqn - vn * dh) / c));
-    const double alpha3 = 0.5 * (dh + ((dqn - vn * dh) / c));
+    const double q = ddiv(dqn - vn * dh, c);
+    const double alpha1 = 0.5 * (dh - q);
+    const double alpha3 = 0.5 * (dh + q);
     const double alpha2 = dqt - vt * dh;
     const double w1 = fabs(l1) * alpha1, w2 = fabs(l2) * alpha2, w3 = fabs(l3) * alpha3;
     // r1 = {1, l1, v_roe}, r2 = {0, 0, 1}, r3 = {1, l3, v_roe} in x;
@@ -119,16 +121,18 @@ __device__ __forceinline__ CS roe(double g, double half_g, const CS &A, const CS
     const double r1[3] = {1.0, DIR == 0 ? l1 : u_roe, DIR == 0 ? v_roe : l1};
     const double r2[3] = {0.0, DIR == 0 ? 0.0 : 1.0, DIR == 0 ? 1.0 : 0.0};
     const double r3[3] = {1.0, DIR == 0 ? l3 : u_roe, DIR == 0 ? v_roe : l3};
-    double s[3];
+    double sum[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) s[k] = ((r1[k] * w1 + r2[k] * w2) + r3[k] * w3) * 0.5;
+    for (int k = 0; k < 3; ++k) sum[k] = ((r1[k] * w1 + r2[k] * w2) + r3[k] * w3) * 0.5;
     const CS FA = phys_flux<DIR>(half_g, A), FB = phys_flux<DIR>(half_g, B);
-    return {0.5 * (FA.h + FB.h) - s[0], 0.5 * (FA.hu + FB.hu) - s[1], 0.5 * (FA.hv + FB.hv) - s[2]};
+    return {0.5 * (FA.h + FB.h) - sum[0], 0.5 * (FA.hu + FB.hu) - sum[1],
+            0.5 * (FA.hv + FB.hv) - sum[2]};
 }
 
 template <int RIEMANN, int DIR>
-__device__ __forceinline__ CS riemann(double g, double half_g, const CS &A, const CS &B,
+__device__ __forceinline__ CS riemann(double g, double half_g, const CS &A0, const CS &B0,
                                       bool *fail) {
+    const CSV A = with_velocity(A0), B = with_velocity(B0);
     if (RIEMANN == 0) return hll<DIR>(g, half_g, A, B, fail);
     if (RIEMANN == 1) return rusanov<DIR>(g, half_g, A, B);
     return roe<DIR>(g, half_g, A, B);
@@ -195,8 +199,9 @@ __device__ __forceinline__ void interface_flux(const Tile &t, int r, int c, doub
     const double b_star = dmax(b_m, b_p);
     const double h_m = dmax(0.0, eta_m - b_m), h_p = dmax(0.0, eta_p - b_p);
     // safe_velocity (flux_assembly_bathy.hpp:180-185)
-    const double u_m = (h_m < EPS) ? 0.0 : A.hu / h_m, v_m = (h_m < EPS) ? 0.0 : A.hv / h_m;
-    const double u_p = (h_p < EPS) ? 0.0 : B.hu / h_p, v_p = (h_p < EPS) ? 0.0 : B.hv / h_p;
+    double u_m = 0.0, v_m = 0.0, u_p = 0.0, v_p = 0.0;
+    if (!(h_m < EPS)) sf::div2_rn(A.hu, A.hv, h_m, u_m, v_m);
+    if (!(h_p < EPS)) sf::div2_rn(B.hu, B.hv, h_p, u_p, v_p);
     const double hs_m = dmax(0.0, eta_m - b_star), hs_p = dmax(0.0, eta_p - b_star);
     const CS Um = {hs_m, hs_m * u_m, hs_m * v_m}, Up = {hs_p, hs_p * u_p, hs_p * v_p};
     const CS F = riemann<RIEMANN, DIR>(g, half_g, Um, Up, fail);

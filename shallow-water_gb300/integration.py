@@ -15,10 +15,11 @@ import os
 
 CASE_BLOCK = '''        case BackendType::GB300: {
 #if USE_GB300
-            warn_if_ignored_optimized_settings(cfg_, "GB300");
-
-            if (cfg_.bathymetry.type == BathymetryType::Flat ||
-                cfg_.bathymetry.type == BathymetryType::GaussHill) {
+            // MUSCL + HLL over Flat / GaussHill bathymetry runs the fused scheme (as the
+            // CUDA backend); every other [solver] / [bathymetry] choice runs the modular
+            // scheme, as the Serial backend would (FastHLLMUSCLBathyGB300Solver decides).
+            if (cfg_.boundary.type == BoundaryType::ReflectingWalls &&
+                cfg_.solver.time == TimeIntegratorType::SSPRK3) {
 
                 FastHLLMUSCLBathyGB300Solver solver(cfg_);
                 solver.run();
@@ -26,8 +27,8 @@ CASE_BLOCK = '''        case BackendType::GB300: {
             }
 
             throw std::runtime_error("Unsupported GB300 solver combination. "
-                                     "The GB300 backend supports MUSCL + HLL + SSPRK3 + "
-                                     "ReflectingWalls with Flat or GaussHill bathymetry.");
+                                     "The GB300 backend supports SSPRK3 + ReflectingWalls "
+                                     "with any reconstruction, riemann and bathymetry.");
 #else
             throw std::runtime_error(
                 "GB300 backend was requested in simulation_config.toml, but this binary "

@@ -156,3 +156,25 @@ def test_gb300_backend_with_native_output(patched_tree):
     else:
         assert r.returncode != 0
         assert "GB300 backend: swe_create: no CUDA device" in r.stderr
+
+
+def test_gb300_backend_dispatches_modular_combinations(patched_app):
+    """[solver] PiecewiseConst + Rusanov over no bathymetry (a Serial-backend combination)
+    reaches the GB300 class, which runs it with the modular scheme."""
+    tree, exe = patched_app
+    cfg = tree / "configs" / "simulation_config.toml"
+    os.chmod(cfg, 0o644)
+    text = CONFIG.replace("{backend}", "GB300").replace('reconstruction = "MUSCL"',
+                                                          'reconstruction = "PiecewiseConst"')
+    text = text.replace('riemann = "HLL"', 'riemann = "Rusanov"').replace('type = "GaussHill"',
+                                                                        'type = "None"')
+    cfg.write_text(text)
+    r = subprocess.run([str(exe)], cwd=tree, capture_output=True, text=True, timeout=120)
+    import torch
+    if torch.cuda.is_available():
+        assert r.returncode == 0, r.stderr
+        assert "GB300 modular solver active (PiecewiseConst + Rusanov)" in r.stdout
+    else:
+        assert r.returncode != 0
+        assert "Unsupported" not in r.stderr
+        assert "GB300 backend: swe_create: no CUDA device" in r.stderr
