@@ -60,6 +60,9 @@ def parse():
                     help="comma list of the extra forms to measure")
     ap.add_argument("--fp32-n", type=int, default=16384)
     ap.add_argument("--ens-count", type=int, default=512)
+    ap.add_argument("--ens-precisions", default="fp64,fp32_mixed")
+    ap.add_argument("--ens-schedule", default="",
+                    help="fixed SHAPE:GRID for every precision instead of the autotuner")
     ap.add_argument("--adj-n", type=int, default=1024)
     ap.add_argument("--adj-steps", type=int, default=200)
     ap.add_argument("--acc-n", type=int, default=2048)
@@ -285,11 +288,16 @@ def form_ensemble(args, sw):
     res = {"instances": len(specs), "cells": cells,
            "sides": sorted({n for n, _ in specs})}
     members = [P.ensemble_member(n, sd) for n, sd in specs]
-    for prec in ("fp64", "fp32_mixed"):
+    for prec in args.ens_precisions.split(","):
         with sw.Ensemble(sizes, precision=prec) as ens:
             for q, mbr in enumerate(members):
                 ens.upload(q, *mbr)
-            tune = ens.tune(steps=1)
+            if args.ens_schedule:
+                shape, grid = args.ens_schedule.split(":")
+                ens.set_schedule(shape, int(grid))
+                tune = {"shape": shape, "grid": int(grid)}
+            else:
+                tune = ens.tune(steps=1)
             steps = 3 if prec == "fp64" else 20
             ens.step(1)
             ens.step(steps)

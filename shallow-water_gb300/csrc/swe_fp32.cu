@@ -334,22 +334,52 @@ __global__ void __launch_bounds__((TI + 1) * TJ, ens_min_blocks_f32(TI, TJ))
     // The instance's view lives in shared memory, read where used, as the single-grid
     // kernel reads its parameters from the constant bank (held in registers it halves
     // the resident CTAs).
+    //
+    // With fewer CTAs than tiles (a persistent schedule) each CTA takes a contiguous
+    // range of the work list, so consecutive tiles mostly belong to one instance: the
+    // view, the instance's dt and its TMA maps are set up once per instance the range
+    // touches, not once per tile, and the next tile's instance needs no global lookup.
     __shared__ StageParams s_p;
-    __shared__ int s_t;
-    for (int T = blockIdx.x; T < e.total_tiles; T += gridDim.x) {
+    __shared__ int s_q, s_t, s_ntiles;
+    __shared__ float s_dtf;
+    const int total = e.total_tiles;
+    int T0 = blockIdx.x, T1 = blockIdx.x + 1;
+    if ((int)gridDim.x < total) {
+        const int per = (total + (int)gridDim.x - 1) / (int)gridDim.x;
+        T0 = blockIdx.x * per;
+        T1 = min(total, T0 + per);
+    }
+    for (int T = T0; T < T1; ++T) {
         if (threadIdx.x == 0) {
-            const int q = e.tile_inst[T];
-            s_p = ens_view(e, q);
-            s_t = T - e.inst[q].tile_base;
+            int q = s_q, t = s_t + 1;
+            const bool fresh = T == T0 || t == s_ntiles;
+            if (T == T0) {
+                q = e.tile_inst[T];
+                t = T - e.inst[q].tile_base;
+            } else if (t == s_ntiles) {
+                q = q + 1;  // the work list holds the instances' tiles in instance order
+                t = 0;
+            }
+            if (fresh) {
+                s_p = ens_view(e, q);
+                s_ntiles = ((e.inst[q].Nx + TI - 1) / TI) * e.inst[q].tiles_j;
+                // the instance's dt of this step, as stage_dt_f32
+                double dt = e.dt_fixed;
+                if (!(dt > 0.0)) {
+                    const double ms = __longlong_as_double((long long)s_p.speed[s_p.slot_read]);
+                    dt = (ms <= EPS) ? 1.0e100 : s_p.cfl_min_dxdy / ms;
+                }
+                s_dtf = (float)dt;
+            }
+            s_q = q;
+            s_t = t;
         }
         __syncthreads();
         const StageParams &p = s_p;
-        const int q = e.tile_inst[T];
-        const int t = s_t;
+        const int q = s_q, t = s_t;
         const int tiles_j = e.inst[q].tiles_j;
         const int ti = t / tiles_j, tj = t - (t / tiles_j) * tiles_j;
-        const BlockDt bd = stage_dt_f32(p);
-        const float dt = bd.f;
+        const float dt = s_dtf;
         tma::TileMaps tm{};
         if (e.maps) {
             const CUtensorMap *m =
@@ -360,13 +390,13 @@ __global__ void __launch_bounds__((TI + 1) * TJ, ens_min_blocks_f32(TI, TJ))
             stage_tile_f32<TI, TJ, STAGE>(p, ti * TI, tj * TJ, dt, e.maps ? &tm : nullptr);
         if (STAGE == 1 && t == 0 && threadIdx.x == 0) {
             p.speed[p.slot_write] = 0ull;
-            if (e.dt_last) e.dt_last[q] = (double)dt;
+            if (e.dt_last) e.dt_last[q] = (double)dt;  // the FP32 dt the update applied
         }
         if (STAGE == 3) {
             block_max_to_slot_f(speed, p.speed + p.slot_write);
             if (t == 0 && threadIdx.x == 0) e.t[q] += (double)dt;
         }
-        __syncthreads();  // the next tile reuses the shared tile buffers
+        __syncthreads();  // the next tile reuses the shared tile buffers and the view
     }
 }
 
