@@ -292,13 +292,16 @@ int swe_ens_last_dt(swe_ens *ens, double *dt);
 int swe_ens_last_step_ms(const swe_ens *ens, double *ms);
 long long swe_ens_kernel_launches(const swe_ens *ens);
 
-/* Schedule: tile shape (SWE_SHAPE_*) and CTAs per launch (0: one CTA per tile). */
+/* Schedule: tile shape (SWE_SHAPE_*) and CTAs per launch (0: one CTA per tile; a larger
+ * grid is capped at the CTAs that fit on the GPU at once, each taking an equal contiguous
+ * share of the tiles in FP32). */
 int swe_ens_set_schedule(swe_ens *ens, int shape, int grid);
 int swe_ens_get_schedule(const swe_ens *ens, int *shape, int *grid, int *total_tiles);
 
-/* Autotuner: times every compiled tile shape with one CTA per tile and with 2, 4 and 8
- * CTAs per SM, `steps` RK3 steps each, on the uploaded ensemble (the state is restored
- * after every candidate), keeps the fastest and returns its ms per step. */
+/* Autotuner: times every compiled tile shape with one CTA per tile and with a persistent
+ * grid of all / half of the CTAs that fit on the GPU at once, `steps` RK3 steps each, on
+ * the uploaded ensemble (the state is restored after every candidate), keeps the fastest
+ * and returns its ms per step. */
 int swe_ens_tune(swe_ens *ens, int steps, double *best_ms);
 
 const char *swe_ens_last_error(const swe_ens *ens);

@@ -220,9 +220,21 @@ EnsParams stage_params(const swe_ens *c, int stage, int slot_read, double dt_fix
     return e;
 }
 
+// CTAs of the current shape resident on the whole GPU at once (0: unknown).
+int resident_ctas(const swe_ens *c) {
+    const int per_sm = c->f32 ? ens_resident_per_sm_f32(c->shape) : ens_resident_per_sm_f64(c->shape);
+    return per_sm * c->num_sms;
+}
+
+// A persistent schedule never asks for more CTAs than fit at once: with every CTA
+// resident, equal shares of the work list finish together instead of in waves.
 int grid_ctas(const swe_ens *c) {
-    if (c->grid > 0) return std::min(c->grid, std::max(c->total_tiles, 1));
-    return std::max(c->total_tiles, 1);
+    const int tiles = std::max(c->total_tiles, 1);
+    if (c->grid <= 0) return tiles;
+    int g = std::min(c->grid, tiles);
+    const int r = resident_ctas(c);
+    if (r > 0 && g > r) g = r;
+    return g;
 }
 
 int launch_step(swe_ens *c, int slot_read, double dt_fixed) {
@@ -567,12 +579,20 @@ int swe_ens_tune(swe_ens *c, int steps, double *best_ms) {
     const int shapes64[] = {SHAPE_8x32, SHAPE_8x16, SHAPE_4x64};
     const int shapes32[] = {SHAPE_8x32, SHAPE_16x32, SHAPE_8x64};
     const int *shapes = c->f32 ? shapes32 : shapes64;
-    const int grids[] = {0, 2, 4, 8};  // 0: one CTA per tile; else CTAs per SM (persistent)
+    // 0: one CTA per tile; 1 / 2: a persistent grid of every resident CTA / half of them
+    const int grids[] = {0, 1, 2};
     double best = 1e300;
     int best_shape = c->shape, best_grid = c->grid;
     for (int si = 0; si < 3; ++si) {
         for (int gm : grids) {
-            int st = swe_ens_set_schedule(c, shapes[si], gm * c->num_sms);
+            int g = 0;
+            if (gm > 0) {
+                const int per_sm = c->f32 ? ens_resident_per_sm_f32(shapes[si])
+                                          : ens_resident_per_sm_f64(shapes[si]);
+                if (per_sm <= 0 || (gm == 2 && per_sm < 2)) continue;
+                g = (gm == 1 ? per_sm : per_sm / 2) * c->num_sms;
+            }
+            int st = swe_ens_set_schedule(c, shapes[si], g);
             if (st) return st;
             st = run_steps(c, 1, 0.0);  // warm-up (also captures the graphs)
             if (st) return st;
@@ -586,7 +606,7 @@ int swe_ens_tune(swe_ens *c, int steps, double *best_ms) {
             if (ms < best) {
                 best = ms;
                 best_shape = shapes[si];
-                best_grid = gm * c->num_sms;
+                best_grid = g;
             }
             st = restore();
             if (st) return st;

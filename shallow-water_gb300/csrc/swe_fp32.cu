@@ -505,6 +505,28 @@ static cudaError_t ens_launch_f32(int stage, const EnsParams &e, int grid, cudaS
     return cudaGetLastError();
 }
 
+template <int TI, int TJ>
+static int ens_resident_f32() {
+    constexpr int NT = (TI + 1) * TJ;
+    int n1 = 0, n2 = 0, n3 = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_ens_stage_f32<TI, TJ, 1>, NT, 0) ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_ens_stage_f32<TI, TJ, 2>, NT, 0) ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n3, k_ens_stage_f32<TI, TJ, 3>, NT, 0)) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n1 < n2 ? (n1 < n3 ? n1 : n3) : (n2 < n3 ? n2 : n3);
+}
+
+int ens_resident_per_sm_f32(int shape) {
+    switch (shape) {
+        case SHAPE_8x32: return ens_resident_f32<8, 32>();
+        case SHAPE_16x32: return ens_resident_f32<16, 32>();
+        case SHAPE_8x64: return ens_resident_f32<8, 64>();
+        default: return 0;
+    }
+}
+
 cudaError_t launch_ens_stage_f32(int shape, int stage, const EnsParams &e, int grid,
                                  cudaStream_t s) {
     switch (shape) {

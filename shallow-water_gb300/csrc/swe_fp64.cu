@@ -651,6 +651,36 @@ static cudaError_t ens_launch_f64(int stage, const EnsParams &e, int grid, cudaS
     }
 }
 
+template <int TI, int TJ, int STAGE>
+static int ens_resident_stage_f64() {
+    constexpr int NT = (TI + 1) * TJ;
+    constexpr size_t smem = sizeof(TileF64<TI, TJ>) + 128;
+    static bool done[64];
+    if (smem_opt_in(k_ens_stage_f64<TI, TJ, STAGE>, smem, done) != cudaSuccess) return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_ens_stage_f64<TI, TJ, STAGE>, NT,
+                                                      smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+template <int TI, int TJ>
+static int ens_resident_f64() {
+    return std::min(ens_resident_stage_f64<TI, TJ, 1>(),
+                    std::min(ens_resident_stage_f64<TI, TJ, 2>(), ens_resident_stage_f64<TI, TJ, 3>()));
+}
+
+int ens_resident_per_sm_f64(int shape) {
+    switch (shape) {
+        case SHAPE_8x32: return ens_resident_f64<8, 32>();
+        case SHAPE_8x16: return ens_resident_f64<8, 16>();
+        case SHAPE_4x64: return ens_resident_f64<4, 64>();
+        default: return 0;
+    }
+}
+
 cudaError_t launch_ens_stage_f64(int shape, int stage, const EnsParams &e, int grid,
                                  cudaStream_t s) {
     switch (shape) {

@@ -16,6 +16,10 @@ constexpr int TILE_I_F64 = 8, TILE_J_F64 = 32;
 // Ensemble stage over the work list; shape is SHAPE_* (8x32, 8x16, 4x64 for FP64).
 cudaError_t launch_ens_stage_f64(int shape, int stage, const EnsParams &e, int grid,
                                  cudaStream_t s);
+// CTAs of each ensemble tile shape that fit on one SM at once (the minimum over the three
+// stage kernels; 0 if the occupancy query fails).
+int ens_resident_per_sm_f64(int shape);
+int ens_resident_per_sm_f32(int shape);
 cudaError_t launch_max_speed_f64(const void *h, const void *hu, const void *hv, int Nx, int Ny,
                                  long long pitch, double g, unsigned long long *slot,
                                  int num_sms, cudaStream_t s);
