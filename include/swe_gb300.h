@@ -247,7 +247,10 @@ int swe_last_step_ms(const swe_ctx *ctx, double *ms);
  * Outputs, in the ghosted host layout with zero ghosts: J, dJ/dh^0,
  * dJ/dhu^0, dJ/dhv^0 and dJ/dB with the initial state held fixed, where the ghosts of B
  * are taken to follow the wall rule (mirror or copy of the interior).  ms (optional)
- * receives the device time.  FP64 contexts only.  No reference counterpart. */
+ * receives the device time.  On an FP32-mixed context the forward is the FP32 stage
+ * kernel and the adjoint runs in FP32 with eta = h + B as the state variable (half the
+ * memory; (38 n_steps + 200) bytes per cell in tape mode); the outputs are the same
+ * derivatives, widened to double.  Fused scheme only.  No reference counterpart. */
 #define SWE_ADJ_TAPE_ALL (-1)
 int swe_adjoint_gauge(swe_ctx *ctx, int n_steps, double dt, int n_gauges, const int *gauge_i,
                       const int *gauge_j, const double *h_obs, int n_snapshots, double *J,

@@ -1,5 +1,16 @@
-// Discrete adjoint of the FP64 scheme with binomial checkpointing (C ABI:
-// swe_adjoint_gauge in include/swe_gb300.h).
+// Discrete adjoint with binomial checkpointing (C ABI: swe_adjoint_gauge in
+// include/swe_gb300.h), of the FP64 scheme on FP64 contexts and of the FP32-mixed
+// scheme on FP32-mixed contexts.
+//
+// FP32-mixed: the forward (and every recomputation) is the FP32 stage kernel; the VJP
+// is the same interface derivative evaluated in FP32 (swe_adjoint_math.cuh is templated
+// on the scalar), with the state variable eta = h + B instead of h: the interface reads
+// eta directly (so its eta adjoint goes to eta alone, not to B), a positivity clamp
+// (eta = B + floor) passes the output adjoint to B, the gauge residual h = eta - B feeds
+// both, and the stage-3 weights are the FP32 kernel's n + c (s' - n) with c = fl(2/3).
+// At the end dJ/dh0 = dJ/deta0 and dJ/dB (h0 fixed) = the B adjoint + dJ/deta0.  Ghost
+// beds must repeat the interior (as the reference's boundary conditions leave them), so
+// that a ghost's eta is its source cell's.
 //
 // Objective: J = sum over steps n = 1..N and gauge cells g of (h^n_g - h_obs^n_g)^2,
 // fixed dt.  Gradients: dJ/dh^0, dJ/dhu^0, dJ/dhv^0 and dJ/dB (initial state held fixed).
@@ -22,6 +33,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "swe_adjoint_math.cuh"
@@ -36,31 +48,48 @@ constexpr int AFT = 128;  // threads per block of the interface pass
 constexpr int AGT = 256;  // threads per block of the gather pass
 constexpr int NC = 14;    // contributions per interface: eta(4), qn(4), qt(4), bm, bp
 
+// T = double: FP64 scheme, state (h, hu, hv); T = float: FP32-mixed, state (eta, hu, hv).
+template <class T>
 struct AdjParams {
-    const double *h, *hu, *hv, *B;       // stage source state, bathymetry
-    const double *lo_h, *lo_hu, *lo_hv;  // adjoint of the stage output
-    const unsigned char *mask;           // positivity clamps of this stage
-    double *ls_h, *ls_hu, *ls_hv;        // adjoint of the stage source (written)
-    double *ln_h, *ln_hu, *ln_hv;        // adjoint of U^n (stage 3 writes, 2 adds, 1 reads)
-    double *gB;                          // dJ/dB (accumulated)
-    double *cx, *cy;                     // interface contributions, NC planes each
-    long long px, py;                    // plane sizes: (Nx + 1) * Ny, Nx * (Ny + 1)
+    const T *h, *hu, *hv, *B;       // stage source state, bathymetry
+    const T *lo_h, *lo_hu, *lo_hv;  // adjoint of the stage output
+    const unsigned char *mask;      // positivity clamps of this stage
+    T *ls_h, *ls_hu, *ls_hv;        // adjoint of the stage source (written)
+    T *ln_h, *ln_hu, *ln_hv;        // adjoint of U^n (stage 3 writes, 2 adds, 1 reads)
+    T *gB;                          // dJ/dB (accumulated)
+    T *cx, *cy;                     // interface contributions, NC planes each
+    long long px, py;               // plane sizes: (Nx + 1) * Ny, Nx * (Ny + 1)
     int Nx, Ny;
     long long pitch;
     int bc;
-    double inv_dx, inv_dy, g, dt;
+    T inv_dx, inv_dy, g, dt;
 };
+
+template <class T>
+__host__ __device__ constexpr bool eta_state() { return std::is_same<T, float>::value; }
+
+// Weight of the stage source in the stage output, and of U^n in stage 3: the FP64
+// kernel's (1.0 / 3.0) U^n + (2.0 / 3.0) (...), the FP32 kernel's n + c (s' - n).
+template <class T, int STAGE>
+__device__ __forceinline__ T src_weight() {
+    if (STAGE == 1) return T(1);
+    if (STAGE == 2) return T(0.25);
+    return eta_state<T>() ? T(2.f / 3.f) : T(2.0 / 3.0);
+}
+template <class T>
+__device__ __forceinline__ T n_weight3() {
+    return eta_state<T>() ? T(1.f - 2.f / 3.f) : T(1.0 / 3.0);
+}
 
 // Adjoint of the divergence at interior cell (i, j): cs * dt * lo, zero where the stage
 // clamped the depth (its output did not depend on the fluxes there) and outside.
-template <int STAGE>
-__device__ __forceinline__ void w_at(const AdjParams &a, int i, int j, double w[3]) {
-    constexpr double cs = STAGE == 1 ? 1.0 : (STAGE == 2 ? 0.25 : 2.0 / 3.0);
-    w[0] = w[1] = w[2] = 0.0;
+template <class T, int STAGE>
+__device__ __forceinline__ void w_at(const AdjParams<T> &a, int i, int j, T w[3]) {
+    w[0] = w[1] = w[2] = T(0);
     if (i < 0 || i >= a.Nx || j < 0 || j >= a.Ny) return;
     const long long k = (long long)(i + NG) * a.pitch + (j + NG);
     if (a.mask[k]) return;
-    const double f = cs * a.dt;
+    const T f = src_weight<T, STAGE>() * a.dt;
     w[0] = f * a.lo_h[k];
     w[1] = f * a.lo_hu[k];
     w[2] = f * a.lo_hv[k];
@@ -71,15 +100,15 @@ __device__ __forceinline__ void w_at(const AdjParams &a, int i, int j, double w[
 // row i.  The stencil is staged exactly as the forward kernel stages it: the state of
 // ghost cells from the mirrored (reflecting, normal momentum negated) or clamped
 // (transmissive) interior cell, B where it lies, ghosts included.
-template <int STAGE, int DIR>
-__global__ void __launch_bounds__(AFT) k_adj_faces(const AdjParams a) {
+template <class T, int STAGE, int DIR>
+__global__ void __launch_bounds__(AFT) k_adj_faces(const AdjParams<T> a) {
     const int t = blockIdx.x * AFT + threadIdx.x;
     const int along = DIR == 0 ? a.Ny : a.Ny + 1;  // contiguous index range
     if (t >= along) return;
     const int f = DIR == 0 ? (int)blockIdx.y - 1 : t - 1;  // interface index
     const int o = DIR == 0 ? t : (int)blockIdx.y;          // the other coordinate
     const long long P = a.pitch;
-    adj::FaceIn<double> in;
+    adj::FaceIn<T> in;
     for (int q = 0; q < 4; ++q) {
         const int c = f - 1 + q;  // stencil cell along the normal
         bool fl;
@@ -88,32 +117,37 @@ __global__ void __launch_bounds__(AFT) k_adj_faces(const AdjParams a) {
                                       : (long long)(o + NG) * P + (m + NG);
         const int cb = clamp_int(c + NG, 0, (DIR == 0 ? a.Nx : a.Ny) + 3);
         const long long kb = DIR == 0 ? (long long)cb * P + (o + NG) : (long long)(o + NG) * P + cb;
-        const double b = a.B[kb];
-        const double qn = DIR == 0 ? a.hu[ks] : a.hv[ks];
-        in.e[q] = a.h[ks] + b;
+        const T b = a.B[kb];
+        const T qn = DIR == 0 ? a.hu[ks] : a.hv[ks];
+        if (eta_state<T>()) {  // the FP32 kernel's ghost: its source's depth over its own bed
+            const T bs = a.B[ks], e = a.h[ks];
+            in.e[q] = (b == bs) ? e : (e - bs) + b;
+        } else {
+            in.e[q] = a.h[ks] + b;
+        }
         in.n[q] = fl ? -qn : qn;
         in.t[q] = DIR == 0 ? a.hv[ks] : a.hu[ks];
         if (q == 1) in.bm = b;
         if (q == 2) in.bp = b;
     }
-    double wm[3], wp[3];
+    T wm[3], wp[3];
     if (DIR == 0) {
-        w_at<STAGE>(a, f, o, wm);
-        w_at<STAGE>(a, f + 1, o, wp);
+        w_at<T, STAGE>(a, f, o, wm);
+        w_at<T, STAGE>(a, f + 1, o, wp);
     } else {
-        w_at<STAGE>(a, o, f, wm);
-        w_at<STAGE>(a, o, f + 1, wp);
+        w_at<T, STAGE>(a, o, f, wm);
+        w_at<T, STAGE>(a, o, f + 1, wp);
     }
-    const double inv = DIR == 0 ? a.inv_dx : a.inv_dy;
+    const T inv = DIR == 0 ? a.inv_dx : a.inv_dy;
     const int n = DIR == 0 ? 1 : 2, tg = DIR == 0 ? 2 : 1;  // normal / tangential field
-    adj::FaceOut<double> d;
+    adj::FaceOut<T> d;
     d.fh = inv * (wp[0] - wm[0]);
     d.fqt = inv * (wp[tg] - wm[tg]);
     d.fqn_m = -inv * wm[n];
     d.fqn_p = inv * wp[n];
-    adj::FaceIn<double> ad;
-    adj::face_vjp(in, a.g, EPS, d, ad);
-    double *C = DIR == 0 ? a.cx : a.cy;
+    adj::FaceIn<T> ad;
+    adj::face_vjp(in, a.g, T(EPS), d, ad);
+    T *C = DIR == 0 ? a.cx : a.cy;
     const long long pl = DIR == 0 ? a.px : a.py;
     const long long idx = DIR == 0 ? (long long)(f + 1) * a.Ny + o : (long long)o * (a.Ny + 1) + (f + 1);
     for (int q = 0; q < 4; ++q) {
@@ -159,11 +193,11 @@ __device__ __forceinline__ int virtual_coords(int a, int N, int bc, int *v, bool
 
 // Sums, for interior cell a along one direction (rows for DIR 0, columns for DIR 1), the
 // contributions of the interfaces whose stencil holds a or a ghost copy of it.
-template <int DIR>
-__device__ __forceinline__ void gather_dir(const AdjParams &a, int ca, int other, double &acc_h,
-                                           double &acc_qn, double &acc_qt, double &acc_B) {
+template <class T, int DIR>
+__device__ __forceinline__ void gather_dir(const AdjParams<T> &a, int ca, int other, T &acc_h,
+                                           T &acc_qn, T &acc_qt, T &acc_B) {
     const int N = DIR == 0 ? a.Nx : a.Ny;
-    const double *C = DIR == 0 ? a.cx : a.cy;
+    const T *C = DIR == 0 ? a.cx : a.cy;
     const long long pl = DIR == 0 ? a.px : a.py;
     auto at = [&](int f) {  // linear index of interface f (valid range [-1, N - 1])
         return DIR == 0 ? (long long)(f + 1) * a.Ny + other : (long long)other * (a.Ny + 1) + (f + 1);
@@ -176,9 +210,9 @@ __device__ __forceinline__ void gather_dir(const AdjParams &a, int ca, int other
             const int f = v[q] + 1 - k;  // interface whose stencil slot k is cell v
             if (f < -1 || f > N - 1) continue;
             const long long x = at(f);
-            const double ce = C[k * pl + x], cn = C[(4 + k) * pl + x];
+            const T ce = C[k * pl + x], cn = C[(4 + k) * pl + x];
             acc_h += ce;
-            acc_B += ce;
+            if (!eta_state<T>()) acc_B += ce;  // eta = h + B read at the interface
             acc_qn += fl[q] ? -cn : cn;
             acc_qt += C[(8 + k) * pl + x];
         }
@@ -189,26 +223,29 @@ __device__ __forceinline__ void gather_dir(const AdjParams &a, int ca, int other
 }
 
 // Per interior cell: adjoint of the stage source and of U^n, and dJ/dB.
-template <int STAGE>
-__global__ void __launch_bounds__(AGT) k_adj_gather(const AdjParams a) {
+template <class T, int STAGE>
+__global__ void __launch_bounds__(AGT) k_adj_gather(const AdjParams<T> a) {
     const int cj = blockIdx.x * AGT + threadIdx.x, ci = blockIdx.y;
     if (cj >= a.Ny) return;
-    constexpr double cs = STAGE == 1 ? 1.0 : (STAGE == 2 ? 0.25 : 2.0 / 3.0);
-    double acc_h = 0.0, acc_hu = 0.0, acc_hv = 0.0, acc_B = 0.0;
-    gather_dir<0>(a, ci, cj, acc_h, acc_hu, acc_hv, acc_B);
-    gather_dir<1>(a, cj, ci, acc_h, acc_hv, acc_hu, acc_B);
+    const T cs = src_weight<T, STAGE>();
+    T acc_h = T(0), acc_hu = T(0), acc_hv = T(0), acc_B = T(0);
+    gather_dir<T, 0>(a, ci, cj, acc_h, acc_hu, acc_hv, acc_B);
+    gather_dir<T, 1>(a, cj, ci, acc_h, acc_hv, acc_hu, acc_B);
     const long long k = (long long)(ci + NG) * a.pitch + (cj + NG);
     const bool m = a.mask[k];
-    const double l0 = m ? 0.0 : a.lo_h[k], l1 = m ? 0.0 : a.lo_hu[k], l2 = m ? 0.0 : a.lo_hv[k];
-    double o0 = acc_h + cs * l0, o1 = acc_hu + cs * l1, o2 = acc_hv + cs * l2;
-    if (STAGE == 3) {  // the forward's (1.0 / 3.0) * U^n
-        a.ln_h[k] = (1.0 / 3.0) * l0;
-        a.ln_hu[k] = (1.0 / 3.0) * l1;
-        a.ln_hv[k] = (1.0 / 3.0) * l2;
+    // a clamped FP32 cell is eta = B + floor: its eta adjoint goes to B
+    if (eta_state<T>() && m) acc_B += a.lo_h[k];
+    const T l0 = m ? T(0) : a.lo_h[k], l1 = m ? T(0) : a.lo_hu[k], l2 = m ? T(0) : a.lo_hv[k];
+    T o0 = acc_h + cs * l0, o1 = acc_hu + cs * l1, o2 = acc_hv + cs * l2;
+    if (STAGE == 3) {  // the forward's weight of U^n
+        const T wn = n_weight3<T>();
+        a.ln_h[k] = wn * l0;
+        a.ln_hu[k] = wn * l1;
+        a.ln_hv[k] = wn * l2;
     } else if (STAGE == 2) {
-        a.ln_h[k] += 0.75 * l0;
-        a.ln_hu[k] += 0.75 * l1;
-        a.ln_hv[k] += 0.75 * l2;
+        a.ln_h[k] += T(0.75) * l0;
+        a.ln_hu[k] += T(0.75) * l1;
+        a.ln_hv[k] += T(0.75) * l2;
     } else {
         o0 += a.ln_h[k];
         o1 += a.ln_hu[k];
@@ -222,29 +259,47 @@ __global__ void __launch_bounds__(AGT) k_adj_gather(const AdjParams a) {
 
 // Gauge source of one step: lambda_h[g] += 2 (h_g - obs_g), J += sum (h_g - obs_g)^2,
 // one thread in gauge order (deterministic, duplicates allowed).
-__global__ void k_gauge(const double *h, long long P, const int *gi, const int *gj, int ng,
-                        const double *obs, double *lam_h, double *J) {
+// FP32-mixed: h = eta - B in FP64, lambda_eta += 2 (h - obs) and lambda_B -= 2 (h - obs).
+template <class T>
+__global__ void k_gauge(const T *h, const T *B, long long P, const int *gi, const int *gj,
+                        int ng, const double *obs, T *lam_h, T *gB, double *J) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     double s = 0.0;
     for (int q = 0; q < ng; ++q) {
         const long long k = (long long)(gi[q] + NG) * P + (gj[q] + NG);
-        const double r = h[k] - obs[q];
+        const double hk = eta_state<T>() ? (double)h[k] - (double)B[k] : (double)h[k];
+        const double r = hk - obs[q];
         s += r * r;
-        lam_h[k] += 2.0 * r;
+        lam_h[k] += (T)(2.0 * r);
+        if (eta_state<T>()) gB[k] -= (T)(2.0 * r);
     }
     *J += s;
 }
 
+// dJ/dB with h0 held fixed, widened: B adjoint + the eta0 adjoint (FP32-mixed).
+__global__ void k_grad_b_f32(const float *gB, const float *lam_e, double *out, size_t n) {
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
+         t += (size_t)gridDim.x * blockDim.x)
+        out[t] = (double)gB[t] + (double)lam_e[t];
+}
+
+__global__ void k_widen(const float *src, double *out, size_t n) {
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n;
+         t += (size_t)gridDim.x * blockDim.x)
+        out[t] = (double)src[t];
+}
+
+template <class T>
 struct Adj {
     swe_ctx *c;
     size_t fe;  // elements per field
-    double *snap;
+    T *snap;
     int S;
-    double *W[3], *Un1[3], *lam[3], *lamA[3], *lamB[3], *ln[3], *gB;
-    double *cx, *cy;  // interface contributions of the stage being reversed
-    bool tape = false;              // every state and every step's stage states kept
-    double *tU1 = nullptr, *tU2 = nullptr;  // tape: U^(1), U^(2) of step k at 3 k fields
-    unsigned char *tmask = nullptr;         // tape: clamp masks of step k at 3 k fields
+    T *W[3], *Un1[3], *lam[3], *lamA[3], *lamB[3], *ln[3], *gB;
+    T *cx, *cy;  // interface contributions of the stage being reversed
+    bool tape = false;            // every state and every step's stage states kept
+    T *tU1 = nullptr, *tU2 = nullptr;  // tape: U^(1), U^(2) of step k at 3 k fields
+    unsigned char *tmask = nullptr;    // tape: clamp masks of step k at 3 k fields
     unsigned char *mask[3];
     int *gi, *gj;
     double *obs, *J;
@@ -261,7 +316,8 @@ struct Adj {
         if (e_ != cudaSuccess) return e_;          \
     } while (0)
 
-StageParams fwd_params(const Adj &A) {
+template <class T>
+StageParams fwd_params(const Adj<T> &A) {
     const swe_ctx *c = A.c;
     StageParams sp{};
     sp.B = c->B;
@@ -275,6 +331,10 @@ StageParams fwd_params(const Adj &A) {
     sp.ky = pow2_exponent(c->inv_dy);
     sp.g = c->p.g;
     sp.half_g = 0.5 * c->p.g;
+    sp.gf = (float)sp.g;
+    sp.half_gf = (float)sp.half_g;
+    sp.inv_dxf = (float)sp.inv_dx;
+    sp.inv_dyf = (float)sp.inv_dy;
     sp.cfl_min_dxdy = c->cfl_min_dxdy;
     sp.dt_fixed = A.dt;
     sp.speed = A.speed;  // scratch slots: the context's adaptive-dt slots stay untouched
@@ -284,45 +344,61 @@ StageParams fwd_params(const Adj &A) {
     return sp;
 }
 
+template <class T>
+cudaError_t launch_fwd_stage(int stage, const StageParams &sp, cudaStream_t s) {
+    if (eta_state<T>()) return launch_stage_f32(stage, sp, nullptr, s);
+    return launch_stage_f64(stage, sp, nullptr, s);
+}
+
 // One forward step W -> out (out may be W) with the stage states in U1, U2 and the
 // clamp masks in mk[0..2] (null: not kept).
-cudaError_t forward_step_into(Adj &A, double *const *W, double *const *out, double *const *U1,
-                              double *const *U2, unsigned char *const *mk) {
+template <class T>
+cudaError_t forward_step_into(Adj<T> &A, T *const *W, T *const *out, T *const *U1,
+                              T *const *U2, unsigned char *const *mk) {
     swe_ctx *c = A.c;
     StageParams sp = fwd_params(A);
     sp.hn = W[0]; sp.hun = W[1]; sp.hvn = W[2];
     sp.hs = W[0]; sp.hus = W[1]; sp.hvs = W[2];
     sp.ho = U1[0]; sp.huo = U1[1]; sp.hvo = U1[2];
     sp.mask = mk[0];
-    ACK(launch_stage_f64(1, sp, nullptr, c->stream));
+    ACK(launch_fwd_stage<T>(1, sp, c->stream));
     sp.hs = U1[0]; sp.hus = U1[1]; sp.hvs = U1[2];
     sp.ho = U2[0]; sp.huo = U2[1]; sp.hvo = U2[2];
     sp.mask = mk[1];
-    ACK(launch_stage_f64(2, sp, nullptr, c->stream));
+    ACK(launch_fwd_stage<T>(2, sp, c->stream));
     sp.hs = U2[0]; sp.hus = U2[1]; sp.hvs = U2[2];
     sp.ho = out[0]; sp.huo = out[1]; sp.hvo = out[2];
     sp.mask = mk[2];
-    ACK(launch_stage_f64(3, sp, nullptr, c->stream));
+    ACK(launch_fwd_stage<T>(3, sp, c->stream));
     c->launches += 3;
     ++A.fwd_steps;
     return cudaSuccess;
 }
 
+template <class T>
+void ctx_stage_buffers(const swe_ctx *c, T **U1, T **U2) {
+    for (int f = 0; f < 3; ++f) {
+        U1[f] = static_cast<T *>(c->U1[f]);
+        U2[f] = static_cast<T *>(c->U2[f]);
+    }
+}
+
 // One forward step W -> out through the context's stage buffers; masks optional.
-cudaError_t forward_step(Adj &A, double *const *W, double *const *out, bool masks) {
-    swe_ctx *c = A.c;
-    double *U1[3] = {(double *)c->U1[0], (double *)c->U1[1], (double *)c->U1[2]};
-    double *U2[3] = {(double *)c->U2[0], (double *)c->U2[1], (double *)c->U2[2]};
+template <class T>
+cudaError_t forward_step(Adj<T> &A, T *const *W, T *const *out, bool masks) {
+    T *U1[3], *U2[3];
+    ctx_stage_buffers(A.c, U1, U2);
     unsigned char *none[3] = {nullptr, nullptr, nullptr};
     return forward_step_into(A, W, out, U1, U2, masks ? A.mask : none);
 }
 
-cudaError_t launch_adj(Adj &A, int stage, double *const *state, double *const *lo,
-                       const unsigned char *mask, double *const *ls) {
+template <class T>
+cudaError_t launch_adj(Adj<T> &A, int stage, T *const *state, T *const *lo,
+                       const unsigned char *mask, T *const *ls) {
     swe_ctx *c = A.c;
-    AdjParams p{};
+    AdjParams<T> p{};
     p.h = state[0]; p.hu = state[1]; p.hv = state[2];
-    p.B = (const double *)c->B;
+    p.B = static_cast<const T *>(c->B);
     p.lo_h = lo[0]; p.lo_hu = lo[1]; p.lo_hv = lo[2];
     p.mask = mask;
     p.ls_h = ls[0]; p.ls_hu = ls[1]; p.ls_hv = ls[2];
@@ -332,10 +408,10 @@ cudaError_t launch_adj(Adj &A, int stage, double *const *state, double *const *l
     p.Ny = c->p.Ny;
     p.pitch = c->pitch;
     p.bc = c->p.bc;
-    p.inv_dx = c->inv_dx;
-    p.inv_dy = c->inv_dy;
-    p.g = c->p.g;
-    p.dt = A.dt;
+    p.inv_dx = (T)c->inv_dx;
+    p.inv_dy = (T)c->inv_dy;
+    p.g = (T)c->p.g;
+    p.dt = (T)A.dt;
     p.cx = A.cx;
     p.cy = A.cy;
     p.px = (long long)(c->p.Nx + 1) * c->p.Ny;
@@ -344,19 +420,19 @@ cudaError_t launch_adj(Adj &A, int stage, double *const *state, double *const *l
     const dim3 gg((c->p.Ny + AGT - 1) / AGT, c->p.Nx);
     switch (stage) {
         case 1:
-            k_adj_faces<1, 0><<<gx, AFT, 0, c->stream>>>(p);
-            k_adj_faces<1, 1><<<gy, AFT, 0, c->stream>>>(p);
-            k_adj_gather<1><<<gg, AGT, 0, c->stream>>>(p);
+            k_adj_faces<T, 1, 0><<<gx, AFT, 0, c->stream>>>(p);
+            k_adj_faces<T, 1, 1><<<gy, AFT, 0, c->stream>>>(p);
+            k_adj_gather<T, 1><<<gg, AGT, 0, c->stream>>>(p);
             break;
         case 2:
-            k_adj_faces<2, 0><<<gx, AFT, 0, c->stream>>>(p);
-            k_adj_faces<2, 1><<<gy, AFT, 0, c->stream>>>(p);
-            k_adj_gather<2><<<gg, AGT, 0, c->stream>>>(p);
+            k_adj_faces<T, 2, 0><<<gx, AFT, 0, c->stream>>>(p);
+            k_adj_faces<T, 2, 1><<<gy, AFT, 0, c->stream>>>(p);
+            k_adj_gather<T, 2><<<gg, AGT, 0, c->stream>>>(p);
             break;
         default:
-            k_adj_faces<3, 0><<<gx, AFT, 0, c->stream>>>(p);
-            k_adj_faces<3, 1><<<gy, AFT, 0, c->stream>>>(p);
-            k_adj_gather<3><<<gg, AGT, 0, c->stream>>>(p);
+            k_adj_faces<T, 3, 0><<<gx, AFT, 0, c->stream>>>(p);
+            k_adj_faces<T, 3, 1><<<gy, AFT, 0, c->stream>>>(p);
+            k_adj_gather<T, 3><<<gg, AGT, 0, c->stream>>>(p);
             break;
     }
     c->launches += 2;
@@ -364,49 +440,60 @@ cudaError_t launch_adj(Adj &A, int stage, double *const *state, double *const *l
     return cudaGetLastError();
 }
 
-// Adjoint of step k (W holds U^k; lam holds the adjoint of U^(k+1) before its source).
-cudaError_t adjoint_step(Adj &A, int k) {
+template <class T>
+cudaError_t gauge_source(Adj<T> &A, const T *h, int k) {
     swe_ctx *c = A.c;
-    ACK(forward_step(A, A.W, A.Un1, true));
-    double *U1[3] = {(double *)c->U1[0], (double *)c->U1[1], (double *)c->U1[2]};
-    double *U2[3] = {(double *)c->U2[0], (double *)c->U2[1], (double *)c->U2[2]};
-    k_gauge<<<1, 32, 0, c->stream>>>(A.Un1[0], c->pitch, A.gi, A.gj, A.ng,
-                                     A.obs + (size_t)k * A.ng, A.lam[0], A.J);
+    k_gauge<T><<<1, 32, 0, c->stream>>>(h, static_cast<const T *>(c->B), c->pitch, A.gi, A.gj,
+                                        A.ng, A.obs + (size_t)k * A.ng, A.lam[0], A.gB, A.J);
     ++c->launches;
-    ACK(cudaGetLastError());
+    return cudaGetLastError();
+}
+
+// Adjoint of step k (W holds U^k; lam holds the adjoint of U^(k+1) before its source).
+template <class T>
+cudaError_t adjoint_step(Adj<T> &A, int k) {
+    ACK(forward_step(A, A.W, A.Un1, true));
+    T *U1[3], *U2[3];
+    ctx_stage_buffers(A.c, U1, U2);
+    ACK(gauge_source(A, A.Un1[0], k));
     ACK(launch_adj(A, 3, U2, A.lam, A.mask[2], A.lamA));
     ACK(launch_adj(A, 2, U1, A.lamA, A.mask[1], A.lamB));
     ACK(launch_adj(A, 1, A.W, A.lamB, A.mask[0], A.lam));
     return cudaSuccess;
 }
 
-cudaError_t copy_state(Adj &A, double *const *dst, double *const *src) {
+template <class T>
+cudaError_t copy_state(Adj<T> &A, T *const *dst, T *const *src) {
     for (int f = 0; f < 3; ++f)
-        ACK(cudaMemcpyAsync(dst[f], src[f], A.fe * sizeof(double), cudaMemcpyDeviceToDevice,
+        ACK(cudaMemcpyAsync(dst[f], src[f], A.fe * sizeof(T), cudaMemcpyDeviceToDevice,
                             A.c->stream));
     return cudaSuccess;
 }
 
-double *slot_field(Adj &A, int slot, int f) { return A.snap + ((size_t)slot * 3 + f) * A.fe; }
+template <class T>
+T *slot_field(Adj<T> &A, int slot, int f) { return A.snap + ((size_t)slot * 3 + f) * A.fe; }
 
-cudaError_t load_slot(Adj &A, int slot) {
-    double *src[3] = {slot_field(A, slot, 0), slot_field(A, slot, 1), slot_field(A, slot, 2)};
+template <class T>
+cudaError_t load_slot(Adj<T> &A, int slot) {
+    T *src[3] = {slot_field(A, slot, 0), slot_field(A, slot, 1), slot_field(A, slot, 2)};
     return copy_state(A, A.W, src);
 }
 
-cudaError_t store_slot(Adj &A, int slot) {
-    double *dst[3] = {slot_field(A, slot, 0), slot_field(A, slot, 1), slot_field(A, slot, 2)};
+template <class T>
+cudaError_t store_slot(Adj<T> &A, int slot) {
+    T *dst[3] = {slot_field(A, slot, 0), slot_field(A, slot, 1), slot_field(A, slot, 2)};
     return copy_state(A, dst, A.W);
 }
 
-double *tape_field(double *base, Adj &A, int k, int f) { return base + ((size_t)k * 3 + f) * A.fe; }
+template <class T>
+T *tape_field(T *base, Adj<T> &A, int k, int f) { return base + ((size_t)k * 3 + f) * A.fe; }
 
 // Tape mode: one forward sweep keeps U^k in slot k and the stage states and clamp masks
 // of step k in the tape; the reverse sweep then recomputes nothing.
-cudaError_t taped(Adj &A, int n) {
-    swe_ctx *c = A.c;
+template <class T>
+cudaError_t taped(Adj<T> &A, int n) {
     for (int k = 0; k < n; ++k) {
-        double *W[3], *out[3], *U1[3], *U2[3];
+        T *W[3], *out[3], *U1[3], *U2[3];
         unsigned char *mk[3];
         for (int f = 0; f < 3; ++f) {
             W[f] = slot_field(A, k, f);
@@ -418,7 +505,7 @@ cudaError_t taped(Adj &A, int n) {
         ACK(forward_step_into(A, W, out, U1, U2, mk));
     }
     for (int k = n - 1; k >= 0; --k) {
-        double *Wk[3], *U1[3], *U2[3];
+        T *Wk[3], *U1[3], *U2[3];
         const unsigned char *mk[3];
         for (int f = 0; f < 3; ++f) {
             Wk[f] = slot_field(A, k, f);
@@ -426,10 +513,7 @@ cudaError_t taped(Adj &A, int n) {
             U2[f] = tape_field(A.tU2, A, k, f);
             mk[f] = A.tmask + ((size_t)k * 3 + f) * A.fe;
         }
-        k_gauge<<<1, 32, 0, c->stream>>>(slot_field(A, k + 1, 0), c->pitch, A.gi, A.gj, A.ng,
-                                         A.obs + (size_t)k * A.ng, A.lam[0], A.J);
-        ++c->launches;
-        ACK(cudaGetLastError());
+        ACK(gauge_source(A, slot_field(A, k + 1, 0), k));
         ACK(launch_adj(A, 3, U2, A.lam, mk[2], A.lamA));
         ACK(launch_adj(A, 2, U1, A.lamA, mk[1], A.lamB));
         ACK(launch_adj(A, 1, Wk, A.lamB, mk[0], A.lam));
@@ -438,7 +522,8 @@ cudaError_t taped(Adj &A, int n) {
 }
 
 // Adjoint of steps [l, l+n) with U^l in `slot` and s free snapshot slots.
-cudaError_t reverse(Adj &A, int l, int n, int slot, int s) {
+template <class T>
+cudaError_t reverse(Adj<T> &A, int l, int n, int slot, int s) {
     while (true) {
         if (n == 1) {
             ACK(load_slot(A, slot));
@@ -463,7 +548,8 @@ cudaError_t reverse(Adj &A, int l, int n, int slot, int s) {
 
 // split[n][s] minimising F(n, s) = m + F(n - m, s - 1) + F(m, s); F(1, s) = 0,
 // F(n, 0) = n (n - 1) / 2.  With s >= n - 1, storing every state (m = 1) is optimal.
-void build_schedule(Adj &A, int N, int S) {
+template <class T>
+void build_schedule(Adj<T> &A, int N, int S) {
     A.split.assign(N + 1, std::vector<int>(S + 1, 1));
     std::vector<std::vector<long long>> F(N + 1, std::vector<long long>(S + 1, 0));
     for (int n = 2; n <= N; ++n) {
@@ -492,50 +578,25 @@ void build_schedule(Adj &A, int N, int S) {
     }
 }
 
-}  // namespace
-}  // namespace swe
-
-using namespace swe;
-
-extern "C" int swe_adjoint_gauge(swe_ctx *c, int n_steps, double dt, int n_gauges,
-                                 const int *gauge_i, const int *gauge_j, const double *h_obs,
-                                 int n_snapshots, double *J, double *grad_h, double *grad_hu,
-                                 double *grad_hv, double *grad_B, double *ms) {
-    if (!c) return SWE_ERR_BAD_ARG;
-    if (!c->uploaded || c->p.precision != SWE_PRECISION_FP64 || n_steps < 1 || !(dt > 0.0) ||
-        n_gauges < 0 || (n_gauges > 0 && (!gauge_i || !gauge_j || !h_obs)) ||
-        (n_snapshots < 0 && n_snapshots != SWE_ADJ_TAPE_ALL) ||
-        !J || !grad_h || !grad_hu || !grad_hv || !grad_B) {
-        c->err = "swe_adjoint_gauge: bad argument (needs an uploaded FP64 context)";
-        return SWE_ERR_BAD_ARG;
-    }
-    if (c->p.x_halo_lo || c->p.x_halo_hi) {
-        c->err = "swe_adjoint_gauge: not available on slab contexts";
-        return SWE_ERR_UNSUPPORTED;
-    }
-    if (c->p.scheme != SWE_SCHEME_FUSED) {
-        c->err = "swe_adjoint_gauge: the adjoint is of the fused scheme";
-        return SWE_ERR_UNSUPPORTED;
-    }
-    for (int q = 0; q < n_gauges; ++q)
-        if (gauge_i[q] < 0 || gauge_i[q] >= c->p.Nx || gauge_j[q] < 0 || gauge_j[q] >= c->p.Ny) {
-            c->err = "swe_adjoint_gauge: gauge outside the interior";
-            return SWE_ERR_BAD_ARG;
-        }
-    if (cudaSetDevice(c->p.device) != cudaSuccess) return SWE_ERR_CUDA;
-    Adj A;
+// The whole adjoint on a context whose state is of type T.
+template <class T>
+int run_adjoint(swe_ctx *c, int n_steps, double dt, int n_gauges, const int *gauge_i,
+                const int *gauge_j, const double *h_obs, int n_snapshots, double *J,
+                double *grad_h, double *grad_hu, double *grad_hv, double *grad_B, double *ms) {
+    Adj<T> A;
     A.c = c;
     A.fe = c->field_elems;
     A.tape = n_snapshots == SWE_ADJ_TAPE_ALL;
     A.S = A.tape ? n_steps : std::min(n_snapshots, n_steps);
     A.ng = n_gauges;
     A.dt = dt;
-    const size_t fb = A.fe * sizeof(double);
+    const size_t fb = A.fe * sizeof(T);
     auto rounded = [](size_t n) { return (n + 255) / 256 * 256; };
-    const size_t cx_bytes = (size_t)NC * (c->p.Nx + 1) * c->p.Ny * sizeof(double);
-    const size_t cy_bytes = (size_t)NC * c->p.Nx * (c->p.Ny + 1) * sizeof(double);
+    const size_t cx_bytes = (size_t)NC * (c->p.Nx + 1) * c->p.Ny * sizeof(T);
+    const size_t cy_bytes = (size_t)NC * c->p.Nx * (c->p.Ny + 1) * sizeof(T);
+    const size_t wide = eta_state<T>() ? rounded(A.fe * sizeof(double)) : 0;  // output staging
     const size_t bytes = rounded((size_t)(A.S + 1) * 3 * fb) + 19 * rounded(fb) + 3 * rounded(A.fe) +
-                         rounded(cx_bytes) + rounded(cy_bytes) +
+                         rounded(cx_bytes) + rounded(cy_bytes) + wide +
                          (A.tape ? 2 * rounded((size_t)n_steps * 3 * fb) +
                                        rounded((size_t)n_steps * 3 * A.fe)
                                  : 0) +
@@ -559,22 +620,23 @@ extern "C" int swe_adjoint_gauge(swe_ctx *c, int n_steps, double dt, int n_gauge
         p += (n + 255) / 256 * 256;
         return q;
     };
-    A.snap = (double *)take((size_t)(A.S + 1) * 3 * fb);
+    A.snap = (T *)take((size_t)(A.S + 1) * 3 * fb);
     for (int f = 0; f < 3; ++f) {
-        A.W[f] = (double *)take(fb);
-        A.Un1[f] = (double *)take(fb);
-        A.lam[f] = (double *)take(fb);
-        A.lamA[f] = (double *)take(fb);
-        A.lamB[f] = (double *)take(fb);
-        A.ln[f] = (double *)take(fb);
+        A.W[f] = (T *)take(fb);
+        A.Un1[f] = (T *)take(fb);
+        A.lam[f] = (T *)take(fb);
+        A.lamA[f] = (T *)take(fb);
+        A.lamB[f] = (T *)take(fb);
+        A.ln[f] = (T *)take(fb);
         A.mask[f] = (unsigned char *)take(A.fe);
     }
-    A.gB = (double *)take(fb);
-    A.cx = (double *)take(cx_bytes);
-    A.cy = (double *)take(cy_bytes);
+    A.gB = (T *)take(fb);
+    A.cx = (T *)take(cx_bytes);
+    A.cy = (T *)take(cy_bytes);
+    double *widened = wide ? (double *)take(A.fe * sizeof(double)) : nullptr;
     if (A.tape) {
-        A.tU1 = (double *)take((size_t)n_steps * 3 * fb);
-        A.tU2 = (double *)take((size_t)n_steps * 3 * fb);
+        A.tU1 = (T *)take((size_t)n_steps * 3 * fb);
+        A.tU2 = (T *)take((size_t)n_steps * 3 * fb);
         A.tmask = (unsigned char *)take((size_t)n_steps * 3 * A.fe);
     }
     A.gi = (int *)take(sizeof(int) * (n_gauges + 1));
@@ -597,7 +659,7 @@ extern "C" int swe_adjoint_gauge(swe_ctx *c, int n_steps, double dt, int n_gauge
                                 cudaMemcpyHostToDevice, st);
     }
     // slot 0 = U^0 (the context's state, left unchanged)
-    double *Un[3] = {(double *)c->Un[0], (double *)c->Un[1], (double *)c->Un[2]};
+    T *Un[3] = {static_cast<T *>(c->Un[0]), static_cast<T *>(c->Un[1]), static_cast<T *>(c->Un[2])};
     if (e == cudaSuccess) e = copy_state(A, A.W, Un);
     if (e == cudaSuccess) e = store_slot(A, 0);
     if (e != cudaSuccess) return fail(e);
@@ -612,10 +674,28 @@ extern "C" int swe_adjoint_gauge(swe_ctx *c, int n_steps, double dt, int n_gauge
     if (e == cudaSuccess) e = cudaMemcpyAsync(&flags, c->flags, sizeof(int), cudaMemcpyDeviceToHost, st);
     const size_t row = (size_t)(c->p.Ny + 4) * sizeof(double), dp = (size_t)c->pitch * sizeof(double);
     double *outs[4] = {grad_h, grad_hu, grad_hv, grad_B};
-    double *srcs[4] = {A.lam[0], A.lam[1], A.lam[2], A.gB};
-    for (int f = 0; f < 4 && e == cudaSuccess; ++f)
-        e = cudaMemcpy2DAsync(outs[f], row, srcs[f], dp, row, (size_t)(c->p.Nx + 4),
-                              cudaMemcpyDeviceToHost, st);
+    for (int f = 0; f < 4 && e == cudaSuccess; ++f) {
+        const double *src;
+        if (eta_state<T>()) {  // widen; dJ/dh0 = dJ/deta0, dJ/dB (h0 fixed) = gB + dJ/deta0
+            const unsigned blocks = (unsigned)std::min<size_t>((A.fe + 255) / 256, 4096);
+            const float *lam0 = reinterpret_cast<const float *>(A.lam[0]);
+            if (f < 3)
+                k_widen<<<blocks, 256, 0, st>>>(reinterpret_cast<const float *>(A.lam[f]), widened, A.fe);
+            else
+                k_grad_b_f32<<<blocks, 256, 0, st>>>(reinterpret_cast<const float *>(A.gB), lam0,
+                                                     widened, A.fe);
+            c->launches += 1;
+            e = cudaGetLastError();
+            src = widened;
+        } else {
+            src = reinterpret_cast<const double *>(f < 3 ? A.lam[f] : A.gB);
+        }
+        if (e == cudaSuccess)
+            e = cudaMemcpy2DAsync(outs[f], row, src, dp, row, (size_t)(c->p.Nx + 4),
+                                  cudaMemcpyDeviceToHost, st);
+        // the staging buffer is reused by the next field
+        if (e == cudaSuccess && eta_state<T>()) e = cudaStreamSynchronize(st);
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     float t = 0.f;
     if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
@@ -630,4 +710,42 @@ extern "C" int swe_adjoint_gauge(swe_ctx *c, int n_steps, double dt, int n_gauge
         return SWE_ERR_NONFINITE;
     }
     return SWE_OK;
+}
+
+}  // namespace
+}  // namespace swe
+
+using namespace swe;
+
+extern "C" int swe_adjoint_gauge(swe_ctx *c, int n_steps, double dt, int n_gauges,
+                                 const int *gauge_i, const int *gauge_j, const double *h_obs,
+                                 int n_snapshots, double *J, double *grad_h, double *grad_hu,
+                                 double *grad_hv, double *grad_B, double *ms) {
+    if (!c) return SWE_ERR_BAD_ARG;
+    if (!c->uploaded || n_steps < 1 || !(dt > 0.0) ||
+        n_gauges < 0 || (n_gauges > 0 && (!gauge_i || !gauge_j || !h_obs)) ||
+        (n_snapshots < 0 && n_snapshots != SWE_ADJ_TAPE_ALL) ||
+        !J || !grad_h || !grad_hu || !grad_hv || !grad_B) {
+        c->err = "swe_adjoint_gauge: bad argument (needs an uploaded context)";
+        return SWE_ERR_BAD_ARG;
+    }
+    if (c->p.x_halo_lo || c->p.x_halo_hi) {
+        c->err = "swe_adjoint_gauge: not available on slab contexts";
+        return SWE_ERR_UNSUPPORTED;
+    }
+    if (c->p.scheme != SWE_SCHEME_FUSED) {
+        c->err = "swe_adjoint_gauge: the adjoint is of the fused scheme";
+        return SWE_ERR_UNSUPPORTED;
+    }
+    for (int q = 0; q < n_gauges; ++q)
+        if (gauge_i[q] < 0 || gauge_i[q] >= c->p.Nx || gauge_j[q] < 0 || gauge_j[q] >= c->p.Ny) {
+            c->err = "swe_adjoint_gauge: gauge outside the interior";
+            return SWE_ERR_BAD_ARG;
+        }
+    if (cudaSetDevice(c->p.device) != cudaSuccess) return SWE_ERR_CUDA;
+    if (c->p.precision == SWE_PRECISION_FP32_MIXED)
+        return run_adjoint<float>(c, n_steps, dt, n_gauges, gauge_i, gauge_j, h_obs, n_snapshots,
+                                  J, grad_h, grad_hu, grad_hv, grad_B, ms);
+    return run_adjoint<double>(c, n_steps, dt, n_gauges, gauge_i, gauge_j, h_obs, n_snapshots, J,
+                               grad_h, grad_hu, grad_hv, grad_B, ms);
 }

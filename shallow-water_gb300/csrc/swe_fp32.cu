@@ -285,11 +285,13 @@ __device__ __forceinline__ float stage_tile_f32(const StageParams &p, int i0, in
                 ov = nv + c * ((sv + dt * rhv) - nv);
             }
         }
-        if (oe - b < H_FLOORF) {  // enforce_positivity on h = eta - B
+        const bool clamped = oe - b < H_FLOORF;
+        if (clamped) {  // enforce_positivity on h = eta - B
             oe = b + H_FLOORF;
             ou = 0.f;
             ov = 0.f;
         }
+        if (p.mask) p.mask[k] = clamped ? 1 : 0;  // for the adjoint
         if (!(fabsf(oe) + fabsf(ou) + fabsf(ov) < INFINITY)) atomicOr(p.flags, FLAG_NONFINITE);
         static_cast<float *>(p.ho)[k] = oe;
         static_cast<float *>(p.huo)[k] = ou;
