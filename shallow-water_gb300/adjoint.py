@@ -1,7 +1,7 @@
 """Gradients of a gauge-misfit objective through the discrete adjoint (swe_adjoint_gauge).
 
 J = sum over steps n = 1..N and gauges q of (h^n at gauge q - h_obs[n-1, q])^2, for N
-fixed-dt SSP-RK3 steps.  :func:`gauge_misfit_gradient` returns J and its gradients with
+fixed-dt SSP-RK3 steps, through the FP64 or the FP32-mixed scheme (the solver's).  :func:`gauge_misfit_gradient` returns J and its gradients with
 respect to the initial state and the bathymetry; :class:`GaugeMisfit` wraps it as a
 ``torch.autograd.Function`` of the initial free surface eta0 and the bathymetry B
 (interior arrays; h0 = eta0 - B, hu0 = hv0 = 0).
@@ -66,18 +66,19 @@ try:
     class GaugeMisfit(torch.autograd.Function):
         """J(eta0, B) with gradients from the GPU discrete adjoint.
 
-        ``GaugeMisfit.apply(eta0, B, steps, dt, gauges, h_obs, Lx, Ly, g, bc, snapshots)``;
-        eta0 and B are float64 (Nx, Ny) tensors.  Backward returns
+        ``GaugeMisfit.apply(eta0, B, steps, dt, gauges, h_obs, Lx, Ly, g, bc, snapshots,
+        precision)``; eta0 and B are float64 (Nx, Ny) tensors; precision "fp32_mixed" runs
+        the FP32 forward and adjoint.  Backward returns
         dJ/deta0 = dJ/dh0 and dJ/dB = (dJ/dB at fixed h0) - dJ/dh0 (h0 = eta0 - B, wet)."""
 
         @staticmethod
         def forward(ctx, eta0, B, steps, dt, gauges, h_obs, Lx=1.0, Ly=1.0, g=9.80665,
-                    bc="reflecting", snapshots=None):
+                    bc="reflecting", snapshots=None, precision="fp64"):
             e = eta0.detach().cpu().double().numpy()
             b = B.detach().cpu().double().numpy()
             h, hu, hv, Bg = ghosted_state(e, b, bc)
             Nx, Ny = e.shape
-            with Solver(Nx, Ny, Lx, Ly, g=g, bc=bc) as s:
+            with Solver(Nx, Ny, Lx, Ly, g=g, bc=bc, precision=precision) as s:
                 s.upload(h, hu, hv, Bg)
                 r = gauge_misfit_gradient(s, steps, dt, gauges, np.asarray(h_obs), snapshots)
             wet = (e - b) > 0
@@ -90,6 +91,6 @@ try:
         @staticmethod
         def backward(ctx, gJ):
             g_eta, g_B = ctx.saved_tensors
-            return (gJ * g_eta, gJ * g_B) + (None,) * 9
+            return (gJ * g_eta, gJ * g_B) + (None,) * 10
 except ImportError:  # pragma: no cover - torch is optional for the C ABI users
     GaugeMisfit = None
