@@ -29,6 +29,7 @@ struct swe_ens {
     int n = 0;
     cudaStream_t stream = nullptr;
     int num_sms = 0;
+    int resident[8] = {-1, -1, -1, -1, -1, -1, -1, -1};  // CTAs per SM by shape, -1: not queried
     bool f32 = false;
     size_t elem = 8;
     std::vector<EnsInst> inst;  // host copy (tiles_j / tile_base for the current shape)
@@ -220,15 +221,20 @@ EnsParams stage_params(const swe_ens *c, int stage, int slot_read, double dt_fix
     return e;
 }
 
-// CTAs of the current shape resident on the whole GPU at once (0: unknown).
-int resident_ctas(const swe_ens *c) {
-    const int per_sm = c->f32 ? ens_resident_per_sm_f32(c->shape) : ens_resident_per_sm_f64(c->shape);
-    return per_sm * c->num_sms;
+// CTAs per SM of a shape (the occupancy query, once per shape and ensemble).
+int resident_per_sm(swe_ens *c, int shape) {
+    if (shape < 0 || shape >= 8) return 0;
+    if (c->resident[shape] < 0)
+        c->resident[shape] = c->f32 ? ens_resident_per_sm_f32(shape) : ens_resident_per_sm_f64(shape);
+    return c->resident[shape];
 }
+
+// CTAs of the current shape resident on the whole GPU at once (0: unknown).
+int resident_ctas(swe_ens *c) { return resident_per_sm(c, c->shape) * c->num_sms; }
 
 // A persistent schedule never asks for more CTAs than fit at once: with every CTA
 // resident, equal shares of the work list finish together instead of in waves.
-int grid_ctas(const swe_ens *c) {
+int grid_ctas(swe_ens *c) {
     const int tiles = std::max(c->total_tiles, 1);
     if (c->grid <= 0) return tiles;
     int g = std::min(c->grid, tiles);
@@ -587,8 +593,7 @@ int swe_ens_tune(swe_ens *c, int steps, double *best_ms) {
         for (int gm : grids) {
             int g = 0;
             if (gm > 0) {
-                const int per_sm = c->f32 ? ens_resident_per_sm_f32(shapes[si])
-                                          : ens_resident_per_sm_f64(shapes[si]);
+                const int per_sm = resident_per_sm(c, shapes[si]);
                 if (per_sm <= 0 || (gm == 2 && per_sm < 2)) continue;
                 g = (gm == 1 ? per_sm : per_sm / 2) * c->num_sms;
             }
