@@ -257,6 +257,180 @@ __global__ void __launch_bounds__(AGT) k_adj_gather(const AdjParams<T> a) {
     a.gB[k] += acc_B;
 }
 
+// Single-pass reverse of one stage for a TI x TJ tile (the FP32 path): the tile's
+// stage source (halo 3) and divergence adjoint (halo 2) are staged in shared memory,
+// every x- and y-interface whose stencil holds a tile cell is reversed there (TI + 3
+// rows of x-interfaces, TJ + 3 columns of y-interfaces: 1.23 interface VJPs per cell,
+// against 1.0 in the two-pass form), and each cell gathers its contributions from
+// shared memory in the two-pass gather's order, so the results are bitwise the same.
+// The interface contributions never reach HBM: about 70 bytes per cell and stage move
+// instead of about 300, which is what bounds the FP32 reverse sweep.
+constexpr int ATI = 8, ATJ = 32, ATT = ATI * ATJ;
+
+template <class T>
+struct AdjTile {
+    T st[4][ATI + 6][ATJ + 6];         // eta (or h + B), qn-x (hu), qn-y (hv), B; halo 3
+    T w[3][ATI + 4][ATJ + 4];          // cs dt lo, zero outside and where clamped; halo 2
+    T cx[NC][ATI + 3][ATJ];            // x-interfaces i0-2 .. i0+TI
+    T cy[NC][ATI][ATJ + 3];            // y-interfaces j0-2 .. j0+TJ
+};
+
+template <class T, int STAGE>
+__global__ void __launch_bounds__(ATT) k_adj_tile(const AdjParams<T> a) {
+    extern __shared__ __align__(16) unsigned char adj_smem[];
+    AdjTile<T> &t = *reinterpret_cast<AdjTile<T> *>(adj_smem);
+    const int tid = threadIdx.x;
+    const int i0 = blockIdx.y * ATI, j0 = blockIdx.x * ATJ;
+    const long long P = a.pitch;
+    // stage source, as k_adj_faces reads each stencil cell
+    for (int e = tid; e < (ATI + 6) * (ATJ + 6); e += ATT) {
+        const int r = e / (ATJ + 6), c = e - r * (ATJ + 6);
+        const int i = i0 - 3 + r, j = j0 - 3 + c;
+        T ev = T(0), u = T(0), v = T(0), b = T(0);
+        if (i >= -2 && i <= a.Nx + 1 && j >= -2 && j <= a.Ny + 1) {
+            bool fx, fy;
+            const int mi = map_coord(i, a.Nx, a.bc, fx), mj = map_coord(j, a.Ny, a.bc, fy);
+            const long long ks = (long long)(mi + NG) * P + (mj + NG);
+            const long long kb = (long long)clamp_int(i + NG, 0, a.Nx + 3) * P +
+                                 clamp_int(j + NG, 0, a.Ny + 3);
+            b = a.B[kb];
+            if (eta_state<T>()) {
+                const T bs = a.B[ks], e0 = a.h[ks];
+                ev = (b == bs) ? e0 : (e0 - bs) + b;
+            } else {
+                ev = a.h[ks] + b;
+            }
+            u = fx ? -a.hu[ks] : a.hu[ks];
+            v = fy ? -a.hv[ks] : a.hv[ks];
+        }
+        t.st[0][r][c] = ev;
+        t.st[1][r][c] = u;
+        t.st[2][r][c] = v;
+        t.st[3][r][c] = b;
+    }
+    for (int e = tid; e < (ATI + 4) * (ATJ + 4); e += ATT) {
+        const int r = e / (ATJ + 4), c = e - r * (ATJ + 4);
+        T w[3];
+        w_at<T, STAGE>(a, i0 - 2 + r, j0 - 2 + c, w);
+        t.w[0][r][c] = w[0];
+        t.w[1][r][c] = w[1];
+        t.w[2][r][c] = w[2];
+    }
+    __syncthreads();
+    const T g = a.g, eps = T(EPS);
+    // x-interfaces f = i0 - 2 + ar between rows f and f + 1, column j0 + c
+    for (int e = tid; e < (ATI + 3) * ATJ; e += ATT) {
+        const int ar = e / ATJ, c = e - ar * ATJ;
+        const int f = i0 - 2 + ar;
+        if (f < -1 || f > a.Nx - 1 || j0 + c >= a.Ny) continue;
+        adj::FaceIn<T> in;
+        for (int q = 0; q < 4; ++q) {  // box row of stencil cell f - 1 + q: ar + q
+            in.e[q] = t.st[0][ar + q][c + 3];
+            in.n[q] = t.st[1][ar + q][c + 3];
+            in.t[q] = t.st[2][ar + q][c + 3];
+        }
+        in.bm = t.st[3][ar + 1][c + 3];
+        in.bp = t.st[3][ar + 2][c + 3];
+        adj::FaceOut<T> d;  // w rows of cells f, f + 1: ar, ar + 1
+        d.fh = a.inv_dx * (t.w[0][ar + 1][c + 2] - t.w[0][ar][c + 2]);
+        d.fqt = a.inv_dx * (t.w[2][ar + 1][c + 2] - t.w[2][ar][c + 2]);
+        d.fqn_m = -a.inv_dx * t.w[1][ar][c + 2];
+        d.fqn_p = a.inv_dx * t.w[1][ar + 1][c + 2];
+        adj::FaceIn<T> ad;
+        adj::face_vjp(in, g, eps, d, ad);
+        for (int q = 0; q < 4; ++q) {
+            t.cx[q][ar][c] = ad.e[q];
+            t.cx[4 + q][ar][c] = ad.n[q];
+            t.cx[8 + q][ar][c] = ad.t[q];
+        }
+        t.cx[12][ar][c] = ad.bm;
+        t.cx[13][ar][c] = ad.bp;
+    }
+    // y-interfaces f = j0 - 2 + bc between columns f and f + 1, row i0 + r
+    for (int e = tid; e < ATI * (ATJ + 3); e += ATT) {
+        const int r = e / (ATJ + 3), bc = e - r * (ATJ + 3);
+        const int f = j0 - 2 + bc;
+        if (f < -1 || f > a.Ny - 1 || i0 + r >= a.Nx) continue;
+        adj::FaceIn<T> in;
+        for (int q = 0; q < 4; ++q) {
+            in.e[q] = t.st[0][r + 3][bc + q];
+            in.n[q] = t.st[2][r + 3][bc + q];
+            in.t[q] = t.st[1][r + 3][bc + q];
+        }
+        in.bm = t.st[3][r + 3][bc + 1];
+        in.bp = t.st[3][r + 3][bc + 2];
+        adj::FaceOut<T> d;
+        d.fh = a.inv_dy * (t.w[0][r + 2][bc + 1] - t.w[0][r + 2][bc]);
+        d.fqt = a.inv_dy * (t.w[1][r + 2][bc + 1] - t.w[1][r + 2][bc]);
+        d.fqn_m = -a.inv_dy * t.w[2][r + 2][bc];
+        d.fqn_p = a.inv_dy * t.w[2][r + 2][bc + 1];
+        adj::FaceIn<T> ad;
+        adj::face_vjp(in, g, eps, d, ad);
+        for (int q = 0; q < 4; ++q) {
+            t.cy[q][r][bc] = ad.e[q];
+            t.cy[4 + q][r][bc] = ad.n[q];
+            t.cy[8 + q][r][bc] = ad.t[q];
+        }
+        t.cy[12][r][bc] = ad.bm;
+        t.cy[13][r][bc] = ad.bp;
+    }
+    __syncthreads();
+    const int r = tid / ATJ, c = tid - r * ATJ;
+    const int ci = i0 + r, cj = j0 + c;
+    if (ci >= a.Nx || cj >= a.Ny) return;
+    T acc_h = T(0), acc_hu = T(0), acc_hv = T(0), acc_B = T(0);
+    // gather_dir<T, 0> and <T, 1> with the contributions read from shared memory
+    for (int dir = 0; dir < 2; ++dir) {
+        const int ca = dir == 0 ? ci : cj, N = dir == 0 ? a.Nx : a.Ny;
+        const int base = dir == 0 ? i0 - 2 : j0 - 2;
+        T &acc_n = dir == 0 ? acc_hu : acc_hv, &acc_t = dir == 0 ? acc_hv : acc_hu;
+        int v[5];
+        bool fl[5];
+        const int nv = virtual_coords(ca, N, a.bc, v, fl);
+        auto C = [&](int q, int f) -> T {
+            return dir == 0 ? t.cx[q][f - base][c] : t.cy[q][r][f - base];
+        };
+        for (int q = 0; q < nv; ++q) {
+            for (int k = 0; k < 4; ++k) {
+                const int f = v[q] + 1 - k;
+                if (f < -1 || f > N - 1) continue;
+                const T ce = C(k, f), cn = C(4 + k, f);
+                acc_h += ce;
+                if (!eta_state<T>()) acc_B += ce;
+                acc_n += fl[q] ? -cn : cn;
+                acc_t += C(8 + k, f);
+            }
+            const int fm = v[q], fp = v[q] - 1;
+            if (fm >= -1 && fm <= N - 1) acc_B += C(12, fm);
+            if (fp >= -1 && fp <= N - 1) acc_B += C(13, fp);
+        }
+    }
+    const T cs = src_weight<T, STAGE>();
+    const long long k = (long long)(ci + NG) * P + (cj + NG);
+    const bool m = a.mask[k];
+    if (eta_state<T>() && m) acc_B += a.lo_h[k];
+    const T l0 = m ? T(0) : a.lo_h[k], l1 = m ? T(0) : a.lo_hu[k], l2 = m ? T(0) : a.lo_hv[k];
+    T o0 = acc_h + cs * l0, o1 = acc_hu + cs * l1, o2 = acc_hv + cs * l2;
+    if (STAGE == 3) {
+        const T wn = n_weight3<T>();
+        a.ln_h[k] = wn * l0;
+        a.ln_hu[k] = wn * l1;
+        a.ln_hv[k] = wn * l2;
+    } else if (STAGE == 2) {
+        a.ln_h[k] += T(0.75) * l0;
+        a.ln_hu[k] += T(0.75) * l1;
+        a.ln_hv[k] += T(0.75) * l2;
+    } else {
+        o0 += a.ln_h[k];
+        o1 += a.ln_hu[k];
+        o2 += a.ln_hv[k];
+    }
+    a.ls_h[k] = o0;
+    a.ls_hu[k] = o1;
+    a.ls_hv[k] = o2;
+    a.gB[k] += acc_B;
+}
+
 // Gauge source of one step: lambda_h[g] += 2 (h_g - obs_g), J += sum (h_g - obs_g)^2,
 // one thread in gauge order (deterministic, duplicates allowed).
 // FP32-mixed: h = eta - B in FP64, lambda_eta += 2 (h - obs) and lambda_B -= 2 (h - obs).
@@ -416,6 +590,24 @@ cudaError_t launch_adj(Adj<T> &A, int stage, T *const *state, T *const *lo,
     p.cy = A.cy;
     p.px = (long long)(c->p.Nx + 1) * c->p.Ny;
     p.py = (long long)c->p.Nx * (c->p.Ny + 1);
+    if constexpr (eta_state<T>()) {  // FP32: the single-pass tile kernel (memory-bound otherwise)
+        const int smem = (int)sizeof(AdjTile<T>);
+        static bool opted[4];
+        if (!opted[stage]) {
+            auto kern = stage == 1 ? k_adj_tile<T, 1> : (stage == 2 ? k_adj_tile<T, 2> : k_adj_tile<T, 3>);
+            ACK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+            opted[stage] = true;
+        }
+        const dim3 gt((c->p.Ny + ATJ - 1) / ATJ, (c->p.Nx + ATI - 1) / ATI);
+        if (stage == 1)
+            k_adj_tile<T, 1><<<gt, ATT, smem, c->stream>>>(p);
+        else if (stage == 2)
+            k_adj_tile<T, 2><<<gt, ATT, smem, c->stream>>>(p);
+        else
+            k_adj_tile<T, 3><<<gt, ATT, smem, c->stream>>>(p);
+        ++c->launches;
+        return cudaGetLastError();
+    }
     const dim3 gx((c->p.Ny + AFT - 1) / AFT, c->p.Nx + 1), gy((c->p.Ny + 1 + AFT - 1) / AFT, c->p.Nx);
     const dim3 gg((c->p.Ny + AGT - 1) / AGT, c->p.Nx);
     switch (stage) {
@@ -592,8 +784,9 @@ int run_adjoint(swe_ctx *c, int n_steps, double dt, int n_gauges, const int *gau
     A.dt = dt;
     const size_t fb = A.fe * sizeof(T);
     auto rounded = [](size_t n) { return (n + 255) / 256 * 256; };
-    const size_t cx_bytes = (size_t)NC * (c->p.Nx + 1) * c->p.Ny * sizeof(T);
-    const size_t cy_bytes = (size_t)NC * c->p.Nx * (c->p.Ny + 1) * sizeof(T);
+    // interface contributions in HBM: the FP64 two-pass reverse only
+    const size_t cx_bytes = eta_state<T>() ? 0 : (size_t)NC * (c->p.Nx + 1) * c->p.Ny * sizeof(T);
+    const size_t cy_bytes = eta_state<T>() ? 0 : (size_t)NC * c->p.Nx * (c->p.Ny + 1) * sizeof(T);
     const size_t wide = eta_state<T>() ? rounded(A.fe * sizeof(double)) : 0;  // output staging
     const size_t bytes = rounded((size_t)(A.S + 1) * 3 * fb) + 19 * rounded(fb) + 3 * rounded(A.fe) +
                          rounded(cx_bytes) + rounded(cy_bytes) + wide +
