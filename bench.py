@@ -41,6 +41,12 @@ NCU_TRAFFIC_BYTES_PER_CELL_LAUNCH = 71.7
 # ncu thread-level instruction counts of the stage kernel; the pipe executes 2 per clock
 # per SM, so its peak is 2 x SMs x clock.
 FP64_OPS_PER_CELL_UPDATE = 484.9
+# Warp instructions per cell update (the three stages) of the FP32 kernels, from their
+# ncu captures: the single-grid stage kernel (15.7 + 15.9 + 17.4) and the ensemble stage
+# kernel (17.6 + 16.9 + 18.6).  Both are bound by instruction issue, 4 warp instructions
+# per clock per SM.
+F32_WARP_INST_PER_CELL_UPDATE = 49.0
+F32_ENS_WARP_INST_PER_CELL_UPDATE = 53.1
 
 
 def parse():
@@ -198,6 +204,22 @@ def fp64_pipe(gcups: float, dev: int):
             "peak_source": f"2 x {sms} SMs x {mhz:.0f} MHz"}
 
 
+def issue_roofline(gcups: float, inst_per_cell: float, dev: int = 0) -> dict:
+    """The bound of the FP32 stage kernels: warp-instruction issue, 4 per clock per SM."""
+    import torch
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            mhz = float(json.load(f)["sm_max_mhz"])
+    except (OSError, KeyError, ValueError):
+        mhz = 2070.0
+    peak = 4.0 * sms * mhz * 1e6 / 1e9  # G warp instructions / s
+    achieved = gcups * inst_per_cell
+    return {"achieved": achieved, "peak": peak, "unit": "G warp instructions/s",
+            "frac": achieved / peak, "warp_instructions_per_cell_update": inst_per_cell,
+            "cap_gcups": peak / inst_per_cell, "peak_source": f"4 x {sms} SMs x {mhz:.0f} MHz"}
+
+
 def cpu_threads() -> int:
     try:
         return len(os.sched_getaffinity(0))
@@ -246,7 +268,8 @@ def form_fp32(args, sw, fp64_gcups):
     gcups = n * n / (ms / 1e3) / 1e9
     out = {"grid": [n, n], "ms_per_step": ms, "gcups": gcups,
            "hbm_frac_of_measured": 108 * n * n / (ms / 1e3) / 1e9 / peaks()[0],
-           "bytes_per_cell_update": 108, "speedup_vs_fp64": gcups / fp64_gcups}
+           "bytes_per_cell_update": 108, "speedup_vs_fp64": gcups / fp64_gcups,
+           "issue_roofline": issue_roofline(gcups, F32_WARP_INST_PER_CELL_UPDATE)}
     m, K = args.acc_n, args.acc_steps
     h, hu, hv, B = workload(m, args.seed)
     with sw.Solver(m, m, bc="transmissive") as s64, \
@@ -307,6 +330,13 @@ def form_ensemble(args, sw):
                          "hbm_frac_of_measured": bpc * cells / (ms / 1e3) / 1e9 / peaks()[0],
                          "schedule": {"shape": tune["shape"], "grid": tune["grid"]},
                          "launches_per_step": 3, "graph_replay": True}
+            g = res[prec]["gcups"]
+            if prec == "fp64":
+                res[prec]["fp64_pipe_roofline"] = fp64_pipe(g, 0)
+            else:  # against the single-grid kernel's instruction count, and its own
+                res[prec]["issue_roofline"] = issue_roofline(g, F32_WARP_INST_PER_CELL_UPDATE)
+                res[prec]["issue_roofline_own_instructions"] = issue_roofline(
+                    g, F32_ENS_WARP_INST_PER_CELL_UPDATE)
     return res
 
 
