@@ -210,7 +210,11 @@ class FastHLLMUSCLBathyGB300Solver {
         if (status == SWE_OK) return;
         std::string msg = std::string("GB300 backend: ") + what + ": " + swe_status_string(status);
         if (ctx_ && swe_last_error(ctx_)[0]) msg += std::string(" (") + swe_last_error(ctx_) + ")";
-        if (status == SWE_ERR_NONFINITE) msg = "non-finite state detected in GB300 solver";
+        // the modular scheme reports the Serial backend's own messages ("non-finite state
+        // detected in positivity correction", "HLL could not provide dissipation speed.")
+        if (status == SWE_ERR_NONFINITE)
+            msg = fused(cfg_) ? std::string("non-finite state detected in GB300 solver")
+                              : std::string(swe_last_error(ctx_));
         throw std::runtime_error(msg);
     }
 
