@@ -913,7 +913,7 @@ using namespace swe;
 extern "C" int swe_adjoint_gauge(swe_ctx *c, int n_steps, double dt, int n_gauges,
                                  const int *gauge_i, const int *gauge_j, const double *h_obs,
                                  int n_snapshots, double *J, double *grad_h, double *grad_hu,
-                                 double *grad_hv, double *grad_B, double *ms) {
+                                 double *grad_hv, double *grad_B, double *ms) try {
     if (!c) return SWE_ERR_BAD_ARG;
     if (!c->uploaded || n_steps < 1 || !(dt > 0.0) ||
         n_gauges < 0 || (n_gauges > 0 && (!gauge_i || !gauge_j || !h_obs)) ||
@@ -941,4 +941,6 @@ extern "C" int swe_adjoint_gauge(swe_ctx *c, int n_steps, double dt, int n_gauge
                                   J, grad_h, grad_hu, grad_hv, grad_B, ms);
     return run_adjoint<double>(c, n_steps, dt, n_gauges, gauge_i, gauge_j, h_obs, n_snapshots, J,
                                grad_h, grad_hu, grad_hv, grad_B, ms);
+} catch (...) {  // host allocation failures do not cross the C ABI
+    return SWE_ERR_BAD_ARG;
 }

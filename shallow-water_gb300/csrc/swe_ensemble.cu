@@ -313,7 +313,7 @@ int run_steps(swe_ens *c, int n_steps, double dt_fixed) {
 extern "C" {
 
 int swe_ens_create(const swe_params *base, int n, const int *Nx, const int *Ny, const double *Lx,
-                   const double *Ly, swe_ens **out) {
+                   const double *Ly, swe_ens **out) try {
     if (!base || !out || n <= 0 || !Nx || !Ny) return SWE_ERR_BAD_ARG;
     *out = nullptr;
     swe_params b = *base;
@@ -400,9 +400,11 @@ int swe_ens_create(const swe_params *base, int n, const int *Nx, const int *Ny, 
     if (build_tiles(c) != SWE_OK) return cleanup(SWE_ERR_CUDA);
     *out = c;
     return SWE_OK;
+} catch (...) {  // host allocation failures do not cross the C ABI
+    return SWE_ERR_BAD_ARG;
 }
 
-void swe_ens_destroy(swe_ens *c) {
+void swe_ens_destroy(swe_ens *c) try {
     if (!c) return;
     cudaSetDevice(c->base.device);
     if (c->stream) cudaStreamSynchronize(c->stream);
@@ -416,12 +418,13 @@ void swe_ens_destroy(swe_ens *c) {
     if (c->stream) cudaStreamDestroy(c->stream);
     cudaGetLastError();
     delete c;
+} catch (...) {  // host allocation failures do not cross the C ABI
 }
 
 const char *swe_ens_last_error(const swe_ens *c) { return c ? c->err.c_str() : "null ensemble"; }
 
 int swe_ens_upload(swe_ens *c, int q, const double *h, const double *hu, const double *hv,
-                   const double *B) {
+                   const double *B) try {
     if (!c || q < 0 || q >= c->n || !h || !hu || !hv || !B)
         return efail(c, SWE_ERR_BAD_ARG, "swe_ens_upload: bad argument");
     ECK(cudaSetDevice(c->base.device));
@@ -459,9 +462,11 @@ int swe_ens_upload(swe_ens *c, int q, const double *h, const double *hu, const d
     ECK(cudaStreamSynchronize(c->stream));
     c->uploaded[q] = 1;
     return SWE_OK;
+} catch (...) {  // host allocation failures do not cross the C ABI
+    return SWE_ERR_BAD_ARG;
 }
 
-int swe_ens_download(swe_ens *c, int q, double *h, double *hu, double *hv) {
+int swe_ens_download(swe_ens *c, int q, double *h, double *hu, double *hv) try {
     if (!c || q < 0 || q >= c->n || !h || !hu || !hv)
         return efail(c, SWE_ERR_BAD_ARG, "swe_ens_download: bad argument");
     ECK(cudaSetDevice(c->base.device));
@@ -491,9 +496,11 @@ int swe_ens_download(swe_ens *c, int q, double *h, double *hu, double *hv) {
     }
     ECK(cudaStreamSynchronize(c->stream));
     return SWE_OK;
+} catch (...) {  // host allocation failures do not cross the C ABI
+    return SWE_ERR_BAD_ARG;
 }
 
-int swe_ens_step(swe_ens *c, int n_steps, double dt) {
+int swe_ens_step(swe_ens *c, int n_steps, double dt) try {
     if (!c || n_steps < 0 || !(dt == dt)) return efail(c, SWE_ERR_BAD_ARG, "swe_ens_step: bad argument");
     for (int q = 0; q < c->n; ++q)
         if (!c->uploaded[q]) return efail(c, SWE_ERR_BAD_ARG, "swe_ens_step: instance %d not uploaded", q);
@@ -513,31 +520,39 @@ int swe_ens_step(swe_ens *c, int n_steps, double dt) {
     if (flags & FLAG_NONFINITE)
         return efail(c, SWE_ERR_NONFINITE, "non-finite state detected in GB300 ensemble");
     return SWE_OK;
+} catch (...) {  // host allocation failures do not cross the C ABI
+    return SWE_ERR_BAD_ARG;
 }
 
-int swe_ens_times(swe_ens *c, double *t) {
+int swe_ens_times(swe_ens *c, double *t) try {
     if (!c || !t) return efail(c, SWE_ERR_BAD_ARG, "swe_ens_times: bad argument");
     ECK(cudaMemcpyAsync(t, c->d_t, c->n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     ECK(cudaStreamSynchronize(c->stream));
     return SWE_OK;
+} catch (...) {  // host allocation failures do not cross the C ABI
+    return SWE_ERR_BAD_ARG;
 }
 
-int swe_ens_last_dt(swe_ens *c, double *dt) {
+int swe_ens_last_dt(swe_ens *c, double *dt) try {
     if (!c || !dt) return efail(c, SWE_ERR_BAD_ARG, "swe_ens_last_dt: bad argument");
     ECK(cudaMemcpyAsync(dt, c->d_dt, c->n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     ECK(cudaStreamSynchronize(c->stream));
     return SWE_OK;
+} catch (...) {  // host allocation failures do not cross the C ABI
+    return SWE_ERR_BAD_ARG;
 }
 
-int swe_ens_last_step_ms(const swe_ens *c, double *ms) {
+int swe_ens_last_step_ms(const swe_ens *c, double *ms) try {
     if (!c || !ms) return SWE_ERR_BAD_ARG;
     *ms = c->last_ms;
     return SWE_OK;
+} catch (...) {  // host allocation failures do not cross the C ABI
+    return SWE_ERR_BAD_ARG;
 }
 
 long long swe_ens_kernel_launches(const swe_ens *c) { return c ? c->launches : 0; }
 
-int swe_ens_set_schedule(swe_ens *c, int shape, int grid) {
+int swe_ens_set_schedule(swe_ens *c, int shape, int grid) try {
     if (!c || grid < 0 || !shape_ok(c, shape))
         return efail(c, SWE_ERR_BAD_ARG, "swe_ens_set_schedule: unsupported shape %d", shape);
     ECK(cudaSetDevice(c->base.device));
@@ -548,17 +563,21 @@ int swe_ens_set_schedule(swe_ens *c, int shape, int grid) {
     }
     destroy_graphs(c);
     return SWE_OK;
+} catch (...) {  // host allocation failures do not cross the C ABI
+    return SWE_ERR_BAD_ARG;
 }
 
-int swe_ens_get_schedule(const swe_ens *c, int *shape, int *grid, int *total_tiles) {
+int swe_ens_get_schedule(const swe_ens *c, int *shape, int *grid, int *total_tiles) try {
     if (!c) return SWE_ERR_BAD_ARG;
     if (shape) *shape = c->shape;
     if (grid) *grid = c->grid;
     if (total_tiles) *total_tiles = c->total_tiles;
     return SWE_OK;
+} catch (...) {  // host allocation failures do not cross the C ABI
+    return SWE_ERR_BAD_ARG;
 }
 
-int swe_ens_tune(swe_ens *c, int steps, double *best_ms) {
+int swe_ens_tune(swe_ens *c, int steps, double *best_ms) try {
     if (!c || steps <= 0) return efail(c, SWE_ERR_BAD_ARG, "swe_ens_tune: bad argument");
     for (int q = 0; q < c->n; ++q)
         if (!c->uploaded[q]) return efail(c, SWE_ERR_BAD_ARG, "swe_ens_tune: instance %d not uploaded", q);
@@ -622,6 +641,8 @@ int swe_ens_tune(swe_ens *c, int steps, double *best_ms) {
     ECK(cudaStreamSynchronize(c->stream));
     if (best_ms) *best_ms = best / steps;
     return SWE_OK;
+} catch (...) {  // host allocation failures do not cross the C ABI
+    return SWE_ERR_BAD_ARG;
 }
 
 }  // extern "C"

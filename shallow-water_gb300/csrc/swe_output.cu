@@ -315,7 +315,7 @@ int drain(swe_snapshot *s) {
 
 extern "C" {
 
-int swe_snapshot_open(const char *path, const swe_snapshot_params *p, swe_snapshot **out) {
+int swe_snapshot_open(const char *path, const swe_snapshot_params *p, swe_snapshot **out) try {
     if (!out) return SWE_ERR_BAD_ARG;
     *out = nullptr;
     if (!path || !p || p->Nx < 1 || p->Ny < 1 || !(p->dx > 0.0) || !(p->dy > 0.0) ||
@@ -372,21 +372,25 @@ int swe_snapshot_open(const char *path, const swe_snapshot_params *p, swe_snapsh
     }
     *out = s;
     return SWE_OK;
+} catch (...) {  // no exception crosses the C ABI (allocation, threads)
+    return SWE_ERR_IO;
 }
 
-int swe_snapshot_bathymetry(swe_snapshot *s, const double *B) {
+int swe_snapshot_bathymetry(swe_snapshot *s, const double *B) try {
     if (!s || !B) return snap_fail(s, SWE_ERR_BAD_ARG, "swe_snapshot_bathymetry: null argument");
     if (s->closed) return snap_fail(s, SWE_ERR_BAD_ARG, "swe_snapshot_bathymetry: file closed");
     if (s->bathymetry_written) return SWE_OK;  // netCDF_writer.cpp:87-89
     if (!write_host_field(s, s->v_B, -1, B)) return snap_fail(s, SWE_ERR_IO, s->f.error());
     s->bathymetry_written = true;
     return SWE_OK;
+} catch (...) {  // no exception crosses the C ABI (allocation, threads)
+    return SWE_ERR_IO;
 }
 
 int swe_snapshot_metadata(swe_snapshot *s, double dt, const char *backend,
                           const char *riemann_solver, const char *reconstruction,
                           const char *time_integrator, const char *boundary_condition,
-                          const char *bathymetry) {
+                          const char *bathymetry) try {
     if (!s) return SWE_ERR_BAD_ARG;
     if (s->closed) return snap_fail(s, SWE_ERR_BAD_ARG, "swe_snapshot_metadata: file closed");
     // netCDF_writer.cpp:107-133: backend alone does not trigger the metadata.
@@ -406,10 +410,12 @@ int swe_snapshot_metadata(swe_snapshot *s, double dt, const char *backend,
     if (!ok) return snap_fail(s, SWE_ERR_IO, f.error());
     s->metadata_written = true;
     return SWE_OK;
+} catch (...) {  // no exception crosses the C ABI (allocation, threads)
+    return SWE_ERR_IO;
 }
 
 int swe_snapshot_write_host(swe_snapshot *s, double time, const double *h, const double *hu,
-                            const double *hv) {
+                            const double *hv) try {
     if (!s || !h || !hu || !hv)
         return snap_fail(s, SWE_ERR_BAD_ARG, "swe_snapshot_write_host: null argument");
     if (s->closed) return snap_fail(s, SWE_ERR_BAD_ARG, "swe_snapshot_write_host: file closed");
@@ -427,9 +433,11 @@ int swe_snapshot_write_host(swe_snapshot *s, double time, const double *h, const
         return snap_fail(s, SWE_ERR_IO, s->f.error());
     s->next_record = rec + 1;
     return SWE_OK;
+} catch (...) {  // no exception crosses the C ABI (allocation, threads)
+    return SWE_ERR_IO;
 }
 
-int swe_snapshot_write(swe_snapshot *s, swe_ctx *c, double time) {
+int swe_snapshot_write(swe_snapshot *s, swe_ctx *c, double time) try {
     if (!s || !c) return snap_fail(s, SWE_ERR_BAD_ARG, "swe_snapshot_write: null argument");
     if (s->closed) return snap_fail(s, SWE_ERR_BAD_ARG, "swe_snapshot_write: file closed");
     if (!c->uploaded) return snap_fail(s, SWE_ERR_BAD_ARG, "swe_snapshot_write: no state uploaded");
@@ -475,6 +483,8 @@ int swe_snapshot_write(swe_snapshot *s, swe_ctx *c, double time) {
     ++s->next_record;
     s->next_slot ^= 1;
     return SWE_OK;
+} catch (...) {  // no exception crosses the C ABI (allocation, threads)
+    return SWE_ERR_CUDA;
 }
 
 int swe_snapshot_flush(swe_snapshot *s) {
@@ -495,7 +505,7 @@ int swe_snapshot_stats(const swe_snapshot *s, double *copy_s, double *write_s, l
     return SWE_OK;
 }
 
-int swe_snapshot_close(swe_snapshot *s) {
+int swe_snapshot_close(swe_snapshot *s) try {
     if (!s) return SWE_ERR_BAD_ARG;
     if (s->closed) return SWE_OK;
     int st = s->device >= 0 ? drain(s) : SWE_OK;
@@ -511,12 +521,15 @@ int swe_snapshot_close(swe_snapshot *s) {
     if (!s->f.close() && st == SWE_OK) st = snap_fail(s, SWE_ERR_IO, s->f.error());
     s->closed = true;
     return st;
+} catch (...) {  // no exception crosses the C ABI (allocation, threads)
+    return SWE_ERR_IO;
 }
 
-void swe_snapshot_destroy(swe_snapshot *s) {
+void swe_snapshot_destroy(swe_snapshot *s) try {
     if (!s) return;
     swe_snapshot_close(s);
     delete s;
+} catch (...) {  // no exception crosses the C ABI (allocation, threads)
 }
 
 const char *swe_snapshot_last_error(const swe_snapshot *s) {
@@ -541,7 +554,7 @@ int swe_sanity_log_open(const char *path, const char *time_unit, const char *h_u
                         int save_every, double dt, const char *backend,
                         const char *riemann_solver, const char *reconstruction,
                         const char *time_integrator, const char *boundary_condition,
-                        const char *bathymetry, swe_sanity_log **out) {
+                        const char *bathymetry, swe_sanity_log **out) try {
     if (!out) return SWE_ERR_BAD_ARG;
     *out = nullptr;
     if (!path) return SWE_ERR_BAD_ARG;
@@ -583,10 +596,12 @@ int swe_sanity_log_open(const char *path, const char *time_unit, const char *h_u
     }
     *out = l;
     return SWE_OK;
+} catch (...) {  // no exception crosses the C ABI (allocation, threads)
+    return SWE_ERR_IO;
 }
 
 int swe_sanity_log_write(swe_sanity_log *l, unsigned long long step, double time,
-                         double rel_err, double h_min) {
+                         double rel_err, double h_min) try {
     if (!l) return SWE_ERR_BAD_ARG;
     if (l->closed) {
         l->err = "swe_sanity_log_write: file closed";
@@ -610,9 +625,11 @@ int swe_sanity_log_write(swe_sanity_log *l, unsigned long long step, double time
     }
     l->next_record = r + 1;
     return SWE_OK;
+} catch (...) {  // no exception crosses the C ABI (allocation, threads)
+    return SWE_ERR_IO;
 }
 
-int swe_sanity_log_close(swe_sanity_log *l) {
+int swe_sanity_log_close(swe_sanity_log *l) try {
     if (!l) return SWE_ERR_BAD_ARG;
     if (l->closed) return SWE_OK;
     l->closed = true;
@@ -621,12 +638,15 @@ int swe_sanity_log_close(swe_sanity_log *l) {
         return SWE_ERR_IO;
     }
     return SWE_OK;
+} catch (...) {  // no exception crosses the C ABI (allocation, threads)
+    return SWE_ERR_IO;
 }
 
-void swe_sanity_log_destroy(swe_sanity_log *l) {
+void swe_sanity_log_destroy(swe_sanity_log *l) try {
     if (!l) return;
     swe_sanity_log_close(l);
     delete l;
+} catch (...) {  // no exception crosses the C ABI (allocation, threads)
 }
 
 const char *swe_sanity_log_last_error(const swe_sanity_log *l) {
