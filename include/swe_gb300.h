@@ -96,6 +96,11 @@ typedef struct swe_params {
 
 typedef struct swe_ctx swe_ctx; /* opaque */
 
+/* sizeof(swe_params) and sizeof(swe_snapshot_params) as this library was built, so that
+ * bindings written in other languages can check their copy of the layout. */
+size_t swe_params_size(void);
+size_t swe_snapshot_params_size(void);
+
 /* Fills *p with defaults: nG = 2, L = 1, g = 9.80665, cfl = 0.45, reflecting, FP64,
  * the fused scheme (modular fields: MUSCL, HLL, bathymetry on),
  * device 0.  Nx and Ny must still be set. */

@@ -45,6 +45,7 @@ EXPORTS = (
     "swe_snapshot_records", "swe_snapshot_stats", "swe_snapshot_close", "swe_snapshot_destroy",
     "swe_snapshot_last_error", "swe_sanity_log_open", "swe_sanity_log_write",
     "swe_sanity_log_close", "swe_sanity_log_destroy", "swe_sanity_log_last_error",
+    "swe_params_size", "swe_snapshot_params_size",
 )
 TOTALS_NOALLOC_MAX_BLOCKS = 1024
 ADJ_TAPE_ALL = -1  # n_snapshots value of swe_adjoint_gauge's tape mode
@@ -106,6 +107,13 @@ def lib(path: str = LIB_PATH):
     L = ctypes.CDLL(path)
     dp = ctypes.POINTER(ctypes.c_double)
     vp = ctypes.c_void_p
+    L.swe_params_size.argtypes = []
+    L.swe_params_size.restype = ctypes.c_size_t
+    L.swe_snapshot_params_size.argtypes = []
+    L.swe_snapshot_params_size.restype = ctypes.c_size_t
+    if (L.swe_params_size() != ctypes.sizeof(SweParams) or
+            L.swe_snapshot_params_size() != ctypes.sizeof(SnapshotParams)):
+        raise RuntimeError(f"{path}: struct layout differs from this binding (rebuild it)")
     L.swe_params_default.argtypes = [ctypes.POINTER(SweParams)]
     L.swe_params_default.restype = None
     L.swe_create.argtypes = [ctypes.POINTER(SweParams), ctypes.POINTER(vp)]

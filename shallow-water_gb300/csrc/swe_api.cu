@@ -229,6 +229,9 @@ void build_maps(swe_ctx *c) {
 
 extern "C" {
 
+size_t swe_params_size(void) { return sizeof(swe_params); }
+size_t swe_snapshot_params_size(void) { return sizeof(swe_snapshot_params); }
+
 void swe_params_default(swe_params *p) {
     if (!p) return;
     std::memset(p, 0, sizeof *p);

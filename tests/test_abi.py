@@ -35,6 +35,13 @@ def test_params_default(sw):
     p = sw._lib.SweParams()
     L.swe_params_default(ctypes.byref(p))
     assert (p.nG, p.Lx, p.Ly, p.g, p.cfl, p.bc, p.precision) == (2, 1.0, 1.0, 9.80665, 0.45, 0, 0)
+    assert (p.scheme, p.reconstruction, p.riemann, p.bathymetry) == (0, 1, 0, 1)
+
+
+def test_struct_layouts_match_the_binding(sw):
+    L = sw.lib()
+    assert L.swe_params_size() == ctypes.sizeof(sw._lib.SweParams)
+    assert L.swe_snapshot_params_size() == ctypes.sizeof(sw._lib.SnapshotParams)
 
 
 @pytest.mark.parametrize("field,value", [("nG", 1), ("Nx", 1), ("Ny", 0), ("Lx", 0.0),
