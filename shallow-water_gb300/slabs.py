@@ -146,6 +146,15 @@ class SlabGrid:
             self.time += d
         return self.time
 
+    def write_snapshot(self, writer, **metadata):
+        """Appends the whole grid's state to an ``output.NetCDFWriter`` (one record at
+        ``self.time``).  The slabs are gathered first, as the reference's 4-GPU solver
+        gathers to one host before writing; with ranks, the rank holding slab 0 writes
+        and the others pass ``writer=None``."""
+        state = self.download()
+        if self.comm is None or self.comm.rank == 0:
+            writer.write_snapshot(state, self.time, **metadata)
+
     def download(self):
         """The whole grid's (h, hu, hv), ghosts by the wall rule, on every process."""
         pieces = {k: s.download() for k, s in self.local.items()}

@@ -84,9 +84,17 @@ def gloo_worker(rank, world, port_no, Nx, Ny, bc, steps, out_dir):
         grid = slabs.SlabGrid(Nx, Ny, bc=bc, comm=slabs.TorchComm(),
                               make_local=make_oracle_local(Ny, port.G_REFERENCE, 0.45, bc))
         grid.upload(h, hu, hv, B)
+        writer = None
+        if rank == 0:  # the gathered grid as NetCDF records, written by rank 0 alone
+            out_mod = importlib.import_module("shallow-water_gb300.output")
+            writer = out_mod.NetCDFWriter(os.path.join(out_dir, "slabs.nc"), (Nx, Ny, 1.0, 1.0))
+            writer.write_bathymetry(B)
+        grid.write_snapshot(writer, dt=0.0, backend="GB300")
         t = grid.step(steps)
+        grid.write_snapshot(writer)
         out = grid.download()
         if rank == 0:
+            writer.close()
             np.savez(os.path.join(out_dir, "slabs.npz"), h=out[0], hu=out[1], hv=out[2], t=t)
         dist.barrier()
     finally:

@@ -63,6 +63,14 @@ def test_slabs_gloo_ranks_bitwise(port, tmp_path, world, bc):
     assert float(r["t"]) == t_want
     for k, b in zip(("h", "hu", "hv"), want):
         assert np.array_equal(r[k], b)
+    # the records rank 0 wrote from the gathered slabs: t = 0 and the end state
+    from ncclassic import ClassicFile
+    f = ClassicFile(os.path.join(tmp_path, "slabs.nc"))
+    assert f.numrecs == 2 and f.read("time").tolist() == [0.0, t_want]
+    h0 = so.case(Nx, Ny, bc, 5)[0]
+    assert np.array_equal(f.read("h")[0].astype(np.float64), h0[2:-2, 2:-2])
+    for k, b in zip(("h", "hu", "hv"), want):
+        assert np.array_equal(f.read(k)[1].astype(np.float64), b[2:-2, 2:-2])
 
 
 @pytest.mark.gpu
