@@ -276,7 +276,7 @@ struct AdjTile {
 };
 
 template <class T, int STAGE>
-__global__ void __launch_bounds__(ATT) k_adj_tile(const AdjParams<T> a) {
+__global__ void __launch_bounds__(ATT, 4) k_adj_tile(const AdjParams<T> a) {
     extern __shared__ __align__(16) unsigned char adj_smem[];
     AdjTile<T> &t = *reinterpret_cast<AdjTile<T> *>(adj_smem);
     const int tid = threadIdx.x;

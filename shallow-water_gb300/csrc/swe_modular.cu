@@ -26,7 +26,9 @@
 namespace swe {
 namespace mod {
 
-constexpr int TI = 8, TJ = 32, NT = TI * TJ;  // tile: 8 x-rows by 32 y-columns
+// tile: 8 x-rows by 32 y-columns; 288 threads, so that the tile's 552 interfaces are at
+// most two per thread (with 256, a few threads took four and the rest waited at the barrier)
+constexpr int TI = 8, TJ = 32, NT = (TI + 1) * TJ;
 constexpr int RI = TI + 4, RJ = TJ + 4;        // staged rows / columns (2-cell halo)
 constexpr double EPS = 1.0e-8;                 // constants::eps (include/constants.hpp:5)
 constexpr double H_FLOOR = 1.0e-8;             // serial_solver.hpp:454
@@ -275,31 +277,34 @@ __global__ void __launch_bounds__(NT) k_modular_stage(const ModParams p) {
     }
     __syncthreads();
     bool fail = false;
-    // x-interfaces between staged rows a+1 and a+2 (interior rows i0+a-1 and i0+a)
-    for (int e = tid; e < (TI + 1) * TJ; e += NT) {
-        const int a = e / TJ, c = e - a * TJ;
-        if (i0 + a - 1 > p.Nx - 1 || j0 + c >= p.Ny) continue;
-        double f[4];
-        interface_flux<RECON, RIEMANN, BATHY, 0>(t, a + 1, c + 2, p.g, p.half_g, f, &fail);
+    // x-interfaces between staged rows a+1 and a+2 (interior rows i0+a-1 and i0+a): one
+    // per thread
+    {
+        const int a = tid / TJ, c = tid - a * TJ;
+        if (i0 + a - 1 <= p.Nx - 1 && j0 + c < p.Ny) {
+            double f[4];
+            interface_flux<RECON, RIEMANN, BATHY, 0>(t, a + 1, c + 2, p.g, p.half_g, f, &fail);
 #pragma unroll
-        for (int q = 0; q < 4; ++q) t.fx[q][a][c] = f[q];
+            for (int q = 0; q < 4; ++q) t.fx[q][a][c] = f[q];
+        }
     }
-    // y-interfaces between staged columns b+1 and b+2
-    for (int e = tid; e < TI * (TJ + 1); e += NT) {
-        const int r = e / (TJ + 1), b = e - r * (TJ + 1);
-        if (i0 + r >= p.Nx || j0 + b - 1 > p.Ny - 1) continue;
-        double f[4];
-        interface_flux<RECON, RIEMANN, BATHY, 1>(t, r + 2, b + 1, p.g, p.half_g, f, &fail);
-        t.fy[0][r][b] = f[0];
-        t.fy[1][r][b] = f[3];  // hu
-        t.fy[2][r][b] = f[1];  // hv of G^-
-        t.fy[3][r][b] = f[2];  // hv of G^+
+    // y-interfaces between staged columns b+1 and b+2: threads 0 .. TI * (TJ + 1) - 1
+    if (tid < TI * (TJ + 1)) {
+        const int r = tid / (TJ + 1), b = tid - r * (TJ + 1);
+        if (i0 + r < p.Nx && j0 + b - 1 <= p.Ny - 1) {
+            double f[4];
+            interface_flux<RECON, RIEMANN, BATHY, 1>(t, r + 2, b + 1, p.g, p.half_g, f, &fail);
+            t.fy[0][r][b] = f[0];
+            t.fy[1][r][b] = f[3];  // hu
+            t.fy[2][r][b] = f[1];  // hv of G^-
+            t.fy[3][r][b] = f[2];  // hv of G^+
+        }
     }
     __syncthreads();
     const int r = tid / TJ, c = tid - (tid / TJ) * TJ;
     const int i = i0 + r, j = j0 + c;
     bool bad = false;
-    if (i < p.Nx && j < p.Ny) {
+    if (r < TI && i < p.Nx && j < p.Ny) {
         // FiniteVolumeBathy / FiniteVolume::apply_spatial_operator: F^-(i) - F^+(i-1)
         double rhs[3];
         rhs[0] = p.nidx * (t.fx[0][r + 1][c] - t.fx[0][r][c]) - p.idy * (t.fy[0][r][c + 1] - t.fy[0][r][c]);
