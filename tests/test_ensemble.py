@@ -3,7 +3,6 @@ its own CFL dt, equals the CPU oracle run on that instance alone (FP64: bitwise;
 bitwise equal to the single-grid FP32 path), for every schedule the autotuner can pick."""
 from __future__ import annotations
 
-import numpy as np
 import pytest
 
 from conftest import bitwise_equal

@@ -6,8 +6,6 @@ against the allocating swe_totals on the same state, twice in a row (the second 
 meets the first call's leftovers in the shared scratch)."""
 from __future__ import annotations
 
-import ctypes
-
 import numpy as np
 import pytest
 
