@@ -31,6 +31,7 @@ namespace mod {
 constexpr int TI = 8, TJ = 32, NT = (TI + 1) * TJ;
 constexpr int RI = TI + 4, RJ = TJ + 4;        // staged rows / columns (2-cell halo)
 constexpr double EPS = 1.0e-8;                 // constants::eps (include/constants.hpp:5)
+constexpr int64_t EPS_BITS = 0x3E45798EE2308C3ALL;  // bits of 1.0e-8
 constexpr double H_FLOOR = 1.0e-8;             // serial_solver.hpp:454
 
 struct CS {
@@ -43,8 +44,11 @@ struct CSV {
     double h, hu, hv, u, v;
 };
 
-__device__ __forceinline__ double dmin(double a, double b) { return (b < a) ? b : a; }
-__device__ __forceinline__ double dmax(double a, double b) { return (a < b) ? b : a; }
+// Comparisons, min / max, |x|, 0.5 x and minmod on the bit patterns (swe_f64_exact.cuh):
+// the IEEE decisions and values, NaN included, off the FP64 pipe, which otherwise spends
+// about a third of its issue slots on them here.
+__device__ __forceinline__ double dmin(double a, double b) { return x64::dmin(a, b); }  // std::min
+__device__ __forceinline__ double dmax(double a, double b) { return x64::dmax(a, b); }  // std::max
 
 // IEEE division and square root, correctly rounded on the integer pipes
 // (swe_soft_f64.cuh): the same results as the FP64 unit's, off the FP64 pipe.
@@ -53,7 +57,7 @@ __device__ __forceinline__ double dsqrt(double a) { return sf::sqrt_rn(a); }
 
 __device__ __forceinline__ CSV with_velocity(const CS &s) {
     CSV r{s.h, s.hu, s.hv, 0.0, 0.0};
-    if (s.h > EPS) sf::div2_rn(s.hu, s.hv, s.h, r.u, r.v);
+    if (x64::gt_pos_const(s.h, EPS_BITS)) sf::div2_rn(s.hu, s.hv, s.h, r.u, r.v);  // h > eps
     return r;
 }
 
@@ -72,8 +76,8 @@ __device__ __forceinline__ CS hll(double g, double half_g, const CSV &A, const C
     const double cA = dsqrt(g * A.h), cB = dsqrt(g * B.h);
     const double sR = dmax(uA + cA, uB + cB);
     const double sL = dmin(uA - cA, uB - cB);
-    if (sL >= 0.0) return phys_flux<DIR>(half_g, A);
-    if (sL < 0.0 && sR > 0.0) {
+    if (x64::le(0.0, sL)) return phys_flux<DIR>(half_g, A);
+    if (x64::lt(sL, 0.0) && x64::lt(0.0, sR)) {
         const CS FA = phys_flux<DIR>(half_g, A), FB = phys_flux<DIR>(half_g, B);
         const double ss = sL * sR, d = sR - sL;
         CS r;
@@ -82,7 +86,7 @@ __device__ __forceinline__ CS hll(double g, double half_g, const CSV &A, const C
         r.hv = ddiv(sR * FA.hv - sL * FB.hv + ss * (B.hv - A.hv), d);
         return r;
     }
-    if (sR <= 0.0) return phys_flux<DIR>(half_g, B);
+    if (x64::le(sR, 0.0)) return phys_flux<DIR>(half_g, B);
     *fail = true;
     return {0.0, 0.0, 0.0};
 }
@@ -92,11 +96,12 @@ template <int DIR>
 __device__ __forceinline__ CS rusanov(double g, double half_g, const CSV &A, const CSV &B) {
     const double uA = DIR == 0 ? A.u : A.v, uB = DIR == 0 ? B.u : B.v;
     const double hB = dmax(B.h, 0.0), hA = dmax(A.h, 0.0);
-    const double a = dmax(fabs(uA) + dsqrt(g * hA), fabs(uB) + dsqrt(g * hB));
+    const double a = dmax(x64::fabs_(uA) + dsqrt(g * hA), x64::fabs_(uB) + dsqrt(g * hB));
     const CS FA = phys_flux<DIR>(half_g, A), FB = phys_flux<DIR>(half_g, B);
-    const double ha = 0.5 * a;
-    return {0.5 * (FA.h + FB.h) - ha * (B.h - A.h), 0.5 * (FA.hu + FB.hu) - ha * (B.hu - A.hu),
-            0.5 * (FA.hv + FB.hv) - ha * (B.hv - A.hv)};
+    const double ha = x64::halve(a);  // 0.5 * a
+    return {x64::halve(FA.h + FB.h) - ha * (B.h - A.h),
+            x64::halve(FA.hu + FB.hu) - ha * (B.hu - A.hu),
+            x64::halve(FA.hv + FB.hv) - ha * (B.hv - A.hv)};
 }
 
 // ROE (riemann/ROE.hpp:10-63), compute_roe_avg (:66-69) for u and v over the one
@@ -104,7 +109,7 @@ __device__ __forceinline__ CS rusanov(double g, double half_g, const CSV &A, con
 // written: 0 * x keeps the sign of x and its NaN, as the reference's std::array product.
 template <int DIR>
 __device__ __forceinline__ CS roe(double g, double half_g, const CSV &A, const CSV &B) {
-    const double h = (A.h + B.h) / 2.0;
+    const double h = x64::halve(A.h + B.h);  // (A.h + B.h) / 2.0
     const double c = dsqrt(g * h);
     const double sA = dsqrt(A.h), sB = dsqrt(B.h);
     double u_roe, v_roe;
@@ -114,10 +119,11 @@ __device__ __forceinline__ CS roe(double g, double half_g, const CSV &A, const C
     const double dh = B.h - A.h, dhu = B.hu - A.hu, dhv = B.hv - A.hv;
     const double dqn = DIR == 0 ? dhu : dhv, dqt = DIR == 0 ? dhv : dhu;
     const double q = ddiv(dqn - vn * dh, c);
-    const double alpha1 = 0.5 * (dh - q);
-    const double alpha3 = 0.5 * (dh + q);
+    const double alpha1 = x64::halve(dh - q);
+    const double alpha3 = x64::halve(dh + q);
     const double alpha2 = dqt - vt * dh;
-    const double w1 = fabs(l1) * alpha1, w2 = fabs(l2) * alpha2, w3 = fabs(l3) * alpha3;
+    const double w1 = x64::fabs_(l1) * alpha1, w2 = x64::fabs_(l2) * alpha2,
+                 w3 = x64::fabs_(l3) * alpha3;
     // r1 = {1, l1, v_roe}, r2 = {0, 0, 1}, r3 = {1, l3, v_roe} in x;
     // r1 = {1, u_roe, l1}, r2 = {0, 1, 0}, r3 = {1, u_roe, l3} in y.
     const double r1[3] = {1.0, DIR == 0 ? l1 : u_roe, DIR == 0 ? v_roe : l1};
@@ -125,10 +131,10 @@ __device__ __forceinline__ CS roe(double g, double half_g, const CSV &A, const C
     const double r3[3] = {1.0, DIR == 0 ? l3 : u_roe, DIR == 0 ? v_roe : l3};
     double sum[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) sum[k] = ((r1[k] * w1 + r2[k] * w2) + r3[k] * w3) * 0.5;
+    for (int k = 0; k < 3; ++k) sum[k] = x64::halve((r1[k] * w1 + r2[k] * w2) + r3[k] * w3);
     const CS FA = phys_flux<DIR>(half_g, A), FB = phys_flux<DIR>(half_g, B);
-    return {0.5 * (FA.h + FB.h) - sum[0], 0.5 * (FA.hu + FB.hu) - sum[1],
-            0.5 * (FA.hv + FB.hv) - sum[2]};
+    return {x64::halve(FA.h + FB.h) - sum[0], x64::halve(FA.hu + FB.hu) - sum[1],
+            x64::halve(FA.hv + FB.hv) - sum[2]};
 }
 
 template <int RIEMANN, int DIR>
@@ -140,11 +146,9 @@ __device__ __forceinline__ CS riemann(double g, double half_g, const CS &A0, con
     return roe<DIR>(g, half_g, A, B);
 }
 
-// minmod_scalar (reconstruction/muscl.hpp:7-10)
-__device__ __forceinline__ double minmod_scalar(double a, double b) {
-    if (a * b <= 0.0) return 0.0;
-    return (a > 0.0 ? 1.0 : -1.0) * dmin(fabs(a), fabs(b));
-}
+// minmod_scalar (reconstruction/muscl.hpp:7-10), the same expression as the optimised
+// solver's minmod (HPC_kernels.hpp:41-44), so x64::minmod computes it
+__device__ __forceinline__ double minmod_scalar(double a, double b) { return x64::minmod(a, b); }
 
 struct Tile {
     double w[3][RI][RJ];  // eta (or h), hu, hv of the staged cells
@@ -175,8 +179,8 @@ __device__ __forceinline__ void reconstruct(const Tile &t, int r, int c, CS *A, 
                    minmod_scalar(c0.hv - cm.hv, c1.hv - c0.hv)};
     const CS s1 = {minmod_scalar(c1.h - c0.h, c2.h - c1.h), minmod_scalar(c1.hu - c0.hu, c2.hu - c1.hu),
                    minmod_scalar(c1.hv - c0.hv, c2.hv - c1.hv)};
-    *A = {c0.h + 0.5 * s0.h, c0.hu + 0.5 * s0.hu, c0.hv + 0.5 * s0.hv};
-    *B = {c1.h - 0.5 * s1.h, c1.hu - 0.5 * s1.hu, c1.hv - 0.5 * s1.hv};
+    *A = {c0.h + x64::halve(s0.h), c0.hu + x64::halve(s0.hu), c0.hv + x64::halve(s0.hv)};
+    *B = {c1.h - x64::halve(s1.h), c1.hu - x64::halve(s1.hu), c1.hv - x64::halve(s1.hv)};
 }
 
 // One interface: FluxAssemblyBathy (flux_assembly_bathy.hpp:18-192) or FluxAssembly
@@ -199,12 +203,13 @@ __device__ __forceinline__ void interface_flux(const Tile &t, int r, int c, doub
     const double eta_m = A.h, eta_p = B.h;
     const double b_m = t.b[r][c], b_p = t.b[r + DI][c + DJ];
     const double b_star = dmax(b_m, b_p);
-    const double h_m = dmax(0.0, eta_m - b_m), h_p = dmax(0.0, eta_p - b_p);
+    // positive_height = std::max(0.0, h), i.e. h > 0 ? h : 0.0
+    const double h_m = x64::positive_part(eta_m - b_m), h_p = x64::positive_part(eta_p - b_p);
     // safe_velocity (flux_assembly_bathy.hpp:180-185)
     double u_m = 0.0, v_m = 0.0, u_p = 0.0, v_p = 0.0;
-    if (!(h_m < EPS)) sf::div2_rn(A.hu, A.hv, h_m, u_m, v_m);
-    if (!(h_p < EPS)) sf::div2_rn(B.hu, B.hv, h_p, u_p, v_p);
-    const double hs_m = dmax(0.0, eta_m - b_star), hs_p = dmax(0.0, eta_p - b_star);
+    if (!x64::lt(h_m, EPS)) sf::div2_rn(A.hu, A.hv, h_m, u_m, v_m);
+    if (!x64::lt(h_p, EPS)) sf::div2_rn(B.hu, B.hv, h_p, u_p, v_p);
+    const double hs_m = x64::positive_part(eta_m - b_star), hs_p = x64::positive_part(eta_p - b_star);
     const CS Um = {hs_m, hs_m * u_m, hs_m * v_m}, Up = {hs_p, hs_p * u_p, hs_p * v_p};
     const CS F = riemann<RIEMANN, DIR>(g, half_g, Um, Up, fail);
     const double corr_m = half_g * (h_m * h_m - hs_m * hs_m);
@@ -324,12 +329,13 @@ __global__ void __launch_bounds__(NT) k_modular_stage(const ModParams p) {
                 o[f] = 1.0 / 3.0 * un[f][k] + 2.0 / 3.0 * s + p.c3 * rhs[f];  // compute_U_next
         }
         if (BATHY) {  // enforce_positivity (serial_solver.hpp:453-478)
-            if (o[0] < H_FLOOR) {
+            if (x64::lt(o[0], H_FLOOR)) {
                 o[0] = H_FLOOR;
                 o[1] = 0.0;
                 o[2] = 0.0;
             }
-            bad = !isfinite(o[0]) || !isfinite(o[1]) || !isfinite(o[2]);
+            auto finite = [](double x) { return (x64::bits(x) & x64::ABS) < x64::INF_BITS; };
+            bad = !finite(o[0]) || !finite(o[1]) || !finite(o[2]);
         }
         p.ho[k] = o[0];
         p.huo[k] = o[1];
