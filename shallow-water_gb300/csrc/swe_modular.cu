@@ -62,23 +62,21 @@ __device__ __forceinline__ CSV with_velocity(const CS &s) {
 }
 
 // RiemannSolver::F / G (riemann/riemann.hpp:10-19); half_g = 0.5 * g (exact).
-template <int DIR>
-__device__ __forceinline__ CS phys_flux(double half_g, const CSV &U) {
+__device__ __forceinline__ CS phys_flux(int DIR, double half_g, const CSV &U) {
     if (DIR == 0) return {U.hu, U.u * U.u * U.h + half_g * U.h * U.h, U.hu * U.v};
     return {U.hv, U.hu * U.v, U.h * U.v * U.v + half_g * U.h * U.h};
 }
 
 // HLL (riemann/HLL.hpp:10-45).  Sets *fail where the reference throws "HLL could not
 // provide dissipation speed." (NaN speeds).
-template <int DIR>
-__device__ __forceinline__ CS hll(double g, double half_g, const CSV &A, const CSV &B, bool *fail) {
+__device__ __forceinline__ CS hll(int DIR, double g, double half_g, const CSV &A, const CSV &B, bool *fail) {
     const double uA = DIR == 0 ? A.u : A.v, uB = DIR == 0 ? B.u : B.v;
     const double cA = dsqrt(g * A.h), cB = dsqrt(g * B.h);
     const double sR = dmax(uA + cA, uB + cB);
     const double sL = dmin(uA - cA, uB - cB);
-    if (x64::le(0.0, sL)) return phys_flux<DIR>(half_g, A);
+    if (x64::le(0.0, sL)) return phys_flux(DIR, half_g, A);
     if (x64::lt(sL, 0.0) && x64::lt(0.0, sR)) {
-        const CS FA = phys_flux<DIR>(half_g, A), FB = phys_flux<DIR>(half_g, B);
+        const CS FA = phys_flux(DIR, half_g, A), FB = phys_flux(DIR, half_g, B);
         const double ss = sL * sR, d = sR - sL;
         CS r;
         sf::div2_rn(sR * FA.h - sL * FB.h + ss * (B.h - A.h),
@@ -86,18 +84,17 @@ __device__ __forceinline__ CS hll(double g, double half_g, const CSV &A, const C
         r.hv = ddiv(sR * FA.hv - sL * FB.hv + ss * (B.hv - A.hv), d);
         return r;
     }
-    if (x64::le(sR, 0.0)) return phys_flux<DIR>(half_g, B);
+    if (x64::le(sR, 0.0)) return phys_flux(DIR, half_g, B);
     *fail = true;
     return {0.0, 0.0, 0.0};
 }
 
 // Rusanov (riemann/rusanov.hpp:12-30)
-template <int DIR>
-__device__ __forceinline__ CS rusanov(double g, double half_g, const CSV &A, const CSV &B) {
+__device__ __forceinline__ CS rusanov(int DIR, double g, double half_g, const CSV &A, const CSV &B) {
     const double uA = DIR == 0 ? A.u : A.v, uB = DIR == 0 ? B.u : B.v;
     const double hB = dmax(B.h, 0.0), hA = dmax(A.h, 0.0);
     const double a = dmax(x64::fabs_(uA) + dsqrt(g * hA), x64::fabs_(uB) + dsqrt(g * hB));
-    const CS FA = phys_flux<DIR>(half_g, A), FB = phys_flux<DIR>(half_g, B);
+    const CS FA = phys_flux(DIR, half_g, A), FB = phys_flux(DIR, half_g, B);
     const double ha = x64::halve(a);  // 0.5 * a
     return {x64::halve(FA.h + FB.h) - ha * (B.h - A.h),
             x64::halve(FA.hu + FB.hu) - ha * (B.hu - A.hu),
@@ -107,8 +104,7 @@ __device__ __forceinline__ CS rusanov(double g, double half_g, const CSV &A, con
 // ROE (riemann/ROE.hpp:10-63), compute_roe_avg (:66-69) for u and v over the one
 // denominator sqrt(h1) + sqrt(h2).  The eigenvectors' 0 and 1 entries are multiplied as
 // written: 0 * x keeps the sign of x and its NaN, as the reference's std::array product.
-template <int DIR>
-__device__ __forceinline__ CS roe(double g, double half_g, const CSV &A, const CSV &B) {
+__device__ __forceinline__ CS roe(int DIR, double g, double half_g, const CSV &A, const CSV &B) {
     const double h = x64::halve(A.h + B.h);  // (A.h + B.h) / 2.0
     const double c = dsqrt(g * h);
     const double sA = dsqrt(A.h), sB = dsqrt(B.h);
@@ -132,18 +128,18 @@ __device__ __forceinline__ CS roe(double g, double half_g, const CSV &A, const C
     double sum[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) sum[k] = x64::halve((r1[k] * w1 + r2[k] * w2) + r3[k] * w3);
-    const CS FA = phys_flux<DIR>(half_g, A), FB = phys_flux<DIR>(half_g, B);
+    const CS FA = phys_flux(DIR, half_g, A), FB = phys_flux(DIR, half_g, B);
     return {x64::halve(FA.h + FB.h) - sum[0], x64::halve(FA.hu + FB.hu) - sum[1],
             x64::halve(FA.hv + FB.hv) - sum[2]};
 }
 
-template <int RIEMANN, int DIR>
-__device__ __forceinline__ CS riemann(double g, double half_g, const CS &A0, const CS &B0,
-                                      bool *fail) {
+template <int RIEMANN>
+__device__ __forceinline__ CS riemann(int DIR, double g, double half_g, const CS &A0,
+                                      const CS &B0, bool *fail) {
     const CSV A = with_velocity(A0), B = with_velocity(B0);
-    if (RIEMANN == 0) return hll<DIR>(g, half_g, A, B, fail);
-    if (RIEMANN == 1) return rusanov<DIR>(g, half_g, A, B);
-    return roe<DIR>(g, half_g, A, B);
+    if (RIEMANN == 0) return hll(DIR, g, half_g, A, B, fail);
+    if (RIEMANN == 1) return rusanov(DIR, g, half_g, A, B);
+    return roe(DIR, g, half_g, A, B);
 }
 
 // minmod_scalar (reconstruction/muscl.hpp:7-10), the same expression as the optimised
@@ -166,8 +162,9 @@ __device__ __forceinline__ CS cell(const Tile &t, int r, int c) {
 
 // U_L / U_B and U_R / U_T of the interface between staged cells (r, c) and
 // (r + DI, c + DJ): PiecewiseConst (piecewise_const.hpp:11-30) or MUSCL (muscl.hpp:14-66).
-template <int RECON, int DI, int DJ>
-__device__ __forceinline__ void reconstruct(const Tile &t, int r, int c, CS *A, CS *B) {
+template <int RECON>
+__device__ __forceinline__ void reconstruct(const Tile &t, int r, int c, int DI, int DJ, CS *A,
+                                            CS *B) {
     const CS c0 = cell(t, r, c), c1 = cell(t, r + DI, c + DJ);
     if (RECON == 0) {
         *A = c0;
@@ -185,14 +182,14 @@ __device__ __forceinline__ void reconstruct(const Tile &t, int r, int c, CS *A, 
 
 // One interface: FluxAssemblyBathy (flux_assembly_bathy.hpp:18-192) or FluxAssembly
 // (flux_assembly.hpp:11-45).  out: h, hu / hv of F^-, the same of F^+, the other momentum.
-template <int RECON, int RIEMANN, bool BATHY, int DIR>
-__device__ __forceinline__ void interface_flux(const Tile &t, int r, int c, double g,
+template <int RECON, int RIEMANN, bool BATHY>
+__device__ __forceinline__ void interface_flux(int DIR, const Tile &t, int r, int c, double g,
                                                double half_g, double out[4], bool *fail) {
-    constexpr int DI = DIR == 0 ? 1 : 0, DJ = DIR == 0 ? 0 : 1;
+    const int DI = DIR == 0 ? 1 : 0, DJ = DIR == 0 ? 0 : 1;
     CS A, B;
-    reconstruct<RECON, DI, DJ>(t, r, c, &A, &B);
+    reconstruct<RECON>(t, r, c, DI, DJ, &A, &B);
     if (!BATHY) {
-        const CS F = riemann<RIEMANN, DIR>(g, half_g, A, B, fail);
+        const CS F = riemann<RIEMANN>(DIR, g, half_g, A, B, fail);
         const double qn = DIR == 0 ? F.hu : F.hv, qt = DIR == 0 ? F.hv : F.hu;
         out[0] = F.h;
         out[1] = qn;
@@ -211,7 +208,7 @@ __device__ __forceinline__ void interface_flux(const Tile &t, int r, int c, doub
     if (!x64::lt(h_p, EPS)) sf::div2_rn(B.hu, B.hv, h_p, u_p, v_p);
     const double hs_m = x64::positive_part(eta_m - b_star), hs_p = x64::positive_part(eta_p - b_star);
     const CS Um = {hs_m, hs_m * u_m, hs_m * v_m}, Up = {hs_p, hs_p * u_p, hs_p * v_p};
-    const CS F = riemann<RIEMANN, DIR>(g, half_g, Um, Up, fail);
+    const CS F = riemann<RIEMANN>(DIR, g, half_g, Um, Up, fail);
     const double corr_m = half_g * (h_m * h_m - hs_m * hs_m);
     const double corr_p = half_g * (h_p * h_p - hs_p * hs_p);
     const double qn = DIR == 0 ? F.hu : F.hv, qt = DIR == 0 ? F.hv : F.hu;
@@ -282,27 +279,39 @@ __global__ void __launch_bounds__(NT) k_modular_stage(const ModParams p) {
     }
     __syncthreads();
     bool fail = false;
-    // x-interfaces between staged rows a+1 and a+2 (interior rows i0+a-1 and i0+a): one
-    // per thread
-    {
-        const int a = tid / TJ, c = tid - a * TJ;
-        if (i0 + a - 1 <= p.Nx - 1 && j0 + c < p.Ny) {
-            double f[4];
-            interface_flux<RECON, RIEMANN, BATHY, 0>(t, a + 1, c + 2, p.g, p.half_g, f, &fail);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) t.fx[q][a][c] = f[q];
+    // One interface per thread and direction: the x-interface between staged rows a+1 and
+    // a+2 (interior rows i0+a-1 and i0+a), then, for the first TI * (TJ + 1) threads, the
+    // y-interface between staged columns b+1 and b+2.  Both directions run through one
+    // copy of the interface code (a loop, not unrolled): two inlined copies of it
+    // stalled the kernel on instruction fetch.
+#pragma unroll 1
+    for (int dir = 0; dir < 2; ++dir) {
+        int r, c, q0, q1;  // staged cell of the interface's minus side; shared slots
+        bool valid;
+        if (dir == 0) {
+            q0 = tid / TJ;
+            q1 = tid - q0 * TJ;
+            valid = i0 + q0 - 1 <= p.Nx - 1 && j0 + q1 < p.Ny;
+            r = q0 + 1;
+            c = q1 + 2;
+        } else {
+            q0 = tid / (TJ + 1);
+            q1 = tid - q0 * (TJ + 1);
+            valid = tid < TI * (TJ + 1) && i0 + q0 < p.Nx && j0 + q1 - 1 <= p.Ny - 1;
+            r = q0 + 2;
+            c = q1 + 1;
         }
-    }
-    // y-interfaces between staged columns b+1 and b+2: threads 0 .. TI * (TJ + 1) - 1
-    if (tid < TI * (TJ + 1)) {
-        const int r = tid / (TJ + 1), b = tid - r * (TJ + 1);
-        if (i0 + r < p.Nx && j0 + b - 1 <= p.Ny - 1) {
-            double f[4];
-            interface_flux<RECON, RIEMANN, BATHY, 1>(t, r + 2, b + 1, p.g, p.half_g, f, &fail);
-            t.fy[0][r][b] = f[0];
-            t.fy[1][r][b] = f[3];  // hu
-            t.fy[2][r][b] = f[1];  // hv of G^-
-            t.fy[3][r][b] = f[2];  // hv of G^+
+        if (!valid) continue;
+        double f[4];
+        interface_flux<RECON, RIEMANN, BATHY>(dir, t, r, c, p.g, p.half_g, f, &fail);
+        if (dir == 0) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) t.fx[q][q0][q1] = f[q];
+        } else {
+            t.fy[0][q0][q1] = f[0];
+            t.fy[1][q0][q1] = f[3];  // hu
+            t.fy[2][q0][q1] = f[1];  // hv of G^-
+            t.fy[3][q0][q1] = f[2];  // hv of G^+
         }
     }
     __syncthreads();
