@@ -141,6 +141,22 @@ int swe_download(swe_ctx *ctx, double *h, double *hu, double *hv);
  * without a dissipation speed (swe_last_error names which). */
 int swe_step(swe_ctx *ctx, int n_steps, double dt, double *t_inout);
 
+/* swe_upload(h, hu, hv, B) + swe_step(n_steps, dt, t_inout) + swe_download(h_out,
+ * hu_out, hv_out) in one call, with the same results, for a host that holds the state
+ * between steps (the reference's SolverAssembly loop, whose solvers keep h_, hu_, hv_ in
+ * host memory).  The FP64 fused scheme on one grid overlaps the transfers with the
+ * stage kernels: the state is uploaded in bands of rows while the first stage computes
+ * the flux divergence of the bands already resident and reduces their wave speeds (the
+ * step's dt is applied once every band is in), and the last stage runs by bands whose
+ * rows are copied back while the next band computes.  Host arrays in page-locked memory
+ * overlap; pageable ones give the same results without overlap.  The outputs may be the
+ * input arrays.  Other forms and slab contexts run the three calls in sequence.  No
+ * reference counterpart: the reference's GPU backends upload once and download per
+ * output (cuda_solver.hpp:277-296). */
+int swe_step_host(swe_ctx *ctx, const double *h, const double *hu, const double *hv,
+                  const double *B, double *h_out, double *hu_out, double *hv_out, int n_steps,
+                  double dt, double *t_inout);
+
 /* ---- Slabs (x-decomposition over several GPUs) ---------------------------------------
  * The reference's 4-GPU backend splits x into slabs (build_subdomains,
  * cuda_solver_4gpu.hpp:281-304) and exchanges two ghost rows per neighbour after every

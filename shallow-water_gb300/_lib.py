@@ -33,7 +33,7 @@ RIEMANN_SOLVERS = {"HLL": 0, "Rusanov": 1, "ROE": 2}
 # Every symbol include/swe_gb300.h declares.
 EXPORTS = (
     "swe_params_default", "swe_create", "swe_destroy", "swe_upload", "swe_download",
-    "swe_step", "swe_max_wave_speed", "swe_stable_dt", "swe_dt_log", "swe_last_error",
+    "swe_step", "swe_step_host", "swe_max_wave_speed", "swe_stable_dt", "swe_dt_log", "swe_last_error",
     "swe_status_string", "swe_kernel_launches", "swe_last_step_ms", "swe_totals",
     "swe_ens_create", "swe_ens_destroy", "swe_ens_upload", "swe_ens_download", "swe_ens_step",
     "swe_ens_times", "swe_ens_last_dt", "swe_ens_last_step_ms", "swe_ens_kernel_launches",
@@ -126,6 +126,9 @@ def lib(path: str = LIB_PATH):
     L.swe_download.restype = ctypes.c_int
     L.swe_step.argtypes = [vp, ctypes.c_int, ctypes.c_double, dp]
     L.swe_step.restype = ctypes.c_int
+    L.swe_step_host.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp, ctypes.c_int, ctypes.c_double,
+                                dp]
+    L.swe_step_host.restype = ctypes.c_int
     L.swe_max_wave_speed.argtypes = [vp, dp]
     L.swe_max_wave_speed.restype = ctypes.c_int
     L.swe_stable_dt.argtypes = [vp, dp]

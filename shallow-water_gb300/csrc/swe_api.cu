@@ -196,6 +196,18 @@ int refresh_speed(swe_ctx *c) {
     return SWE_OK;
 }
 
+// Room for one dt per step of a call in the device dt record.
+int ensure_dt_log(swe_ctx *c, int n_steps) {
+    if (c->dt_log_cap >= n_steps) return SWE_OK;
+    if (c->dt_log) CK(cudaFree(c->dt_log));
+    c->dt_log = nullptr;
+    c->dt_log_cap = 0;
+    const int cap = std::max(n_steps, 1024);
+    CK(cudaMalloc(&c->dt_log, (size_t)cap * sizeof(double)));
+    c->dt_log_cap = cap;
+    return SWE_OK;
+}
+
 cudaError_t launch_stage(swe_ctx *c, int stage, const StageParams &sp) {
     if (fp32(c))
         return launch_stage_f32(stage, sp, c->maps_ok ? &c->maps[stage - 1] : nullptr, c->stream);
@@ -370,6 +382,8 @@ void swe_destroy(swe_ctx *c) {
     if (c->base) cudaFree(c->base);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    for (cudaEvent_t e : c->band_ev) cudaEventDestroy(e);
+    if (c->xfer) cudaStreamDestroy(c->xfer);
     if (c->stream) cudaStreamDestroy(c->stream);
     cudaGetLastError();
     delete c;
@@ -460,14 +474,8 @@ int swe_step(swe_ctx *c, int n_steps, double dt, double *t_inout) {
     int st = set_device(c);
     if (st) return st;
     if (modular(c)) return step_modular(c, n_steps, dt, t_inout);
-    if (c->dt_log_cap < n_steps) {
-        if (c->dt_log) CK(cudaFree(c->dt_log));
-        c->dt_log = nullptr;
-        c->dt_log_cap = 0;
-        const int cap = std::max(n_steps, 1024);
-        CK(cudaMalloc(&c->dt_log, (size_t)cap * sizeof(double)));
-        c->dt_log_cap = cap;
-    }
+    st = ensure_dt_log(c, n_steps);
+    if (st) return st;
     const double t0 = t_inout ? *t_inout : 0.0;
     CK(cudaMemcpyAsync(c->t_accum, &t0, sizeof(double), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemsetAsync(c->flags, 0, sizeof(int), c->stream));
@@ -499,6 +507,150 @@ int swe_step(swe_ctx *c, int n_steps, double dt, double *t_inout) {
     double t1 = 0.0;
     CK(cudaMemcpyAsync(&flags, c->flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(&t1, c->t_accum, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    c->last_ms = ms;
+    c->last_steps = n_steps;
+    if (t_inout) *t_inout = t1;
+    if (flags & FLAG_TIMEOUT)
+        return fail(c, SWE_ERR_TIMEOUT, "a tile's TMA copy did not complete (state undefined)");
+    if (flags & FLAG_NONFINITE)
+        return fail(c, SWE_ERR_NONFINITE, "non-finite state detected in GB300 solver");
+    return SWE_OK;
+}
+
+// swe_step_host: bands of about 64 tile rows (512 grid rows), at most kMaxBands.
+constexpr int kBandTileRows = 64, kMaxBands = 32;
+
+int swe_step_host(swe_ctx *c, const double *h, const double *hu, const double *hv,
+                  const double *B, double *h_out, double *hu_out, double *hv_out, int n_steps,
+                  double dt, double *t_inout) {
+    if (!c || !h || !hu || !hv || !h_out || !hu_out || !hv_out || n_steps < 0)
+        return fail(c, SWE_ERR_BAD_ARG, "swe_step_host: bad argument");
+    if (!(dt == dt)) return fail(c, SWE_ERR_BAD_ARG, "swe_step_host: dt is NaN");
+    if (!c->uploaded && !B) return fail(c, SWE_ERR_BAD_ARG, "swe_step_host: first upload needs B");
+    int st = set_device(c);
+    if (st) return st;
+    // The overlapped schedule is the FP64 fused drop-in's on one grid; the other forms run
+    // the same three calls back to back.
+    if (fp32(c) || modular(c) || c->p.x_halo_lo || c->p.x_halo_hi || n_steps == 0) {
+        st = swe_upload(c, h, hu, hv, B);
+        if (st) return st;
+        st = swe_step(c, n_steps, dt, t_inout);
+        if (st) return st;
+        return swe_download(c, h_out, hu_out, hv_out);
+    }
+    st = ensure_dt_log(c, n_steps);
+    if (st) return st;
+    if (!c->xfer) CK(cudaStreamCreateWithFlags(&c->xfer, cudaStreamNonBlocking));
+    while ((int)c->band_ev.size() < 2 * kMaxBands) {
+        cudaEvent_t e = nullptr;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        c->band_ev.push_back(e);
+    }
+    const int Nx = c->p.Nx, Ny = c->p.Ny, R = Nx + 2 * NG;
+    const int tile_rows = (Nx + TILE_I_F64 - 1) / TILE_I_F64;
+    const int nb = std::min(kMaxBands, std::max(1, (tile_rows + kBandTileRows - 1) / kBandTileRows));
+    // Band b: tile rows [T(b), T(b + 1)).  Its stage needs ghosted rows below
+    // T(b + 1) * TI + 4 (the tile, its 2-row halo and the wall ghosts); its interior rows
+    // end at ghosted row T(b + 1) * TI + 2.
+    auto T = [&](int b) { return (int)((long long)tile_rows * b / nb); };
+    auto upto = [&](int b) { return b == nb ? R : std::min(R, T(b) * TILE_I_F64 + 4); };
+    auto done_to = [&](int b) { return b == nb ? R : std::min(R, T(b) * TILE_I_F64 + NG); };
+    const size_t row = (size_t)(Ny + 4) * sizeof(double);
+    const size_t dpitch = (size_t)c->pitch * sizeof(double);
+    cudaEvent_t *up = c->band_ev.data(), *fin = c->band_ev.data() + kMaxBands;
+
+    const double t0 = t_inout ? *t_inout : 0.0;
+    CK(cudaMemcpyAsync(c->t_accum, &t0, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemsetAsync(c->flags, 0, sizeof(int), c->stream));
+    c->steps_done = 0;
+    CK(cudaMemsetAsync(c->speed, 0, sizeof(unsigned long long), c->stream));  // slot 0
+    CK(cudaEventRecord(c->ev0, c->stream));
+    CK(cudaStreamWaitEvent(c->xfer, c->ev0, 0));  // nothing in flight reads U^n any more
+
+    // Upload by bands on the transfer stream; as each band lands, the compute stream
+    // reduces its max wave speed and computes L(U^n) on the tile rows it completes.
+    const double *src[4] = {h, hu, hv, B};
+    void *dst[4] = {c->Un[0], c->Un[1], c->Un[2], c->B};
+    StageParams sp = stage_params(c, dt);
+    sp.slot_read = 0;
+    sp.slot_write = 1;
+    sp.log_index = 0;
+    sp.hs = c->Un[0]; sp.hus = c->Un[1]; sp.hvs = c->Un[2];
+    sp.hn = c->Un[0]; sp.hun = c->Un[1]; sp.hvn = c->Un[2];
+    sp.ho = c->U2[0]; sp.huo = c->U2[1]; sp.hvo = c->U2[2];  // L(U^n), free until stage 2
+    for (int b = 0; b < nb; ++b) {
+        const int r0 = b == 0 ? 0 : upto(b), r1 = upto(b + 1);
+        for (int f = 0; f < 4; ++f) {
+            if (!src[f] || r1 <= r0) continue;
+            CK(cudaMemcpy2DAsync(static_cast<char *>(dst[f]) + (size_t)r0 * dpitch, dpitch,
+                                 src[f] + (size_t)r0 * (Ny + 4), row, row, (size_t)(r1 - r0),
+                                 cudaMemcpyHostToDevice, c->xfer));
+        }
+        CK(cudaEventRecord(up[b], c->xfer));
+        CK(cudaStreamWaitEvent(c->stream, up[b], 0));
+        const int i0 = std::max(r0, NG) - NG, i1 = std::min(r1, Nx + NG) - NG;
+        CK(launch_max_speed_rows_f64(c->Un[0], c->Un[1], c->Un[2], i0, i1, Ny, c->pitch,
+                                     c->p.g, c->speed, c->num_sms, c->stream));
+        CK(launch_stage_f64(0, sp, c->maps_ok ? &c->maps[0] : nullptr, c->stream, T(b),
+                            T(b + 1)));
+        c->launches += 2;
+    }
+    c->uploaded = true;
+    CK(launch_combine1_f64(sp, c->U1[0], c->U1[1], c->U1[2], c->num_sms, c->stream));
+    ++c->launches;
+
+    for (int s = 0; s < n_steps; ++s) {
+        sp.slot_read = (int)(c->steps_done & 1);
+        sp.slot_write = sp.slot_read ^ 1;
+        sp.log_index = s;
+        if (s > 0) {
+            sp.hs = c->Un[0]; sp.hus = c->Un[1]; sp.hvs = c->Un[2];
+            sp.ho = c->U1[0]; sp.huo = c->U1[1]; sp.hvo = c->U1[2];
+            CK(launch_stage(c, 1, sp));
+            ++c->launches;
+        }
+        sp.hs = c->U1[0]; sp.hus = c->U1[1]; sp.hvs = c->U1[2];
+        sp.ho = c->U2[0]; sp.huo = c->U2[1]; sp.hvo = c->U2[2];
+        CK(launch_stage(c, 2, sp));
+        sp.hs = c->U2[0]; sp.hus = c->U2[1]; sp.hvs = c->U2[2];
+        sp.ho = c->Un[0]; sp.huo = c->Un[1]; sp.hvo = c->Un[2];
+        c->launches += 1;
+        if (s + 1 < n_steps) {
+            CK(launch_stage(c, 3, sp));
+            ++c->launches;
+        } else {
+            // Last stage by bands; each finished band's ghosts are filled and the band
+            // copied out while the next band computes.
+            for (int b = 0; b < nb; ++b) {
+                CK(launch_stage_f64(3, sp, c->maps_ok ? &c->maps[2] : nullptr, c->stream, T(b),
+                                    T(b + 1)));
+                const int r0 = b == 0 ? 0 : done_to(b), r1 = done_to(b + 1);
+                CK(launch_fill_ghost_band_f64(c->Un[0], c->Un[1], c->Un[2], Nx, Ny, c->pitch,
+                                              c->p.bc, r0, r1, c->stream));
+                c->launches += 2;
+                CK(cudaEventRecord(fin[b], c->stream));
+                CK(cudaStreamWaitEvent(c->xfer, fin[b], 0));
+                double *out[3] = {h_out, hu_out, hv_out};
+                for (int f = 0; f < 3; ++f) {
+                    if (r1 <= r0) continue;
+                    CK(cudaMemcpy2DAsync(out[f] + (size_t)r0 * (Ny + 4), row,
+                                         static_cast<const char *>(c->Un[f]) + (size_t)r0 * dpitch,
+                                         dpitch, row, (size_t)(r1 - r0), cudaMemcpyDeviceToHost,
+                                         c->xfer));
+                }
+            }
+        }
+        ++c->steps_done;
+    }
+    CK(cudaEventRecord(c->ev1, c->stream));
+    int flags = 0;
+    double t1 = 0.0;
+    CK(cudaMemcpyAsync(&flags, c->flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(&t1, c->t_accum, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->xfer));
     CK(cudaStreamSynchronize(c->stream));
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));

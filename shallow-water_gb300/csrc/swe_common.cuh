@@ -43,6 +43,7 @@ struct StageParams {
     int *flags;                  // FLAG_* bits
     unsigned char *mask;         // optional: 1 where positivity clamped the cell (adjoint)
     int halo_lo, halo_hi;        // x sides whose ghost rows a neighbour slab supplies
+    int tile_row0;               // first tile row of a launch over a band of tile rows
 };
 
 // Ensemble of independent grids (one per instance) in shared field pools.

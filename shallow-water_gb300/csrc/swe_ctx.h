@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/swe_gb300.h"
 #include "swe_tma.cuh"
@@ -30,6 +31,10 @@ struct swe_ctx {
     double dx = 0, dy = 0, inv_dx = 0, inv_dy = 0, cfl_min_dxdy = 0;
     long long launches = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // bracket the stage launches of swe_step
+    // swe_step_host: a transfer stream and one event per band of rows (uploaded /
+    // finished), created on first use.
+    cudaStream_t xfer = nullptr;
+    std::vector<cudaEvent_t> band_ev;
     double last_ms = 0.0;
     double modular_dt = 0.0;   // the modular scheme's fixed dt of the last swe_step
     swe::StageMaps maps[3]{};  // FP32 form: TMA maps of U^n, U^(1), U^(2) (stage sources)

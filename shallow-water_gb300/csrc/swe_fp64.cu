@@ -21,6 +21,8 @@
 // reference's re-division (h*u)/h, which is decided from one exact FMA residual.
 // Divisions and square roots, about twenty FP64-pipe slots each, are computed
 // correctly rounded on the integer pipe (swe_soft_f64.cuh).
+#include <algorithm>
+
 #include "swe_common.cuh"
 #include "swe_f64_exact.cuh"
 #include "swe_soft_f64.cuh"
@@ -65,7 +67,7 @@ __device__ __forceinline__ void safe_velocity2(double q1, double q2, double h, d
 //                    speeds and flux sums, 3 HLL combination, 4 corrections and
 //                    cell update.
 #ifndef SWE_F64_SOFT_MUL
-#define SWE_F64_SOFT_MUL 0x00
+#define SWE_F64_SOFT_MUL 0x10
 #endif
 #ifndef SWE_F64_SOFT_ADD
 #define SWE_F64_SOFT_ADD 0x00
@@ -420,6 +422,12 @@ __device__ __forceinline__ double stage_tile_f64(const StageParams &p, int i0, i
             fsub<4>(x64::neg(mul_const(p.inv_dx, p.kx, fsub<4>(S.xf[1][ty + 1][tx], S.xf[1][ty][tx]))),
                     mul_const(p.inv_dy, p.ky, fsub<4>(S.yf[2][ty][tx + 1], S.yf[3][ty][tx])));
         const long long k = (long long)(ii + NG) * P + (jj + NG);
+        if (STAGE == 0) {  // L(U^n) alone: stage 1 before its dt is known
+            static_cast<double *>(p.ho)[k] = rh;
+            static_cast<double *>(p.huo)[k] = rhu;
+            static_cast<double *>(p.hvo)[k] = rhv;
+            return 0.0;
+        }
         const double sh = hs[k];  // interior cell: no ghost mapping
         const double shu = S.hu[ty + NG][tx + NG];
         const double shv = S.hv[ty + NG][tx + NG];
@@ -482,26 +490,72 @@ constexpr int ens_min_blocks(int TI, int TJ) {
                ? SWE_ENS_F64_THREADS_PER_SM / ((TI + 1) * TJ) : 1;
 }
 
-// Single grid: one CTA per tile.
+// Single grid: one CTA per tile, over tile rows p.tile_row0 + blockIdx.y.  STAGE 0 is
+// stage 1 without its dt: it stores L(U^n) in the output buffers, and k_combine1_f64
+// forms U^(1) once the max wave speed is reduced.
 template <int TI, int TJ, int STAGE>
 __global__ void __launch_bounds__((TI + 1) * TJ, min_blocks(TI, TJ))
     k_stage_f64(const StageParams p, const __grid_constant__ CUtensorMap tm_h,
                 const __grid_constant__ CUtensorMap tm_u,
                 const __grid_constant__ CUtensorMap tm_v,
                 const __grid_constant__ CUtensorMap tm_b, int use_tma) {
-    const double dt = stage_dt(p);
+    const double dt = STAGE == 0 ? 0.0 : stage_dt(p);
     const tma::TileMaps maps{&tm_h, &tm_u, &tm_v, &tm_b};
-    const double speed = stage_tile_f64<TI, TJ, STAGE>(p, blockIdx.y * TI, blockIdx.x * TJ, dt,
+    const int tr = p.tile_row0 + (int)blockIdx.y;
+    const double speed = stage_tile_f64<TI, TJ, STAGE>(p, tr * TI, blockIdx.x * TJ, dt,
                                                        use_tma ? &maps : nullptr);
-    if (STAGE == 1 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+    const bool first = blockIdx.x == 0 && tr == 0 && threadIdx.x == 0;
+    if (STAGE == 1 && first) {
         p.speed[p.slot_write] = 0ull;  // read by nobody until stage 3 of this step
         if (p.dt_log) p.dt_log[p.log_index] = dt;
     }
     if (STAGE == 3) {
         block_max_to_slot(speed, p.speed + p.slot_write);
-        if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && p.t_accum)
-            *p.t_accum += dt;
+        if (first && p.t_accum) *p.t_accum += dt;
     }
+}
+
+// The rest of stage 1 after k_stage_f64<.., 0>: U^(1) = U^n + dt L(U^n) with the
+// positivity correction and the non-finite check, the same operations in the same
+// order as the fused stage (HPC_solver.hpp:246-248, HPC_kernels.hpp:305-312).
+// p.ho/huo/hvo hold L on entry (read) and receive U^(1) through (o_h, o_hu, o_hv).
+__global__ void __launch_bounds__(256) k_combine1_f64(const StageParams p, double *o_h,
+                                                      double *o_hu, double *o_hv) {
+    const double dt = stage_dt(p);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        p.speed[p.slot_write] = 0ull;
+        if (p.dt_log) p.dt_log[p.log_index] = dt;
+    }
+    const double *hs = static_cast<const double *>(p.hs);
+    const double *hus = static_cast<const double *>(p.hus);
+    const double *hvs = static_cast<const double *>(p.hvs);
+    const double *lh = static_cast<const double *>(p.ho);
+    const double *lhu = static_cast<const double *>(p.huo);
+    const double *lhv = static_cast<const double *>(p.hvo);
+    const long long n = (long long)p.Nx * p.Ny;
+    bool bad = false;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t / p.Ny), j = (int)(t - (t / p.Ny) * p.Ny);
+        const long long k = (long long)(i + NG) * p.pitch + (j + NG);
+        double oh = fadd<4>(hs[k], fmul<4>(dt, lh[k]));
+        double ohu = fadd<4>(hus[k], fmul<4>(dt, lhu[k]));
+        double ohv = fadd<4>(hvs[k], fmul<4>(dt, lhv[k]));
+        const bool clamped = x64::lt(oh, H_FLOOR);
+        if (clamped) {
+            oh = H_FLOOR;
+            ohu = 0.0;
+            ohv = 0.0;
+        }
+        if (p.mask) p.mask[k] = clamped ? 1 : 0;
+        bad |= ((x64::bits(oh) & x64::ABS) >= x64::INF_BITS) ||
+               ((x64::bits(ohu) & x64::ABS) >= x64::INF_BITS) ||
+               ((x64::bits(ohv) & x64::ABS) >= x64::INF_BITS);
+        o_h[k] = oh;
+        o_hu[k] = ohu;
+        o_hv[k] = ohv;
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(p.flags, FLAG_NONFINITE);
 }
 
 // Ensemble: CTAs stride over a flat list of (instance, tile) work items; every tile
@@ -538,16 +592,17 @@ __global__ void __launch_bounds__((TI + 1) * TJ, ens_min_blocks(TI, TJ)) k_ens_s
     }
 }
 
-// Max wave speed of a state into one slot (used once after an upload).
+// Max wave speed of interior rows [i0, i1) of a state into one slot (after an upload,
+// whole or by bands of rows).
 __global__ void __launch_bounds__(256) k_max_speed_f64(const double *h, const double *hu,
-                                                       const double *hv, int Nx, int Ny,
+                                                       const double *hv, int i0, int i1, int Ny,
                                                        long long P, double g,
                                                        unsigned long long *slot) {
     double v = 0.0;
-    const long long n = (long long)Nx * Ny;
+    const long long n = (long long)(i1 - i0) * Ny;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
          t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t / Ny), j = (int)(t - (t / Ny) * Ny);
+        const int i = i0 + (int)(t / Ny), j = (int)(t - (t / Ny) * Ny);
         const long long k = (long long)(i + NG) * P + (j + NG);
         v = dmax(v, cell_speed(g, h[k], hu[k], hv[k]));
     }
@@ -586,6 +641,44 @@ __global__ void k_fill_ghosts_f64(double *h, double *hu, double *hv, int Nx, int
     hv[kd] = fy ? -hv[ks] : hv[ks];
 }
 
+// The same ghost rule over ghosted rows [r0, r1) only: whole rows where they are x-ghost
+// rows, the four y-ghost columns elsewhere.  Every source cell lies in rows below r1 or
+// in the band itself, so a band can be filled (and copied out) as soon as the stage that
+// writes its interior rows and those before them has run.
+__global__ void k_fill_ghost_band_f64(double *h, double *hu, double *hv, int Nx, int Ny,
+                                      long long P, int bc, int r0, int r1) {
+    const int NyT = Ny + 2 * NG;
+    const int lo = min(max(r0, 0), NG), hi = max(min(r1, Nx + 2 * NG), Nx + NG);
+    const int n_lo = max(min(r1, NG) - r0, 0);             // rows 0, 1 in the band
+    const int n_hi = max(hi - max(r0, Nx + NG), 0);        // rows Nx+2, Nx+3 in the band
+    const int a = max(r0, NG), b = min(r1, Nx + NG);
+    const int n_in = max(b - a, 0);                        // interior rows in the band
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int i, j;
+    if (t < n_lo * NyT) {
+        i = lo + t / NyT;
+        j = t - (t / NyT) * NyT;
+    } else if (t < (n_lo + n_hi) * NyT) {
+        const int u = t - n_lo * NyT;
+        i = max(r0, Nx + NG) + u / NyT;
+        j = u - (u / NyT) * NyT;
+    } else if (t < (n_lo + n_hi) * NyT + 4 * n_in) {
+        const int u = t - (n_lo + n_hi) * NyT;
+        i = a + (u >> 2);
+        const int c = u & 3;
+        j = c < 2 ? c : Ny + c;
+    } else {
+        return;
+    }
+    bool fx, fy;
+    const int si = map_coord(i - NG, Nx, bc, fx) + NG;
+    const int sj = map_coord(j - NG, Ny, bc, fy) + NG;
+    const long long kd = (long long)i * P + j, ks = (long long)si * P + sj;
+    h[kd] = h[ks];
+    hu[kd] = fx ? -hu[ks] : hu[ks];
+    hv[kd] = fy ? -hv[ks] : hv[ks];
+}
+
 }  // namespace
 
 // Once per kernel and device: the largest shared-memory carveout (four tiles of up to
@@ -607,14 +700,18 @@ static cudaError_t smem_opt_in(K kernel, size_t bytes, bool (&done)[64]) {
 }
 
 template <int TI, int TJ, int STAGE>
-static cudaError_t single_launch_f64(const StageParams &p, const StageMaps *maps,
-                                     cudaStream_t s) {
+static cudaError_t single_launch_f64(StageParams p, const StageMaps *maps, cudaStream_t s,
+                                     int tr0, int tr1) {
     constexpr int NT = (TI + 1) * TJ;
     constexpr size_t smem = sizeof(TileF64<TI, TJ>) + 128;  // + alignment slack
     static bool done[64];  // one per kernel instantiation
     const cudaError_t e = smem_opt_in(k_stage_f64<TI, TJ, STAGE>, smem, done);
     if (e != cudaSuccess) return e;
-    const dim3 grid((p.Ny + TJ - 1) / TJ, (p.Nx + TI - 1) / TI);
+    const int rows = (p.Nx + TI - 1) / TI;
+    if (tr1 < 0 || tr1 > rows) tr1 = rows;
+    if (tr0 < 0 || tr0 >= tr1) return tr0 == tr1 ? cudaSuccess : cudaErrorInvalidValue;
+    p.tile_row0 = tr0;
+    const dim3 grid((p.Ny + TJ - 1) / TJ, tr1 - tr0);
     static const StageMaps none{};  // unused when use_tma is 0
     const StageMaps &m = maps ? *maps : none;
     k_stage_f64<TI, TJ, STAGE><<<grid, NT, smem, s>>>(p, m.e, m.u, m.v, m.b, maps ? 1 : 0);
@@ -622,13 +719,27 @@ static cudaError_t single_launch_f64(const StageParams &p, const StageMaps *maps
 }
 
 cudaError_t launch_stage_f64(int stage, const StageParams &p, const StageMaps *maps,
-                             cudaStream_t s) {
+                             cudaStream_t s, int tile_row0, int tile_row1) {
     static_assert(TILE_I_F64 == 8 && TILE_J_F64 == 32, "tile of the TMA maps");
     switch (stage) {
-        case 1: return single_launch_f64<8, 32, 1>(p, maps, s);
-        case 2: return single_launch_f64<8, 32, 2>(p, maps, s);
-        default: return single_launch_f64<8, 32, 3>(p, maps, s);
+        case 0: return single_launch_f64<8, 32, 0>(p, maps, s, tile_row0, tile_row1);
+        case 1: return single_launch_f64<8, 32, 1>(p, maps, s, tile_row0, tile_row1);
+        case 2: return single_launch_f64<8, 32, 2>(p, maps, s, tile_row0, tile_row1);
+        default: return single_launch_f64<8, 32, 3>(p, maps, s, tile_row0, tile_row1);
     }
+}
+
+cudaError_t launch_combine1_f64(const StageParams &p, void *h, void *hu, void *hv, int num_sms,
+                                cudaStream_t s) {
+    const long long n = (long long)p.Nx * p.Ny;
+    long long blocks = (n + 255) / 256;
+    const long long cap = (long long)num_sms * 8;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    k_combine1_f64<<<(unsigned)blocks, 256, 0, s>>>(p, static_cast<double *>(h),
+                                                      static_cast<double *>(hu),
+                                                      static_cast<double *>(hv));
+    return cudaGetLastError();
 }
 
 template <int TI, int TJ, int STAGE>
@@ -691,18 +802,25 @@ cudaError_t launch_ens_stage_f64(int shape, int stage, const EnsParams &e, int g
     }
 }
 
-cudaError_t launch_max_speed_f64(const void *h, const void *hu, const void *hv, int Nx, int Ny,
-                                 long long pitch, double g, unsigned long long *slot,
-                                 int num_sms, cudaStream_t s) {
-    const long long n = (long long)Nx * Ny;
+cudaError_t launch_max_speed_rows_f64(const void *h, const void *hu, const void *hv, int i0,
+                                      int i1, int Ny, long long pitch, double g,
+                                      unsigned long long *slot, int num_sms, cudaStream_t s) {
+    if (i1 <= i0) return cudaSuccess;
+    const long long n = (long long)(i1 - i0) * Ny;
     long long blocks = (n + 255) / 256;
     const long long cap = (long long)num_sms * 8;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
     k_max_speed_f64<<<(unsigned)blocks, 256, 0, s>>>(
         static_cast<const double *>(h), static_cast<const double *>(hu),
-        static_cast<const double *>(hv), Nx, Ny, pitch, g, slot);
+        static_cast<const double *>(hv), i0, i1, Ny, pitch, g, slot);
     return cudaGetLastError();
+}
+
+cudaError_t launch_max_speed_f64(const void *h, const void *hu, const void *hv, int Nx, int Ny,
+                                 long long pitch, double g, unsigned long long *slot,
+                                 int num_sms, cudaStream_t s) {
+    return launch_max_speed_rows_f64(h, hu, hv, 0, Nx, Ny, pitch, g, slot, num_sms, s);
 }
 
 cudaError_t launch_fill_ghosts_f64(void *h, void *hu, void *hv, int Nx, int Ny, long long pitch,
@@ -712,6 +830,21 @@ cudaError_t launch_fill_ghosts_f64(void *h, void *hu, void *hv, int Nx, int Ny, 
                                                        static_cast<double *>(hu),
                                                        static_cast<double *>(hv), Nx, Ny, pitch,
                                                        bc, halo_lo, halo_hi);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_ghost_band_f64(void *h, void *hu, void *hv, int Nx, int Ny,
+                                       long long pitch, int bc, int r0, int r1,
+                                       cudaStream_t s) {
+    const int NyT = Ny + 2 * NG;
+    const int n_lo = std::max(std::min(r1, NG) - r0, 0);
+    const int n_hi = std::max(std::min(r1, Nx + 2 * NG) - std::max(r0, Nx + NG), 0);
+    const int n_in = std::max(std::min(r1, Nx + NG) - std::max(r0, NG), 0);
+    const long long n = (long long)(n_lo + n_hi) * NyT + 4ll * n_in;
+    if (n <= 0) return cudaSuccess;
+    k_fill_ghost_band_f64<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+        static_cast<double *>(h), static_cast<double *>(hu), static_cast<double *>(hv), Nx, Ny,
+        pitch, bc, r0, r1);
     return cudaGetLastError();
 }
 

@@ -10,8 +10,20 @@ namespace swe {
 
 // FP64 drop-in (swe_fp64.cu, compiled with --fmad=false).
 // maps (optional): TMA maps of the stage source (h, hu, hv, B) for interior tiles.
+// Tile rows [tile_row0, tile_row1) only (tile_row1 < 0: to the last).  Stage 0 stores
+// L(U^n) in p.ho/huo/hvo; launch_combine1_f64 then forms U^(1) into (h, hu, hv) with the
+// step's dt, bitwise as stage 1.
 cudaError_t launch_stage_f64(int stage, const StageParams &p, const StageMaps *maps,
-                             cudaStream_t s);
+                             cudaStream_t s, int tile_row0 = 0, int tile_row1 = -1);
+cudaError_t launch_combine1_f64(const StageParams &p, void *h, void *hu, void *hv, int num_sms,
+                                cudaStream_t s);
+// Max wave speed of interior rows [i0, i1) into slot (atomic max).
+cudaError_t launch_max_speed_rows_f64(const void *h, const void *hu, const void *hv, int i0,
+                                      int i1, int Ny, long long pitch, double g,
+                                      unsigned long long *slot, int num_sms, cudaStream_t s);
+// Ghosts of ghosted rows [r0, r1) by the wall rule (no slab sides).
+cudaError_t launch_fill_ghost_band_f64(void *h, void *hu, void *hv, int Nx, int Ny,
+                                       long long pitch, int bc, int r0, int r1, cudaStream_t s);
 constexpr int TILE_I_F64 = 8, TILE_J_F64 = 32;
 // Ensemble stage over the work list; shape is SHAPE_* (8x32, 8x16, 4x64 for FP64).
 cudaError_t launch_ens_stage_f64(int shape, int stage, const EnsParams &e, int grid,

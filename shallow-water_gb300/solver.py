@@ -121,6 +121,28 @@ class Solver:
         self._check(st, "swe_step")
         return self.time
 
+    def step_host(self, h, hu, hv, B=None, out=None, n_steps: int = 1,
+                  dt: float | None = None):
+        """upload + step + download in one call (swe_step_host): the FP64 fused scheme
+        overlaps the host transfers with the stage kernels.  ``out`` (three ghosted
+        arrays, which may be the inputs) receives the state; returns ``out``."""
+        h, hu, hv = (_ghosted(a, self.Nx, self.Ny, n) for a, n in ((h, "h"), (hu, "hu"), (hv, "hv")))
+        Bp = None if B is None else _dp(_ghosted(B, self.Nx, self.Ny, "B"))
+        shape = (self.Nx + 4, self.Ny + 4)
+        if out is None:
+            out = tuple(np.empty(shape, dtype=np.float64) for _ in range(3))
+        for a in out:
+            if a.shape != shape or a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError(f"out arrays must be C-contiguous float64 {shape}")
+        self._keep = (h, hu, hv, B)
+        t = ctypes.c_double(self.time)
+        st = self._lib.swe_step_host(self._ctx, _dp(h), _dp(hu), _dp(hv), Bp,
+                                     *(_dp(a) for a in out), int(n_steps), float(dt or 0.0),
+                                     ctypes.byref(t))
+        self._check(st, "swe_step_host")
+        self.time = t.value
+        return out
+
     def stage(self, stage: int, dt: float):
         """One RK stage with fixed dt (swe_stage); stage s writes buffer s % 3."""
         self._check(self._lib.swe_stage(self._ctx, int(stage), float(dt)), "swe_stage")
