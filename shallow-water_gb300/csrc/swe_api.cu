@@ -520,8 +520,11 @@ int swe_step(swe_ctx *c, int n_steps, double dt, double *t_inout) {
     return SWE_OK;
 }
 
-// swe_step_host: bands of about 64 tile rows (512 grid rows), at most kMaxBands.
-constexpr int kBandTileRows = 64, kMaxBands = 32;
+// swe_step_host: bands of about SWE_HOST_BAND_TILE_ROWS tile rows, at most kMaxBands.
+#ifndef SWE_HOST_BAND_TILE_ROWS
+#define SWE_HOST_BAND_TILE_ROWS 64
+#endif
+constexpr int kBandTileRows = SWE_HOST_BAND_TILE_ROWS, kMaxBands = 64;
 
 int swe_step_host(swe_ctx *c, const double *h, const double *hu, const double *hv,
                   const double *B, double *h_out, double *hu_out, double *hv_out, int n_steps,
