@@ -382,7 +382,7 @@ void swe_destroy(swe_ctx *c) {
     if (c->base) cudaFree(c->base);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
-    for (cudaEvent_t e : c->band_ev) cudaEventDestroy(e);
+    for (int i = 0; i < c->n_band_ev; ++i) cudaEventDestroy(c->band_ev[i]);
     if (c->xfer) cudaStreamDestroy(c->xfer);
     if (c->stream) cudaStreamDestroy(c->stream);
     cudaGetLastError();
@@ -546,12 +546,17 @@ int swe_step_host(swe_ctx *c, const double *h, const double *hu, const double *h
     }
     st = ensure_dt_log(c, n_steps);
     if (st) return st;
+    static_assert(2 * kMaxBands <= (int)(sizeof(c->band_ev) / sizeof(c->band_ev[0])), "events");
     if (!c->xfer) CK(cudaStreamCreateWithFlags(&c->xfer, cudaStreamNonBlocking));
-    while ((int)c->band_ev.size() < 2 * kMaxBands) {
-        cudaEvent_t e = nullptr;
-        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-        c->band_ev.push_back(e);
+    while (c->n_band_ev < 2 * kMaxBands) {
+        CK(cudaEventCreateWithFlags(&c->band_ev[c->n_band_ev], cudaEventDisableTiming));
+        ++c->n_band_ev;
     }
+    // On an early error return, no copy of this call stays in flight.
+    struct XferDrain {
+        cudaStream_t s;
+        ~XferDrain() { cudaStreamSynchronize(s); }
+    } drain{c->xfer};
     const int Nx = c->p.Nx, Ny = c->p.Ny, R = Nx + 2 * NG;
     const int tile_rows = (Nx + TILE_I_F64 - 1) / TILE_I_F64;
     const int nb = std::min(kMaxBands, std::max(1, (tile_rows + kBandTileRows - 1) / kBandTileRows));
@@ -563,7 +568,7 @@ int swe_step_host(swe_ctx *c, const double *h, const double *hu, const double *h
     auto done_to = [&](int b) { return b == nb ? R : std::min(R, T(b) * TILE_I_F64 + NG); };
     const size_t row = (size_t)(Ny + 4) * sizeof(double);
     const size_t dpitch = (size_t)c->pitch * sizeof(double);
-    cudaEvent_t *up = c->band_ev.data(), *fin = c->band_ev.data() + kMaxBands;
+    cudaEvent_t *up = c->band_ev, *fin = c->band_ev + kMaxBands;
 
     const double t0 = t_inout ? *t_inout : 0.0;
     CK(cudaMemcpyAsync(c->t_accum, &t0, sizeof(double), cudaMemcpyHostToDevice, c->stream));

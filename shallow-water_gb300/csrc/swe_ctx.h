@@ -5,7 +5,6 @@
 #include <cuda_runtime.h>
 
 #include <string>
-#include <vector>
 
 #include "../../include/swe_gb300.h"
 #include "swe_tma.cuh"
@@ -34,7 +33,8 @@ struct swe_ctx {
     // swe_step_host: a transfer stream and one event per band of rows (uploaded /
     // finished), created on first use.
     cudaStream_t xfer = nullptr;
-    std::vector<cudaEvent_t> band_ev;
+    cudaEvent_t band_ev[128]{};
+    int n_band_ev = 0;
     double last_ms = 0.0;
     double modular_dt = 0.0;   // the modular scheme's fixed dt of the last swe_step
     swe::StageMaps maps[3]{};  // FP32 form: TMA maps of U^n, U^(1), U^(2) (stage sources)

@@ -248,8 +248,14 @@ __device__ __forceinline__ int mirror(int i, int N, bool *flip) {
     return i;
 }
 
+// Resident CTAs per SM the register budget is sized for: four (56 registers, no spills)
+// run 1-8% faster than the unbounded 70 registers and three CTAs.
+#ifndef SWE_MOD_MIN_BLOCKS
+#define SWE_MOD_MIN_BLOCKS 4
+#endif
+
 template <int RECON, int RIEMANN, bool BATHY>
-__global__ void __launch_bounds__(NT) k_modular_stage(const ModParams p) {
+__global__ void __launch_bounds__(NT, SWE_MOD_MIN_BLOCKS) k_modular_stage(const ModParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Tile &t = *reinterpret_cast<Tile *>(smem_raw);
     const int tid = threadIdx.x;
