@@ -522,7 +522,7 @@ __global__ void __launch_bounds__((TI + 1) * TJ, min_blocks(TI, TJ))
 __global__ void __launch_bounds__(256) k_combine1_f64(const StageParams p, double *o_h,
                                                       double *o_hu, double *o_hv) {
     const double dt = stage_dt(p);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
         p.speed[p.slot_write] = 0ull;
         if (p.dt_log) p.dt_log[p.log_index] = dt;
     }
@@ -532,11 +532,9 @@ __global__ void __launch_bounds__(256) k_combine1_f64(const StageParams p, doubl
     const double *lh = static_cast<const double *>(p.ho);
     const double *lhu = static_cast<const double *>(p.huo);
     const double *lhv = static_cast<const double *>(p.hvo);
-    const long long n = (long long)p.Nx * p.Ny;
     bool bad = false;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(t / p.Ny), j = (int)(t - (t / p.Ny) * p.Ny);
+    for (int i = blockIdx.y; i < p.Nx; i += gridDim.y)
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < p.Ny; j += gridDim.x * blockDim.x) {
         const long long k = (long long)(i + NG) * p.pitch + (j + NG);
         double oh = fadd<4>(hs[k], fmul<4>(dt, lh[k]));
         double ohu = fadd<4>(hus[k], fmul<4>(dt, lhu[k]));
@@ -599,12 +597,10 @@ __global__ void __launch_bounds__(256) k_max_speed_f64(const double *h, const do
                                                        long long P, double g,
                                                        unsigned long long *slot) {
     double v = 0.0;
-    const long long n = (long long)(i1 - i0) * Ny;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
-         t += (long long)gridDim.x * blockDim.x) {
-        const int i = i0 + (int)(t / Ny), j = (int)(t - (t / Ny) * Ny);
-        const long long k = (long long)(i + NG) * P + (j + NG);
-        v = dmax(v, cell_speed(g, h[k], hu[k], hv[k]));
+    for (int i = i0 + (int)blockIdx.y; i < i1; i += gridDim.y) {
+        const long long r = (long long)(i + NG) * P + NG;
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < Ny; j += gridDim.x * blockDim.x)
+            v = dmax(v, cell_speed(g, h[r + j], hu[r + j], hv[r + j]));
     }
     block_max_to_slot(v, slot);
 }
@@ -729,14 +725,18 @@ cudaError_t launch_stage_f64(int stage, const StageParams &p, const StageMaps *m
     }
 }
 
+// A grid over (column blocks, rows) of at most 8 CTAs per SM: columns by threads, rows
+// by CTAs, no per-element division.
+static dim3 row_grid(int rows, int cols, int num_sms) {
+    const int cap = std::max(num_sms, 1) * 8;
+    const int gx = std::max(1, std::min((cols + 255) / 256, cap));
+    const int gy = std::max(1, std::min(rows, cap / gx));
+    return dim3(gx, gy);
+}
+
 cudaError_t launch_combine1_f64(const StageParams &p, void *h, void *hu, void *hv, int num_sms,
                                 cudaStream_t s) {
-    const long long n = (long long)p.Nx * p.Ny;
-    long long blocks = (n + 255) / 256;
-    const long long cap = (long long)num_sms * 8;
-    if (blocks > cap) blocks = cap;
-    if (blocks < 1) blocks = 1;
-    k_combine1_f64<<<(unsigned)blocks, 256, 0, s>>>(p, static_cast<double *>(h),
+    k_combine1_f64<<<row_grid(p.Nx, p.Ny, num_sms), 256, 0, s>>>(p, static_cast<double *>(h),
                                                       static_cast<double *>(hu),
                                                       static_cast<double *>(hv));
     return cudaGetLastError();
@@ -806,12 +806,7 @@ cudaError_t launch_max_speed_rows_f64(const void *h, const void *hu, const void 
                                       int i1, int Ny, long long pitch, double g,
                                       unsigned long long *slot, int num_sms, cudaStream_t s) {
     if (i1 <= i0) return cudaSuccess;
-    const long long n = (long long)(i1 - i0) * Ny;
-    long long blocks = (n + 255) / 256;
-    const long long cap = (long long)num_sms * 8;
-    if (blocks > cap) blocks = cap;
-    if (blocks < 1) blocks = 1;
-    k_max_speed_f64<<<(unsigned)blocks, 256, 0, s>>>(
+    k_max_speed_f64<<<row_grid(i1 - i0, Ny, num_sms), 256, 0, s>>>(
         static_cast<const double *>(h), static_cast<const double *>(hu),
         static_cast<const double *>(hv), i0, i1, Ny, pitch, g, slot);
     return cudaGetLastError();
