@@ -60,5 +60,7 @@ def test_create_rejects_bad_params(sw, field, value):
 def test_null_context_calls_are_safe(sw):
     L = sw.lib()
     assert L.swe_step(None, 1, 0.0, None) == sw._lib.SWE_ERR_BAD_ARG
+    assert L.swe_step_host(None, None, None, None, None, None, None, None, 1, 0.0,
+                           None) == sw._lib.SWE_ERR_BAD_ARG
     assert L.swe_status_string(3) == b"non-finite state detected"
     L.swe_destroy(None)
