@@ -668,6 +668,7 @@ def run_gb300(args, dist: Dist):
         torch.cuda.synchronize()
         return cells * E * dist.world / dist.max(time.perf_counter() - e0) / 1e9
 
+    e2e_clocks = ClockSampler(dev)
     e2e = {"value": e2e_rate(one_call), "unit": "GCUPS",
            "h2d_bytes_per_step": 4 * nt * 8, "d2h_bytes_per_step": 3 * nt * 8,
            "steps": E, "api": "swe_step_host (upload, one RK3 step, download; transfers "
@@ -676,6 +677,7 @@ def run_gb300(args, dist: Dist):
     # Both paths advance the same input by one step: their outputs must agree bitwise.
     one = [np.array(a) for a in outs]
     e2e["three_calls_value"] = e2e_rate(three_calls)
+    e2e["clocks"] = e2e_clocks.stop()
     e2e["bitwise_equal_to_three_calls"] = all(
         np.array_equal(x.view(np.uint64), y.view(np.uint64)) for x, y in zip(one, outs))
     del one
