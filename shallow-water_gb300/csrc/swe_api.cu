@@ -559,11 +559,21 @@ int swe_step_host(swe_ctx *c, const double *h, const double *hu, const double *h
     } drain{c->xfer};
     const int Nx = c->p.Nx, Ny = c->p.Ny, R = Nx + 2 * NG;
     const int tile_rows = (Nx + TILE_I_F64 - 1) / TILE_I_F64;
-    const int nb = std::min(kMaxBands, std::max(1, (tile_rows + kBandTileRows - 1) / kBandTileRows));
     // Band b: tile rows [T(b), T(b + 1)).  Its stage needs ghosted rows below
     // T(b + 1) * TI + 4 (the tile, its 2-row halo and the wall ghosts); its interior rows
-    // end at ghosted row T(b + 1) * TI + 2.
-    auto T = [&](int b) { return (int)((long long)tile_rows * b / nb); };
+    // end at ghosted row T(b + 1) * TI + 2.  On large grids the first and the last band
+    // are a quarter of the others: nothing overlaps the first band's upload or the last
+    // band's download.
+    const int edge = tile_rows >= 4 * kBandTileRows ? kBandTileRows / 4 : 0;
+    const int mid_rows = tile_rows - 2 * edge;
+    const int nmid = std::min(kMaxBands - 2, std::max(1, (mid_rows + kBandTileRows - 1) / kBandTileRows));
+    const int nb = nmid + (edge ? 2 : 0);
+    auto T = [&](int b) {
+        if (!edge) return (int)((long long)tile_rows * b / nb);
+        if (b == 0) return 0;
+        if (b == nb) return tile_rows;
+        return edge + (int)((long long)mid_rows * (b - 1) / nmid);
+    };
     auto upto = [&](int b) { return b == nb ? R : std::min(R, T(b) * TILE_I_F64 + 4); };
     auto done_to = [&](int b) { return b == nb ? R : std::min(R, T(b) * TILE_I_F64 + NG); };
     const size_t row = (size_t)(Ny + 4) * sizeof(double);
