@@ -41,12 +41,8 @@ using x64::dmin;
 constexpr int64_t EPS_BITS = 0x3E45798EE2308C3ALL;  // bits of 1.0e-8
 static_assert(sizeof(double) == 8, "double is binary64");
 
-// safe_velocity (HPC_kernels.hpp:37-39): (h > 1e-8) ? q / h : 0.0
-__device__ __forceinline__ double safe_velocity(double q, double h) {
-    return x64::gt_pos_const(h, EPS_BITS) ? sf::div_rn(q, h) : 0.0;
-}
-
-// safe_velocity of two momenta over the same depth (one shared reciprocal).
+// safe_velocity (HPC_kernels.hpp:37-39), (h > 1e-8) ? q / h : 0.0, of two momenta over
+// the same depth (one shared reciprocal).
 __device__ __forceinline__ void safe_velocity2(double q1, double q2, double h, double &u1,
                                                double &u2) {
     if (x64::gt_pos_const(h, EPS_BITS)) {
