@@ -674,6 +674,9 @@ def run_gb300(args, dist: Dist):
            "steps": E, "api": "swe_step_host (upload, one RK3 step, download; transfers "
                               "overlapped with the stage kernels by bands of rows), pinned "
                               "host buffers"}
+    # the last call's compute stream, first band's wait through the last stage band
+    e2e["compute_stream_ms"] = solver.last_step_ms()
+    e2e["wall_ms_per_step"] = cells / (e2e["value"] * 1e9) * 1e3
     # Both paths advance the same input by one step: their outputs must agree bitwise.
     one = [np.array(a) for a in outs]
     e2e["three_calls_value"] = e2e_rate(three_calls)
