@@ -676,7 +676,7 @@ def run_gb300(args, dist: Dist):
                               "host buffers"}
     # the last call's compute stream, first band's wait through the last stage band
     e2e["compute_stream_ms"] = solver.last_step_ms()
-    e2e["wall_ms_per_step"] = cells / (e2e["value"] * 1e9) * 1e3
+    e2e["wall_ms_per_step"] = cells * dist.world / (e2e["value"] * 1e9) * 1e3
     # Both paths advance the same input by one step: their outputs must agree bitwise.
     one = [np.array(a) for a in outs]
     e2e["three_calls_value"] = e2e_rate(three_calls)
