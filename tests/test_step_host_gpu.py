@@ -107,3 +107,28 @@ def test_errors(gpu_lib, sw, problems):
         out = s.step_host(h, hu, hv, B, n_steps=0)
         s.upload(h, hu, hv, B)
         assert same(out, s.download())
+
+
+def test_device_steps_continue_after_it(gpu_lib, sw, problems):
+    """After swe_step_host the device holds the new state and its wave speed: further
+    swe_step calls continue the run as if it had been one swe_step."""
+    Nx, Ny = 1040, 48
+    h, hu, hv, B = problems.random_state(Nx, Ny, seed=12, q_scale=0.1, b_scale=0.05)
+    want, t, dts = sequence(sw, Nx, Ny, h, hu, hv, B, 5, None)
+    with sw.Solver(Nx, Ny) as s:
+        s.step_host(h, hu, hv, B, n_steps=2)
+        s.step(3)
+        assert same(s.download(), want)
+        assert s.time == t
+        assert bitwise_equal(s.dt_log(3), dts[2:])
+
+
+def test_slab_context_runs_the_three_calls(gpu_lib, sw, problems):
+    """A slab context (ghost rows supplied by a neighbour) takes the sequential path."""
+    Nx, Ny = 64, 40
+    h, hu, hv, B = problems.random_state(Nx, Ny, seed=13, q_scale=0.1, b_scale=0.05)
+    want, t, _ = sequence(sw, Nx, Ny, h, hu, hv, B, 2, 1e-4, x_halo=(True, False))
+    with sw.Solver(Nx, Ny, x_halo=(True, False)) as s:
+        got = s.step_host(h, hu, hv, B, n_steps=2, dt=1e-4)
+        assert same(got, want)
+        assert s.time == t
