@@ -384,6 +384,7 @@ void swe_destroy(swe_ctx *c) {
     if (c->ev1) cudaEventDestroy(c->ev1);
     for (int i = 0; i < c->n_band_ev; ++i) cudaEventDestroy(c->band_ev[i]);
     if (c->xfer) cudaStreamDestroy(c->xfer);
+    if (c->aux) cudaStreamDestroy(c->aux);
     if (c->stream) cudaStreamDestroy(c->stream);
     cudaGetLastError();
     delete c;
@@ -546,17 +547,22 @@ int swe_step_host(swe_ctx *c, const double *h, const double *hu, const double *h
     }
     st = ensure_dt_log(c, n_steps);
     if (st) return st;
-    static_assert(2 * kMaxBands <= (int)(sizeof(c->band_ev) / sizeof(c->band_ev[0])), "events");
+    constexpr int kEvents = 2 * kMaxBands + 2;
+    static_assert(kEvents <= (int)(sizeof(c->band_ev) / sizeof(c->band_ev[0])), "events");
     if (!c->xfer) CK(cudaStreamCreateWithFlags(&c->xfer, cudaStreamNonBlocking));
-    while (c->n_band_ev < 2 * kMaxBands) {
+    if (!c->aux) CK(cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking));
+    while (c->n_band_ev < kEvents) {
         CK(cudaEventCreateWithFlags(&c->band_ev[c->n_band_ev], cudaEventDisableTiming));
         ++c->n_band_ev;
     }
-    // On an early error return, no copy of this call stays in flight.
-    struct XferDrain {
-        cudaStream_t s;
-        ~XferDrain() { cudaStreamSynchronize(s); }
-    } drain{c->xfer};
+    // On an early error return, no copy or kernel of this call stays in flight.
+    struct Drain {
+        cudaStream_t a, b;
+        ~Drain() {
+            cudaStreamSynchronize(a);
+            cudaStreamSynchronize(b);
+        }
+    } drain{c->xfer, c->aux};
     const int Nx = c->p.Nx, Ny = c->p.Ny, R = Nx + 2 * NG;
     const int tile_rows = (Nx + TILE_I_F64 - 1) / TILE_I_F64;
     // Band b: tile rows [T(b), T(b + 1)).  Its stage needs ghosted rows below
@@ -579,6 +585,11 @@ int swe_step_host(swe_ctx *c, const double *h, const double *hu, const double *h
     const size_t row = (size_t)(Ny + 4) * sizeof(double);
     const size_t dpitch = (size_t)c->pitch * sizeof(double);
     cudaEvent_t *up = c->band_ev, *fin = c->band_ev + kMaxBands;
+    cudaEvent_t join = c->band_ev[2 * kMaxBands], fork = c->band_ev[2 * kMaxBands + 1];
+    // Consecutive bands alternate between the two compute streams: bands are
+    // independent of each other, and one band's last wave of CTAs then overlaps the next
+    // band's first instead of leaving SMs idle.
+    auto band_stream = [&](int b) { return (b & 1) ? c->aux : c->stream; };
 
     const double t0 = t_inout ? *t_inout : 0.0;
     CK(cudaMemcpyAsync(c->t_accum, &t0, sizeof(double), cudaMemcpyHostToDevice, c->stream));
@@ -587,6 +598,7 @@ int swe_step_host(swe_ctx *c, const double *h, const double *hu, const double *h
     CK(cudaMemsetAsync(c->speed, 0, sizeof(unsigned long long), c->stream));  // slot 0
     CK(cudaEventRecord(c->ev0, c->stream));
     CK(cudaStreamWaitEvent(c->xfer, c->ev0, 0));  // nothing in flight reads U^n any more
+    CK(cudaStreamWaitEvent(c->aux, c->ev0, 0));   // the speed slot is reset
 
     // Upload by bands on the transfer stream; as each band lands, the compute stream
     // reduces its max wave speed and computes L(U^n) on the tile rows it completes.
@@ -608,14 +620,16 @@ int swe_step_host(swe_ctx *c, const double *h, const double *hu, const double *h
                                  cudaMemcpyHostToDevice, c->xfer));
         }
         CK(cudaEventRecord(up[b], c->xfer));
-        CK(cudaStreamWaitEvent(c->stream, up[b], 0));
+        cudaStream_t S = band_stream(b);
+        CK(cudaStreamWaitEvent(S, up[b], 0));
         const int i0 = std::max(r0, NG) - NG, i1 = std::min(r1, Nx + NG) - NG;
         CK(launch_max_speed_rows_f64(c->Un[0], c->Un[1], c->Un[2], i0, i1, Ny, c->pitch,
-                                     c->p.g, c->speed, c->num_sms, c->stream));
-        CK(launch_stage_f64(0, sp, c->maps_ok ? &c->maps[0] : nullptr, c->stream, T(b),
-                            T(b + 1)));
+                                     c->p.g, c->speed, c->num_sms, S));
+        CK(launch_stage_f64(0, sp, c->maps_ok ? &c->maps[0] : nullptr, S, T(b), T(b + 1)));
         c->launches += 2;
     }
+    CK(cudaEventRecord(join, c->aux));
+    CK(cudaStreamWaitEvent(c->stream, join, 0));  // every band's speed and L
     c->uploaded = true;
     CK(launch_combine1_f64(sp, c->U1[0], c->U1[1], c->U1[2], c->num_sms, c->stream));
     ++c->launches;
@@ -641,15 +655,19 @@ int swe_step_host(swe_ctx *c, const double *h, const double *hu, const double *h
             ++c->launches;
         } else {
             // Last stage by bands; each finished band's ghosts are filled and the band
-            // copied out while the next band computes.
+            // copied out while the next band computes.  A band's ghosts come from its own
+            // rows (band 0 and the last band hold the rows the x-ghosts mirror).
+            CK(cudaEventRecord(fork, c->stream));
+            CK(cudaStreamWaitEvent(c->aux, fork, 0));  // stage 2 is complete
             for (int b = 0; b < nb; ++b) {
-                CK(launch_stage_f64(3, sp, c->maps_ok ? &c->maps[2] : nullptr, c->stream, T(b),
+                cudaStream_t S = band_stream(b);
+                CK(launch_stage_f64(3, sp, c->maps_ok ? &c->maps[2] : nullptr, S, T(b),
                                     T(b + 1)));
                 const int r0 = b == 0 ? 0 : done_to(b), r1 = done_to(b + 1);
                 CK(launch_fill_ghost_band_f64(c->Un[0], c->Un[1], c->Un[2], Nx, Ny, c->pitch,
-                                              c->p.bc, r0, r1, c->stream));
+                                              c->p.bc, r0, r1, S));
                 c->launches += 2;
-                CK(cudaEventRecord(fin[b], c->stream));
+                CK(cudaEventRecord(fin[b], S));
                 CK(cudaStreamWaitEvent(c->xfer, fin[b], 0));
                 double *out[3] = {h_out, hu_out, hv_out};
                 for (int f = 0; f < 3; ++f) {
@@ -663,6 +681,8 @@ int swe_step_host(swe_ctx *c, const double *h, const double *hu, const double *h
         }
         ++c->steps_done;
     }
+    CK(cudaEventRecord(join, c->aux));
+    CK(cudaStreamWaitEvent(c->stream, join, 0));
     CK(cudaEventRecord(c->ev1, c->stream));
     int flags = 0;
     double t1 = 0.0;

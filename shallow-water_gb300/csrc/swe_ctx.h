@@ -30,10 +30,11 @@ struct swe_ctx {
     double dx = 0, dy = 0, inv_dx = 0, inv_dy = 0, cfl_min_dxdy = 0;
     long long launches = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // bracket the stage launches of swe_step
-    // swe_step_host: a transfer stream and one event per band of rows (uploaded /
-    // finished), created on first use.
-    cudaStream_t xfer = nullptr;
-    cudaEvent_t band_ev[128]{};
+    // swe_step_host: a transfer stream, a second compute stream for alternate bands, and
+    // one event per band of rows (uploaded / finished) plus two joins, created on first
+    // use.
+    cudaStream_t xfer = nullptr, aux = nullptr;
+    cudaEvent_t band_ev[130]{};
     int n_band_ev = 0;
     double last_ms = 0.0;
     double modular_dt = 0.0;   // the modular scheme's fixed dt of the last swe_step
