@@ -114,6 +114,8 @@ cudaError_t launch_modular(swe_ctx *c, int stage, double dt, void *const *src, v
     m.recon = c->p.reconstruction;
     m.riemann = c->p.riemann;
     m.bathy = c->p.bathymetry;
+    m.kx = pow2_exponent(1.0 / c->dx);
+    m.ky = pow2_exponent(1.0 / c->dy);
     m.flags = c->flags;
     return launch_stage_modular(stage, m, c->stream);
 }

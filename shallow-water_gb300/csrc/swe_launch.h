@@ -78,6 +78,7 @@ struct ModularStage {
     long long pitch;
     double g, dx, dy, dt;
     int recon, riemann, bathy;  // 0 / 1 PiecewiseConst / MUSCL; 0 / 1 / 2 HLL / Rusanov / ROE
+    int kx, ky;                 // log2 of 1 / dx and 1 / dy when powers of two, else 127
     int *flags;                 // FLAG_NONFINITE, FLAG_MODULAR_HLL
 };
 constexpr int FLAG_MODULAR_HLL = 4;  // HLL could not provide a dissipation speed

@@ -227,11 +227,25 @@ struct ModParams {
     long long P;
     double g, half_g;
     double nidx, idy;  // -1.0 / dx and 1.0 / dy (finite_volume_bathy.hpp:17-27)
+    int kx, ky;        // log2 of 1.0 / dx and 1.0 / dy when powers of two, else 127
     double dt, c2, c3; // dt, dt / 4.0, 2.0 * dt / 3.0 (ssp_rk3.hpp:12-37)
     int stage;
     int *flags;
 };
 
+
+// The RK combination's products: correctly rounded on the integer pipes when
+// SWE_MOD_SOFT_CU is set (the same results; it moves work off the FP64 pipe).
+#ifndef SWE_MOD_SOFT_CU
+#define SWE_MOD_SOFT_CU 0
+#endif
+__device__ __forceinline__ double cu(double a, double b) {
+#if SWE_MOD_SOFT_CU
+    return sf::mul_rn(a, b);
+#else
+    return a * b;
+#endif
+}
 
 // Reflecting walls by mirrored index (reflecting_walls.hpp:9-86): a ghost reads its
 // mirror cell, with the normal momentum negated.
@@ -326,22 +340,28 @@ __global__ void __launch_bounds__(NT, SWE_MOD_MIN_BLOCKS) k_modular_stage(const 
     bool bad = false;
     if (r < TI && i < p.Nx && j < p.Ny) {
         // FiniteVolumeBathy / FiniteVolume::apply_spatial_operator: F^-(i) - F^+(i-1)
+        // products by -1/dx and 1/dy: exact exponent shifts when they are powers of two
+        auto mx = [&](double a) {
+            return p.kx != 127 ? x64::neg(x64::scale2(a, p.kx, x64::neg(p.nidx))) : p.nidx * a;
+        };
+        auto my = [&](double a) { return p.ky != 127 ? x64::scale2(a, p.ky, p.idy) : p.idy * a; };
         double rhs[3];
-        rhs[0] = p.nidx * (t.fx[0][r + 1][c] - t.fx[0][r][c]) - p.idy * (t.fy[0][r][c + 1] - t.fy[0][r][c]);
-        rhs[1] = p.nidx * (t.fx[1][r + 1][c] - t.fx[2][r][c]) - p.idy * (t.fy[1][r][c + 1] - t.fy[1][r][c]);
-        rhs[2] = p.nidx * (t.fx[3][r + 1][c] - t.fx[3][r][c]) - p.idy * (t.fy[2][r][c + 1] - t.fy[3][r][c]);
+        rhs[0] = mx(t.fx[0][r + 1][c] - t.fx[0][r][c]) - my(t.fy[0][r][c + 1] - t.fy[0][r][c]);
+        rhs[1] = mx(t.fx[1][r + 1][c] - t.fx[2][r][c]) - my(t.fy[1][r][c + 1] - t.fy[1][r][c]);
+        rhs[2] = mx(t.fx[3][r + 1][c] - t.fx[3][r][c]) - my(t.fy[2][r][c + 1] - t.fy[3][r][c]);
         const long long k = (long long)(i + NG) * p.P + (j + NG);
         const double *src[3] = {p.hs, p.hus, p.hvs}, *un[3] = {p.hn, p.hun, p.hvn};
         double o[3];
 #pragma unroll
         for (int f = 0; f < 3; ++f) {
             const double s = src[f][k];
+            // 1.0 * s == s and 1.0 / 4.0 * s is an exponent shift, both exact
             if (p.stage == 1)
-                o[f] = 1.0 * s + p.dt * rhs[f];                           // compute_U1
+                o[f] = s + cu(p.dt, rhs[f]);                                       // compute_U1
             else if (p.stage == 2)
-                o[f] = 3.0 / 4.0 * un[f][k] + 1.0 / 4.0 * s + p.c2 * rhs[f];  // compute_U2
+                o[f] = cu(3.0 / 4.0, un[f][k]) + x64::scale2(s, -2, 0.25) + cu(p.c2, rhs[f]);  // compute_U2
             else
-                o[f] = 1.0 / 3.0 * un[f][k] + 2.0 / 3.0 * s + p.c3 * rhs[f];  // compute_U_next
+                o[f] = cu(1.0 / 3.0, un[f][k]) + cu(2.0 / 3.0, s) + cu(p.c3, rhs[f]);  // compute_U_next
         }
         if (BATHY) {  // enforce_positivity (serial_solver.hpp:453-478)
             if (x64::lt(o[0], H_FLOOR)) {
@@ -435,6 +455,8 @@ cudaError_t launch_stage_modular(int stage, const ModularStage &m, cudaStream_t 
     p.half_g = 0.5 * m.g;
     p.nidx = -1.0 / m.dx;
     p.idy = 1.0 / m.dy;
+    p.kx = m.kx;
+    p.ky = m.ky;
     p.dt = m.dt;
     p.c2 = m.dt / 4.0;
     p.c3 = 2.0 * m.dt / 3.0;
