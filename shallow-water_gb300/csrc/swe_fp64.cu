@@ -220,12 +220,16 @@ __device__ __forceinline__ Face face_flux(double g, double half_g, double eta_0,
     return f;
 }
 
-// Per-cell wave speed max(|u| + c, |v| + c) (compute_stable_dt body, :288-293).
+// Per-cell wave speed max(|u| + c, |v| + c) (compute_stable_dt body, :288-293), as
+// max(|hu|, |hv|) / h + c.  Correct rounding is monotonic, so for finite values
+// fl(max(a, b) / h) = max(fl(a / h), fl(b / h)) and fl(m + c) = max(fl(|u| + c),
+// fl(|v| + c)): the same bits with one division and one add instead of two each.  (A
+// non-finite state fails the step in the same kernel, whatever its speed.)
 __device__ __forceinline__ double cell_speed(double g, double h, double hu, double hv) {
-    double u, v;
-    safe_velocity2(hu, hv, h, u, v);
+    const double m = x64::gt_pos_const(h, EPS_BITS)
+                         ? sf::div_rn(dmax(x64::fabs_(hu), x64::fabs_(hv)), h) : 0.0;
     const double c = sf::sqrt_rn(g * x64::positive_part(h));  // std::max(0.0, h)
-    return dmax(x64::fabs_(u) + c, x64::fabs_(v) + c);
+    return m + c;
 }
 
 // Block max of per-thread non-negative speeds, then one atomicMax on the bit pattern
