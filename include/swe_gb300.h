@@ -133,7 +133,10 @@ int swe_download(swe_ctx *ctx, double *h, double *hu, double *hv);
  * reduced on the device inside the last stage of the previous step.  If t_inout is
  * not NULL, *t_inout += dt for every step, in step order (HPC_solver.hpp:170).
  * Returns SWE_ERR_NONFINITE if any stage produced a non-finite interior value (the
- * state is then undefined), checked once per call.
+ * state is then undefined), checked once per call.  Returns SWE_ERR_TIMEOUT if a tile's
+ * TMA copy did not land within its deadline (50 ms): every later tile of the call then
+ * returns without work, so the call ends within about two deadlines of the failure; the
+ * state is undefined and the context stays usable (upload a state again).
  * SWE_SCHEME_MODULAR: the step loop of SerialSolver::run (serial_solver.hpp:183-244 with
  * bathymetry, 247-306 without); dt must be > 0 (the Serial backend has no adaptive dt),
  * else SWE_ERR_UNSUPPORTED.  SWE_ERR_NONFINITE then also reports where the reference
@@ -433,6 +436,24 @@ const char *swe_sanity_log_last_error(const swe_sanity_log *l);
  * and the device's own IEEE operations on the current device, and writes how many
  * results differed (NaN results compare equal to any NaN).  Expected: 0. */
 int swe_selftest_soft_f64(long long n, unsigned long long seed, long long *mismatches);
+
+/* The failure path of the stage kernels' bounded TMA waits, run without a fault: `ctas`
+ * blocks each arm a transaction barrier for bytes that no copy delivers and wait on it
+ * through the stage kernels' own helpers, with a deadline of deadline_ms (0 < d <= 1000).
+ * As in a stage launch, every block first reads the flag word and returns at once when
+ * an earlier wait gave up.  Returns SWE_ERR_TIMEOUT when the waits gave up as designed
+ * (SWE_OK would mean a wait completed), with the number of blocks that waited and the
+ * launch's device time.  No copy is issued, so nothing is left in flight. */
+int swe_selftest_wait_timeout(int ctas, double deadline_ms, long long *waited_ctas,
+                              double *elapsed_ms);
+
+/* Test hooks (no counterpart in the reference): the next swe_step, swe_step_host or
+ * swe_stage call (swe_ens_step for an ensemble) starts with its error-flag word holding
+ * the timeout bit, as if a TMA wait of an earlier launch had given up.  Every stage tile
+ * then returns before staging anything and the call returns SWE_ERR_TIMEOUT; the state is
+ * undefined afterwards and the context stays usable. */
+int swe_test_preset_timeout(swe_ctx *ctx);
+int swe_ens_test_preset_timeout(swe_ens *ens);
 
 #ifdef __cplusplus
 }

@@ -45,7 +45,8 @@ EXPORTS = (
     "swe_snapshot_records", "swe_snapshot_stats", "swe_snapshot_close", "swe_snapshot_destroy",
     "swe_snapshot_last_error", "swe_sanity_log_open", "swe_sanity_log_write",
     "swe_sanity_log_close", "swe_sanity_log_destroy", "swe_sanity_log_last_error",
-    "swe_params_size", "swe_snapshot_params_size",
+    "swe_params_size", "swe_snapshot_params_size", "swe_selftest_wait_timeout",
+    "swe_test_preset_timeout", "swe_ens_test_preset_timeout",
 )
 TOTALS_NOALLOC_MAX_BLOCKS = 1024
 ADJ_TAPE_ALL = -1  # n_snapshots value of swe_adjoint_gauge's tape mode
@@ -186,6 +187,13 @@ def lib(path: str = LIB_PATH):
     L.swe_selftest_soft_f64.argtypes = [ctypes.c_longlong, ctypes.c_ulonglong,
                                         ctypes.POINTER(ctypes.c_longlong)]
     L.swe_selftest_soft_f64.restype = ctypes.c_int
+    L.swe_selftest_wait_timeout.argtypes = [ctypes.c_int, ctypes.c_double,
+                                            ctypes.POINTER(ctypes.c_longlong), dp]
+    L.swe_selftest_wait_timeout.restype = ctypes.c_int
+    L.swe_test_preset_timeout.argtypes = [vp]
+    L.swe_test_preset_timeout.restype = ctypes.c_int
+    L.swe_ens_test_preset_timeout.argtypes = [vp]
+    L.swe_ens_test_preset_timeout.restype = ctypes.c_int
     L.swe_ens_last_error.argtypes = [vp]
     L.swe_ens_last_error.restype = ctypes.c_char_p
     cp = ctypes.c_char_p

@@ -54,6 +54,18 @@ int set_device(swe_ctx *c) {
     return SWE_OK;
 }
 
+// Clears the error-flag word at the start of a stepping call.  After
+// swe_test_preset_timeout, the call's flag word starts with FLAG_TIMEOUT set instead (its
+// low byte; the word is little-endian), as if a wait of an earlier launch had given up.
+int clear_flags(swe_ctx *c) {
+    CK(cudaMemsetAsync(c->flags, 0, sizeof(int), c->stream));
+    if (c->preset_timeout) {
+        c->preset_timeout = false;
+        CK(cudaMemsetAsync(c->flags, FLAG_TIMEOUT, 1, c->stream));
+    }
+    return SWE_OK;
+}
+
 }  // namespace
 
 bool swe::encode_tile_map(CUtensorMap *m, const void *base, int rows, int cols,
@@ -481,7 +493,8 @@ int swe_step(swe_ctx *c, int n_steps, double dt, double *t_inout) {
     if (st) return st;
     const double t0 = t_inout ? *t_inout : 0.0;
     CK(cudaMemcpyAsync(c->t_accum, &t0, sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemsetAsync(c->flags, 0, sizeof(int), c->stream));
+    st = clear_flags(c);
+    if (st) return st;
 
     StageParams sp = stage_params(c, dt);
     CK(cudaEventRecord(c->ev0, c->stream));
@@ -595,7 +608,8 @@ int swe_step_host(swe_ctx *c, const double *h, const double *hu, const double *h
 
     const double t0 = t_inout ? *t_inout : 0.0;
     CK(cudaMemcpyAsync(c->t_accum, &t0, sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    CK(cudaMemsetAsync(c->flags, 0, sizeof(int), c->stream));
+    st = clear_flags(c);
+    if (st) return st;
     c->steps_done = 0;
     CK(cudaMemsetAsync(c->speed, 0, sizeof(unsigned long long), c->stream));  // slot 0
     CK(cudaEventRecord(c->ev0, c->stream));
@@ -721,7 +735,8 @@ int swe_stage(swe_ctx *c, int stage, double dt) {
     void *const *dst = stage == 1 ? c->U1 : (stage == 2 ? c->U2 : c->Un);
     sp.hs = src[0]; sp.hus = src[1]; sp.hvs = src[2];
     sp.ho = dst[0]; sp.huo = dst[1]; sp.hvo = dst[2];
-    CK(cudaMemsetAsync(c->flags, 0, sizeof(int), c->stream));
+    st = clear_flags(c);
+    if (st) return st;
     CK(launch_stage(c, stage, sp));
     ++c->launches;
     if (stage == 3) ++c->steps_done;  // the stage wrote the new state's max speed
@@ -843,6 +858,12 @@ int swe_sanity(swe_ctx *c, double *mass, double *h_min, long long *first_negativ
     *energy = r[1];
     *h_min = r[2];
     std::memcpy(first_negative, &r[3], sizeof(long long));
+    return SWE_OK;
+}
+
+int swe_test_preset_timeout(swe_ctx *c) {
+    if (!c) return SWE_ERR_BAD_ARG;
+    c->preset_timeout = true;
     return SWE_OK;
 }
 

@@ -40,6 +40,7 @@ struct swe_ctx {
     double modular_dt = 0.0;   // the modular scheme's fixed dt of the last swe_step
     swe::StageMaps maps[3]{};  // FP32 form: TMA maps of U^n, U^(1), U^(2) (stage sources)
     bool maps_ok = false;
+    bool preset_timeout = false;  // swe_test_preset_timeout: the next stepping call's flag
     std::string err;
 };
 

@@ -57,6 +57,7 @@ struct swe_ens {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     double last_ms = 0.0;
     long long launches = 0;
+    bool preset_timeout = false;   // swe_ens_test_preset_timeout: the next step's flag
     std::string err;
 };
 
@@ -507,6 +508,10 @@ int swe_ens_step(swe_ens *c, int n_steps, double dt) try {
     if (n_steps == 0) return SWE_OK;
     ECK(cudaSetDevice(c->base.device));
     ECK(cudaMemsetAsync(c->d_flags, 0, sizeof(int), c->stream));
+    if (c->preset_timeout) {  // the flag word's low byte (little-endian int)
+        c->preset_timeout = false;
+        ECK(cudaMemsetAsync(c->d_flags, FLAG_TIMEOUT, 1, c->stream));
+    }
     ECK(cudaEventRecord(c->ev0, c->stream));
     int st = run_steps(c, n_steps, dt > 0.0 ? dt : 0.0);
     if (st) return st;
@@ -517,6 +522,8 @@ int swe_ens_step(swe_ens *c, int n_steps, double dt) try {
     float ms = 0.f;
     ECK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
     c->last_ms = ms;
+    if (flags & FLAG_TIMEOUT)
+        return efail(c, SWE_ERR_TIMEOUT, "a tile's TMA copy did not complete (state undefined)");
     if (flags & FLAG_NONFINITE)
         return efail(c, SWE_ERR_NONFINITE, "non-finite state detected in GB300 ensemble");
     return SWE_OK;
@@ -552,6 +559,12 @@ int swe_ens_last_step_ms(const swe_ens *c, double *ms) try {
 
 long long swe_ens_kernel_launches(const swe_ens *c) { return c ? c->launches : 0; }
 
+int swe_ens_test_preset_timeout(swe_ens *c) {
+    if (!c) return SWE_ERR_BAD_ARG;
+    c->preset_timeout = true;
+    return SWE_OK;
+}
+
 int swe_ens_set_schedule(swe_ens *c, int shape, int grid) try {
     if (!c || grid < 0 || !shape_ok(c, shape))
         return efail(c, SWE_ERR_BAD_ARG, "swe_ens_set_schedule: unsupported shape %d", shape);
@@ -582,6 +595,7 @@ int swe_ens_tune(swe_ens *c, int steps, double *best_ms) try {
     for (int q = 0; q < c->n; ++q)
         if (!c->uploaded[q]) return efail(c, SWE_ERR_BAD_ARG, "swe_ens_tune: instance %d not uploaded", q);
     ECK(cudaSetDevice(c->base.device));
+    ECK(cudaMemsetAsync(c->d_flags, 0, sizeof(int), c->stream));
     // Snapshot U^n, speed slots, times and the step parity; every candidate starts there.
     const size_t fb = c->pool_elems * c->elem;
     if (!c->snap) ECK(cudaMalloc(&c->snap, 3 * fb + 4 * c->n * sizeof(double)));
@@ -638,7 +652,11 @@ int swe_ens_tune(swe_ens *c, int steps, double *best_ms) try {
     }
     int st = swe_ens_set_schedule(c, best_shape, best_grid);
     if (st) return st;
+    int flags = 0;
+    ECK(cudaMemcpyAsync(&flags, c->d_flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     ECK(cudaStreamSynchronize(c->stream));
+    if (flags & FLAG_TIMEOUT)  // the timings after the failed wait mean nothing
+        return efail(c, SWE_ERR_TIMEOUT, "swe_ens_tune: a tile's TMA copy did not complete");
     if (best_ms) *best_ms = best / steps;
     return SWE_OK;
 } catch (...) {  // host allocation failures do not cross the C ABI

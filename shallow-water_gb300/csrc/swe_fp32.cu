@@ -137,9 +137,12 @@ struct BlockDt {
     float f;
 };
 
-__device__ __forceinline__ BlockDt stage_dt_f32(const StageParams &p) {
+// The block's dt; `abort` is true (block-uniform) when FLAG_TIMEOUT is already set, read
+// under the same barrier.
+__device__ __forceinline__ BlockDt stage_dt_f32(const StageParams &p, bool &abort) {
     __shared__ double s_dt;
     __shared__ float s_dtf;
+    __shared__ int s_abort;
     if (threadIdx.x == 0) {
         double dt = p.dt_fixed;
         if (!(dt > 0.0)) {
@@ -148,16 +151,21 @@ __device__ __forceinline__ BlockDt stage_dt_f32(const StageParams &p) {
         }
         s_dt = dt;
         s_dtf = (float)dt;
+        s_abort = tma::timeout_set(p.flags);
     }
     __syncthreads();
+    abort = s_abort != 0;
     return BlockDt{s_dt, s_dtf};
 }
 
 // One tile of one RK stage (see stage_tile_f64); returns the thread's cell wave speed of
 // the new state in stage 3, else 0.  (TI + 1) * TJ threads; dt is the block's dt.
+// Interior tiles are staged by TMA through `pipe` when tm is given; `aborted` is set
+// (block-uniform) when that wait gave up, and the caller then returns from the kernel.
 template <int TI, int TJ, int STAGE>
 __device__ __forceinline__ float stage_tile_f32(const StageParams &p, int i0, int j0,
-                                                float dt, const tma::TileMaps *tm = nullptr) {
+                                                float dt, const tma::TileMaps *tm,
+                                                tma::Pipe &pipe, bool &aborted) {
     constexpr int NT = (TI + 1) * TJ, RI = TI + 4, RJ = TJ + 4;
     // 128-byte aligned so the TMA box of each field lands on an aligned address
     __shared__ __align__(128) float s_e[RI][RJ];
@@ -178,23 +186,18 @@ __device__ __forceinline__ float stage_tile_f32(const StageParams &p, int i0, in
     // wall use mirrored indices (their halo holds ghost cells).
     const bool interior = tm != nullptr && i0 >= NG && j0 >= NG && i0 + TI + NG <= p.Nx &&
                           j0 + TJ + NG <= p.Ny;
+    aborted = false;
     if (interior) {
-        __shared__ __align__(8) uint64_t s_bar;
-        if (tid == 0) tma::mbar_init(&s_bar, 1);
-        __syncthreads();
-        if (tid == 0) {
-            tma::fence_proxy_async();  // the previous tile's reads of these buffers
-            tma::mbar_arrive_expect_tx(&s_bar, 4u * RI * RJ * sizeof(float));
-            // halo origin (i0 - 2, j0 - 2) in interior coordinates = (i0, j0) in the
-            // ghosted array; j0 is a multiple of TJ, so x * 4 bytes is 16-byte aligned
-            tma::load_2d(&s_e[0][0], tm->e, j0, i0, &s_bar);
-            tma::load_2d(&s_u[0][0], tm->u, j0, i0, &s_bar);
-            tma::load_2d(&s_v[0][0], tm->v, j0, i0, &s_bar);
-            tma::load_2d(&s_b[0][0], tm->b, j0, i0, &s_bar);
-        }
-        const bool timed_out = !tma::mbar_wait(&s_bar, 0);
-        if (__syncthreads_or(timed_out)) {
-            if (tid == 0) atomicOr(p.flags, FLAG_TIMEOUT);
+        // halo origin (i0 - 2, j0 - 2) in interior coordinates = (i0, j0) in the ghosted
+        // array; j0 is a multiple of TJ, so x * 4 bytes is 16-byte aligned
+        uint64_t *bar = pipe.bar;
+        if (!tma::stage_in(pipe, p.flags, 4u * RI * RJ * sizeof(float), [&] {
+                tma::load_2d(&s_e[0][0], tm->e, j0, i0, bar);
+                tma::load_2d(&s_u[0][0], tm->u, j0, i0, bar);
+                tma::load_2d(&s_v[0][0], tm->v, j0, i0, bar);
+                tma::load_2d(&s_b[0][0], tm->b, j0, i0, bar);
+            })) {
+            aborted = true;
             return 0.f;
         }
     } else {
@@ -306,11 +309,17 @@ __global__ void __launch_bounds__((TI + 1) * TJ)
     k_stage_f32(const StageParams p, const __grid_constant__ CUtensorMap tm_e,
                 const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ CUtensorMap tm_v,
                 const __grid_constant__ CUtensorMap tm_b, const int use_tma) {
-    const BlockDt bd = stage_dt_f32(p);
+    __shared__ __align__(8) uint64_t s_bar;
+    if (use_tma && threadIdx.x == 0) tma::mbar_init(&s_bar, 1);  // visible after stage_dt
+    bool aborted;
+    const BlockDt bd = stage_dt_f32(p, aborted);
+    if (aborted) return;  // an earlier wait of this call gave up
     const float dt = bd.f;
     const tma::TileMaps maps{&tm_e, &tm_u, &tm_v, &tm_b};
+    tma::Pipe pipe{&s_bar, 0u};
     const float speed = stage_tile_f32<TI, TJ, STAGE>(p, blockIdx.y * TI, blockIdx.x * TJ, dt,
-                                                      use_tma ? &maps : nullptr);
+                                                      use_tma ? &maps : nullptr, pipe, aborted);
+    if (aborted) return;
     if (STAGE == 1 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
         p.speed[p.slot_write] = 0ull;
         if (p.dt_log) p.dt_log[p.log_index] = (double)dt;
@@ -342,8 +351,11 @@ __global__ void __launch_bounds__((TI + 1) * TJ, ens_min_blocks_f32(TI, TJ))
     // view, the instance's dt and its TMA maps are set up once per instance the range
     // touches, not once per tile, and the next tile's instance needs no global lookup.
     __shared__ StageParams s_p;
-    __shared__ int s_q, s_t, s_ntiles;
+    __shared__ int s_q, s_t, s_ntiles, s_abort;
     __shared__ float s_dtf;
+    __shared__ __align__(8) uint64_t s_bar;
+    if (e.maps && threadIdx.x == 0) tma::mbar_init(&s_bar, 1);  // visible after the first barrier
+    tma::Pipe pipe{&s_bar, 0u};
     const int total = e.total_tiles;
     int T0 = blockIdx.x, T1 = blockIdx.x + 1;
     if ((int)gridDim.x < total) {
@@ -375,8 +387,10 @@ __global__ void __launch_bounds__((TI + 1) * TJ, ens_min_blocks_f32(TI, TJ))
             }
             s_q = q;
             s_t = t;
+            s_abort = tma::timeout_set(e.flags);
         }
         __syncthreads();
+        if (s_abort) return;  // a wait of this call gave up: the whole launch ends
         const StageParams &p = s_p;
         const int q = s_q, t = s_t;
         const int tiles_j = e.inst[q].tiles_j;
@@ -388,8 +402,10 @@ __global__ void __launch_bounds__((TI + 1) * TJ, ens_min_blocks_f32(TI, TJ))
                 static_cast<const CUtensorMap *>(e.maps) + ((size_t)q * 3 + (STAGE - 1)) * 4;
             tm = tma::TileMaps{m, m + 1, m + 2, m + 3};
         }
-        const float speed =
-            stage_tile_f32<TI, TJ, STAGE>(p, ti * TI, tj * TJ, dt, e.maps ? &tm : nullptr);
+        bool aborted;
+        const float speed = stage_tile_f32<TI, TJ, STAGE>(p, ti * TI, tj * TJ, dt,
+                                                          e.maps ? &tm : nullptr, pipe, aborted);
+        if (aborted) return;
         if (STAGE == 1 && t == 0 && threadIdx.x == 0) {
             p.speed[p.slot_write] = 0ull;
             if (e.dt_last) e.dt_last[q] = (double)dt;  // the FP32 dt the update applied

@@ -249,19 +249,29 @@ __device__ __forceinline__ void block_max_to_slot(double v, unsigned long long *
 }
 
 // The step's dt (compute_stable_dt, HPC_kernels.hpp:296-297, on the max speed reduced by
-// the previous step), computed once per block and shared.
-__device__ __forceinline__ double stage_dt(const StageParams &p) {
+// the previous step), computed once per block and shared.  `abort` is true
+// (block-uniform) when FLAG_TIMEOUT is already set, read under the same barrier; STAGE 0
+// (no dt) only reads the flag.
+template <bool DT = true>
+__device__ __forceinline__ double stage_dt(const StageParams &p, bool &abort) {
     __shared__ double s_dt;
+    __shared__ int s_abort;
     if (threadIdx.x == 0) {
         double dt = p.dt_fixed;
-        if (!(dt > 0.0)) {
+        if (DT && !(dt > 0.0)) {
             const double ms = __longlong_as_double((long long)p.speed[p.slot_read]);
             dt = x64::le(ms, EPS) ? 1.0e100 : p.cfl_min_dxdy / ms;
         }
         s_dt = dt;
+        s_abort = tma::timeout_set(p.flags);
     }
     __syncthreads();
+    abort = s_abort != 0;
     return s_dt;
+}
+__device__ __forceinline__ double stage_dt(const StageParams &p) {
+    bool abort;
+    return stage_dt<true>(p, abort);
 }
 
 // One tile of one RK stage: stage the TI x TJ tile (origin i0, j0 in interior
@@ -294,9 +304,12 @@ __device__ __forceinline__ TileF64<TI, TJ> &tile_smem() {
 // coordinates) plus a 2-cell halo, compute its interfaces, and update its cells.
 // Returns the thread's cell wave speed of the new state (stage 3), else 0.
 // (TI + 1) * TJ threads; the caller provides dt (same for the whole block).
+// Interior tiles are staged by TMA through `pipe` when tm is given; `aborted` is set
+// (block-uniform) when that wait gave up, and the caller then returns from the kernel.
 template <int TI, int TJ, int STAGE, bool SOFT_CU>
 __device__ __forceinline__ double stage_tile_f64(const StageParams &p, int i0, int j0,
-                                                 double dt, const tma::TileMaps *tm) {
+                                                 double dt, const tma::TileMaps *tm,
+                                                 tma::Pipe &pipe, bool &aborted) {
     constexpr int NT = (TI + 1) * TJ, RI = TI + 4, RJ = TJ + 4;
     static_assert(TI * (TJ + 1) <= NT, "one thread per y-face");
     TileF64<TI, TJ> &S = tile_smem<TI, TJ>();
@@ -313,22 +326,18 @@ __device__ __forceinline__ double stage_tile_f64(const StageParams &p, int i0, i
     // interface read through mirrored indices, ghosts from the wall rule.
     const bool interior = tm != nullptr && i0 >= NG && j0 >= NG && i0 + TI + NG <= p.Nx &&
                           j0 + TJ + NG <= p.Ny;
+    aborted = false;
     if (interior) {
-        if (tid == 0) tma::mbar_init(&S.bar, 1);
-        __syncthreads();
-        if (tid == 0) {
-            tma::fence_proxy_async();
-            tma::mbar_arrive_expect_tx(&S.bar, 4u * RI * RJ * sizeof(double));
-            // halo origin (i0 - 2, j0 - 2) in interior coordinates = (i0, j0) in the
-            // ghosted array; j0 is a multiple of TJ, so x * 8 bytes is 16-byte aligned
-            tma::load_2d(&S.eta[0][0], tm->e, j0, i0, &S.bar);
-            tma::load_2d(&S.hu[0][0], tm->u, j0, i0, &S.bar);
-            tma::load_2d(&S.hv[0][0], tm->v, j0, i0, &S.bar);
-            tma::load_2d(&S.B[0][0], tm->b, j0, i0, &S.bar);
-        }
-        const bool timed_out = !tma::mbar_wait(&S.bar, 0);
-        if (__syncthreads_or(timed_out)) {
-            if (tid == 0) atomicOr(p.flags, FLAG_TIMEOUT);
+        // halo origin (i0 - 2, j0 - 2) in interior coordinates = (i0, j0) in the ghosted
+        // array; j0 is a multiple of TJ, so x * 8 bytes is 16-byte aligned
+        uint64_t *bar = pipe.bar;
+        if (!tma::stage_in(pipe, p.flags, 4u * RI * RJ * sizeof(double), [&] {
+                tma::load_2d(&S.eta[0][0], tm->e, j0, i0, bar);
+                tma::load_2d(&S.hu[0][0], tm->u, j0, i0, bar);
+                tma::load_2d(&S.hv[0][0], tm->v, j0, i0, bar);
+                tma::load_2d(&S.B[0][0], tm->b, j0, i0, bar);
+            })) {
+            aborted = true;
             return 0.0;
         }
         for (int t = tid; t < RI * RJ; t += NT) {
@@ -512,11 +521,17 @@ __global__ void __launch_bounds__((TI + 1) * TJ, min_blocks(TI, TJ))
                 const __grid_constant__ CUtensorMap tm_u,
                 const __grid_constant__ CUtensorMap tm_v,
                 const __grid_constant__ CUtensorMap tm_b, int use_tma) {
-    const double dt = STAGE == 0 ? 0.0 : stage_dt(p);
+    TileF64<TI, TJ> &S = tile_smem<TI, TJ>();
+    if (use_tma && threadIdx.x == 0) tma::mbar_init(&S.bar, 1);  // visible after stage_dt
+    bool aborted;
+    const double dt = stage_dt<STAGE != 0>(p, aborted);
+    if (aborted) return;  // an earlier wait of this call gave up
     const tma::TileMaps maps{&tm_h, &tm_u, &tm_v, &tm_b};
+    tma::Pipe pipe{&S.bar, 0u};
     const int tr = p.tile_row0 + (int)blockIdx.y;
     const double speed = stage_tile_f64<TI, TJ, STAGE, true>(p, tr * TI, blockIdx.x * TJ, dt,
-                                                       use_tma ? &maps : nullptr);
+                                                       use_tma ? &maps : nullptr, pipe, aborted);
+    if (aborted) return;
     const bool first = blockIdx.x == 0 && tr == 0 && threadIdx.x == 0;
     if (STAGE == 1 && first) {
         p.speed[p.slot_write] = 0ull;  // read by nobody until stage 3 of this step
@@ -577,6 +592,7 @@ __global__ void __launch_bounds__((TI + 1) * TJ, ens_min_blocks(TI, TJ)) k_ens_s
     // The instance's view lives in shared memory, read where used (see k_ens_stage_f32).
     __shared__ StageParams s_p;
     __shared__ int s_t;
+    tma::Pipe pipe{nullptr, 0u};  // no TMA: every tile uses the mirrored-index loader
     for (int T = blockIdx.x; T < e.total_tiles; T += gridDim.x) {
         if (threadIdx.x == 0) {
             const int q = e.tile_inst[T];
@@ -589,9 +605,11 @@ __global__ void __launch_bounds__((TI + 1) * TJ, ens_min_blocks(TI, TJ)) k_ens_s
         const int t = s_t;
         const int tiles_j = e.inst[q].tiles_j;
         const int ti = t / tiles_j, tj = t - (t / tiles_j) * tiles_j;
-        const double dt = stage_dt(p);
-        const double speed =
-            stage_tile_f64<TI, TJ, STAGE, SWE_ENS_F64_SOFT_CU != 0>(p, ti * TI, tj * TJ, dt, nullptr);
+        bool aborted;
+        const double dt = stage_dt<true>(p, aborted);
+        if (aborted) return;  // FLAG_TIMEOUT set: the call has failed, the launch ends
+        const double speed = stage_tile_f64<TI, TJ, STAGE, SWE_ENS_F64_SOFT_CU != 0>(
+            p, ti * TI, tj * TJ, dt, nullptr, pipe, aborted);
         if (STAGE == 1 && t == 0 && threadIdx.x == 0) {
             p.speed[p.slot_write] = 0ull;
             if (e.dt_last) e.dt_last[q] = dt;

@@ -1,12 +1,15 @@
-// Device self-test of the integer-pipe binary64 division, square root, multiplication
-// and addition (swe_soft_f64.cuh) against the GPU's own IEEE round-to-nearest
-// operations, on hashed
-// operands: raw bit patterns (every class), physical-scale values, near-equal pairs
-// and exact quotients with their neighbours.
+// Device self-tests.
+//  - The integer-pipe binary64 division, square root, multiplication and addition
+//    (swe_soft_f64.cuh) against the GPU's own IEEE round-to-nearest operations, on
+//    hashed operands: raw bit patterns (every class), physical-scale values, near-equal
+//    pairs and exact quotients with their neighbours.
+//  - The give-up path of the stage kernels' bounded TMA waits (swe_tma.cuh), on a
+//    barrier that is armed for bytes no copy delivers.
 #include <cuda_runtime.h>
 
 #include "../../include/swe_gb300.h"
 #include "swe_soft_f64.cuh"
+#include "swe_tma.cuh"
 
 namespace swe {
 namespace {
@@ -69,6 +72,26 @@ __global__ void k_selftest_soft(long long n, u64 seed, unsigned long long *bad) 
     if (local) atomicAdd(bad, local);
 }
 
+// Each block does what a stage tile does before its stencil: read the flag word under a
+// block barrier and return if a wait already gave up, else arm its barrier and wait
+// through tma::stage_in.  The barrier expects `bytes` that nothing delivers, so the wait
+// gives up after deadline_ns, sets FLAG_TIMEOUT, waits once more for (absent) copies and
+// returns; blocks that start after that return at the flag check.
+__global__ void k_selftest_wait_timeout(int *flags, unsigned long long deadline_ns,
+                                        unsigned long long *waited) {
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int s_abort;
+    if (threadIdx.x == 0) {
+        tma::mbar_init(&bar, 1);
+        s_abort = tma::timeout_set(flags);
+    }
+    __syncthreads();
+    if (s_abort) return;
+    if (threadIdx.x == 0) atomicAdd(waited, 1ull);
+    tma::Pipe pipe{&bar, 0u};
+    tma::stage_in(pipe, flags, 1024u, [] {}, deadline_ns);
+}
+
 }  // namespace
 }  // namespace swe
 
@@ -89,4 +112,41 @@ extern "C" int swe_selftest_soft_f64(long long n, unsigned long long seed, long 
     cudaFree(d_bad);
     *mismatches = (long long)h_bad;
     return st;
+}
+
+extern "C" int swe_selftest_wait_timeout(int ctas, double deadline_ms, long long *waited_ctas,
+                                         double *elapsed_ms) {
+    if (ctas < 1 || ctas > (1 << 20) || !(deadline_ms > 0.0) || deadline_ms > 1000.0 ||
+        !waited_ctas || !elapsed_ms)
+        return SWE_ERR_BAD_ARG;
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count == 0) return SWE_ERR_NO_DEVICE;
+    struct Words {
+        unsigned long long waited;
+        int flags;
+    } *d = nullptr, h{};
+    if (cudaMalloc(&d, sizeof *d) != cudaSuccess) return SWE_ERR_CUDA;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int st = SWE_OK;
+    if (cudaMemset(d, 0, sizeof *d) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+        cudaEventCreate(&e1) != cudaSuccess)
+        st = SWE_ERR_CUDA;
+    float ms = 0.f;
+    if (st == SWE_OK) {
+        const unsigned long long ns = (unsigned long long)(deadline_ms * 1.0e6);
+        cudaEventRecord(e0);
+        swe::k_selftest_wait_timeout<<<ctas, 64>>>(&d->flags, ns, &d->waited);
+        cudaEventRecord(e1);
+        if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
+            cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess ||
+            cudaMemcpy(&h, d, sizeof h, cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = SWE_ERR_CUDA;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(d);
+    if (st != SWE_OK) return st;
+    *waited_ctas = (long long)h.waited;
+    *elapsed_ms = ms;
+    return (h.flags & swe::FLAG_TIMEOUT) ? SWE_ERR_TIMEOUT : SWE_OK;
 }
