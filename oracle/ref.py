@@ -7,10 +7,24 @@ from __future__ import annotations
 
 import ctypes
 import os
+import subprocess
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def reference_dir() -> str:
+    """Where the reference's sources lie: SWE_REFERENCE_DIR, else the oracle recipe's
+    default (``make -C oracle print-ref``)."""
+    d = os.environ.get("SWE_REFERENCE_DIR")
+    if d:
+        return d
+    try:
+        return subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True,
+                              text=True, check=True).stdout.strip()
+    except (OSError, subprocess.CalledProcessError):
+        return ""
 LIBS = {
     "g980665": os.path.join(HERE, "_ref", "libswe_ref.so"),
     "g981": os.path.join(HERE, "_ref", "libswe_ref_g981.so"),

@@ -15,9 +15,10 @@ import subprocess
 import pytest
 
 from conftest import ROOT
+from oracle.ref import reference_dir
 
-REF = "/root/reference"
-pytestmark = pytest.mark.skipif(not os.path.isdir(REF) or not shutil.which("g++"),
+REF = reference_dir()
+pytestmark = pytest.mark.skipif(not REF or not os.path.isdir(REF) or not shutil.which("g++"),
                                 reason="reference sources or g++ not available")
 
 CONFIG = """[mesh]
