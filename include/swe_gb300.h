@@ -42,6 +42,10 @@ typedef enum swe_status {
                                 reference's netCDF::exceptions, netCDF_writer.cpp:20) */
 } swe_status;
 
+/* Both wall rules take a ghost row's values from rows next to the same wall, which
+ * swe_step_host's band schedule relies on when it fills and copies out the first and
+ * last bands while other bands still compute; a rule that wraps across the domain would
+ * have to take swe_step_host's three-call path (it does for any other value). */
 typedef enum swe_bc {
     SWE_BC_REFLECTING = 0,   /* apply_reflecting_bc, HPC_solver.hpp:320-371 */
     SWE_BC_TRANSMISSIVE = 1  /* zero-gradient ghost copies; no reference counterpart */
@@ -225,7 +229,8 @@ int swe_sanity(swe_ctx *ctx, double *mass, double *h_min, long long *first_negat
  * (sum h, sum hu, sum hv) * dxdy to out, three doubles in device memory.  It runs on
  * `stream` (a cudaStream_t; NULL is the default stream) with the device that holds the
  * arrays current, and returns without waiting.  The result equals swe_totals for the
- * same state and block count.
+ * same state and block count, bitwise; swe_totals uses four blocks per SM, which
+ * blocks = 0 also picks whenever that fits the capacity (up to 256 SMs).
  *
  * Scratch: the per-block partial sums go to one fixed device array of
  * SWE_TOTALS_NOALLOC_MAX_BLOCKS * 6 doubles (48 KiB) inside the library, which every GPU
@@ -235,7 +240,10 @@ int swe_sanity(swe_ctx *ctx, double *mass, double *h_min, long long *first_negat
  * the array needs no clearing between calls.  All calls on a device share the one array:
  * calls that overlap on the GPU (other streams, other host threads) race and must be
  * serialised by the caller.  The first call on each device looks up the array's
- * address (cudaGetSymbolAddress); make that first call before any stream capture. */
+ * address (cudaGetSymbolAddress) in the context current on that device, and looks it up
+ * again whenever a later call finds a different current context (a non-primary context,
+ * or the primary context after a cudaDeviceReset); make those calls before any stream
+ * capture. */
 int swe_totals_noalloc(const void *h, const void *hu, const void *hv, const void *B,
                        int precision, int Nx, int Ny, long long pitch, double dxdy, int blocks,
                        double *out, void *stream);
@@ -274,7 +282,10 @@ int swe_last_step_ms(const swe_ctx *ctx, double *ms);
  * receives the device time.  On an FP32-mixed context the forward is the FP32 stage
  * kernel and the adjoint runs in FP32 with eta = h + B as the state variable (half the
  * memory; (38 n_steps + 200) bytes per cell in tape mode); the outputs are the same
- * derivatives, widened to double.  Fused scheme only.  No reference counterpart. */
+ * derivatives, widened to double.  With all four gradient pointers NULL only J is
+ * computed, by one forward sweep through the same kernels (bitwise the J of a gradient
+ * call; n_snapshots is ignored): the objective that finite differences of J need.  Fused
+ * scheme only.  No reference counterpart. */
 #define SWE_ADJ_TAPE_ALL (-1)
 int swe_adjoint_gauge(swe_ctx *ctx, int n_steps, double dt, int n_gauges, const int *gauge_i,
                       const int *gauge_j, const double *h_obs, int n_snapshots, double *J,

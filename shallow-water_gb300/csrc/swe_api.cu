@@ -553,7 +553,12 @@ int swe_step_host(swe_ctx *c, const double *h, const double *hu, const double *h
     if (st) return st;
     // The overlapped schedule is the FP64 fused drop-in's on one grid; the other forms run
     // the same three calls back to back.
-    if (fp32(c) || modular(c) || c->p.x_halo_lo || c->p.x_halo_hi || n_steps == 0) {
+    // The band schedule fills and copies out a band's ghost rows while other bands
+    // still compute; that holds only for wall rules whose x-ghost rows mirror or copy
+    // rows of the first or last band (swe_bc).
+    const bool band_safe_bc = c->p.bc == SWE_BC_REFLECTING || c->p.bc == SWE_BC_TRANSMISSIVE;
+    if (fp32(c) || modular(c) || c->p.x_halo_lo || c->p.x_halo_hi || n_steps == 0 ||
+        !band_safe_bc) {
         st = swe_upload(c, h, hu, hv, B);
         if (st) return st;
         st = swe_step(c, n_steps, dt, t_inout);

@@ -10,6 +10,9 @@
 // block order.  The result is deterministic (fixed assignment and order); its error is
 // that of the CHUNK-term chunk sums, about CHUNK roundings of a chunk, plus one
 // rounding of the total.  Works on both forms (FP32 eta - B is exact in FP64).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <climits>
 #include <mutex>
@@ -289,19 +292,45 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mutex;
 double *g_noalloc_ptr[kMaxDevices] = {};
+CUcontext g_noalloc_ctx[kMaxDevices] = {};  // the context each address was looked up in
 
-// Address of this device's copy of the scratch array (set-up on first use per device).
+// The context current on the calling thread (the driver's cuCtxGetCurrent, reached
+// through the runtime's entry-point query so that nothing links libcuda directly).
+bool current_context(CUcontext *ctx) {
+    static PFN_cuCtxGetCurrent_v4000 get = nullptr;
+    if (!get) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 4000, cudaEnableDefault,
+                                             &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn) {
+            cudaGetLastError();
+            return false;
+        }
+        get = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(fn);
+    }
+    return get(ctx) == CUDA_SUCCESS;
+}
+
+// Address of the scratch array in the current context of `device`: looked up on the first
+// call per device, and again whenever the current context is not the one it was looked
+// up in (the array has one copy per context that loaded the library's module).
 int noalloc_scratch(int device, double **out) {
     if (device < 0 || device >= kMaxDevices) return SWE_ERR_BAD_ARG;
+    // NULL on a thread the runtime has not used yet; the look-up below makes the device's
+    // primary context current there.
+    CUcontext ctx = nullptr;
+    if (!current_context(&ctx)) return SWE_ERR_CUDA;
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[device]) {
+    if (!ctx || !g_noalloc_ptr[device] || g_noalloc_ctx[device] != ctx) {
         void *ptr = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&ptr, g_totals_noalloc_scratch);
-        if (e != cudaSuccess || !ptr) {
+        if (e != cudaSuccess || !ptr || !current_context(&ctx) || !ctx) {
             cudaGetLastError();
             return SWE_ERR_CUDA;
         }
         g_noalloc_ptr[device] = static_cast<double *>(ptr);
+        g_noalloc_ctx[device] = ctx;
     }
     *out = g_noalloc_ptr[device];
     return SWE_OK;

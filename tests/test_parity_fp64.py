@@ -69,6 +69,32 @@ def test_dry_cells_and_positivity(gpu_lib, sw, port, problems):
     assert_bitwise(ref, out, dts, t)
 
 
+@pytest.mark.parametrize("bc", [0, 1], ids=["reflecting", "transmissive"])
+def test_wave_speed_of_dry_and_near_dry_cells(gpu_lib, sw, port, problems, bc):
+    """The per-cell wave speed's branches, bitwise through the dt sequence: dry cells
+    (h <= 1e-8, including exactly 1e-8 and 0) carrying large momenta, whose velocity the
+    scheme takes as zero (a speed from |hu| / h there would be ~1e8 and set dt), beside
+    near-dry wet cells (h just above 1e-8) whose large velocity sets the max speed, and
+    ordinary wet cells."""
+    Nx, Ny = 72, 56
+    h, hu, hv, B = problems.random_state(Nx, Ny, seed=41 + bc, q_scale=0.2, b_scale=0.05)
+    rng = np.random.default_rng(43 + bc)
+    dry = rng.random(h.shape) < 0.08
+    h[dry] = rng.choice(np.array([0.0, 3e-9, 1e-8]), size=int(dry.sum()))
+    hu[dry] = rng.choice(np.array([-2.0, 1.0, 3.0]), size=int(dry.sum()))
+    hv[dry] = rng.choice(np.array([-1.5, 0.5, 2.5]), size=int(dry.sum()))
+    fast = ~dry & (rng.random(h.shape) < 0.01)
+    h[fast] = 2.5e-8
+    hu[fast] = rng.choice(np.array([-1e-6, 5e-7]), size=int(fast.sum()))  # |u| up to 40
+    hv[fast] = 3e-7
+    ref, out, dts, t, _ = run_both(sw, port, h, hu, hv, B, Nx, Ny, 12, cfl=0.3, bc=bc, chunks=3)
+    assert_bitwise(ref, out, dts, t)
+    # the first dt is set by a near-dry cell's speed (|u| = 40), neither by the wet cells
+    # (about 4.5) nor by a dry cell's momentum over its depth (up to 1e9)
+    dx = 1.0 / Nx
+    assert 0.3 * dx / 100.0 < dts[0] < 0.3 * dx / 20.0, dts[0]
+
+
 def test_dambreak_transmissive(gpu_lib, sw, port, problems):
     B, _ = problems.gaussian_sum_bathymetry(200, 136, n=16, seed=2, bc="transmissive")
     h, hu, hv = problems.dam_break(B)

@@ -2,8 +2,9 @@
 (their device memory belongs to their own allocator, or their loop must not stall on an
 allocation).  The caller owns the state and the output buffer - here torch tensors - and
 the library uses only its fixed internal scratch array.  Checked through the C ABI
-against the allocating swe_totals on the same state, twice in a row (the second call
-meets the first call's leftovers in the shared scratch)."""
+against the allocating swe_totals on the same state and block count, bitwise, twice in a
+row (the second call meets the first call's leftovers in the shared scratch); the
+device's free memory is the same before and after the calls."""
 from __future__ import annotations
 
 import numpy as np
@@ -48,15 +49,22 @@ def test_noalloc_totals_match_allocating_entry_point(gpu_lib, sw, problems, prec
     eh, ehu, ehv, eB = device_state(torch, h, hu, hv, B, pitch, dtype, f32)
     out = torch.full((3,), float("nan"), dtype=torch.float64, device="cuda")
     prec = sw._lib.SWE_PRECISION_FP32_MIXED if f32 else sw._lib.SWE_PRECISION_FP64
+    # swe_totals's block count: four per SM
+    blocks = 4 * torch.cuda.get_device_properties(0).multi_processor_count
+    assert blocks <= sw._lib.TOTALS_NOALLOC_MAX_BLOCKS
+    want_bits = np.array(want, dtype=np.float64).view(np.uint64)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
     for _ in range(2):
         st = L.swe_totals_noalloc(eh.data_ptr(), ehu.data_ptr(), ehv.data_ptr(), eB.data_ptr(),
-                                  prec, Nx, Ny, pitch, dxdy, 0, out.data_ptr(), None)
+                                  prec, Nx, Ny, pitch, dxdy, blocks, out.data_ptr(), None)
         assert st == sw._lib.SWE_OK
         torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free0  # nothing was allocated
         got = out.cpu().numpy()
-        for g, w in zip(got, want):
-            assert abs(g - w) <= 1e-15 * max(abs(w), 1.0)
+        assert np.array_equal(got.view(np.uint64), want_bits), (got, want)
         out.fill_(float("nan"))
+        torch.cuda.synchronize()
 
 
 def test_noalloc_rejects_more_blocks_than_its_scratch(gpu_lib, sw):
