@@ -48,6 +48,37 @@ def gauge_misfit_gradient(solver: Solver, steps: int, dt: float, gauges, h_obs,
             "grad_B": out[3], "ms": ms.value}
 
 
+def gauge_misfit(solver: Solver, steps: int, dt: float, gauges, h_obs):
+    """J alone, from the solver's current state (left unchanged): one forward sweep
+    through the same stage kernels and gauge sum as :func:`gauge_misfit_gradient`, so the
+    value is bitwise that call's J.  Returns (J, device ms)."""
+    g = np.asarray(gauges, dtype=np.int32).reshape(-1, 2)
+    gi = np.ascontiguousarray(g[:, 0])
+    gj = np.ascontiguousarray(g[:, 1])
+    obs = np.ascontiguousarray(h_obs, dtype=np.float64).reshape(steps, len(gi))
+    J, ms = ctypes.c_double(), ctypes.c_double()
+    ip = ctypes.POINTER(ctypes.c_int)
+    st = solver._lib.swe_adjoint_gauge(solver._ctx, int(steps), float(dt), len(gi),
+                                       gi.ctypes.data_as(ip), gj.ctypes.data_as(ip), _dp(obs),
+                                       0, ctypes.byref(J), None, None, None, None,
+                                       ctypes.byref(ms))
+    solver._check(st, "swe_adjoint_gauge")
+    return J.value, ms.value
+
+
+def gauge_series(solver: Solver, steps: int, dt: float, gauges) -> np.ndarray:
+    """h at the gauge cells after each of ``steps`` fixed-dt steps from the solver's
+    current state, which the run advances: the (steps, n_gauges) observations of a
+    forward run, as the misfit compares them."""
+    g = np.asarray(gauges, dtype=np.int64).reshape(-1, 2)
+    out = np.empty((steps, len(g)))
+    for k in range(steps):
+        solver.step(1, dt)
+        h = solver.download()[0]
+        out[k] = h[g[:, 0] + 2, g[:, 1] + 2]
+    return out
+
+
 def ghosted_state(eta0, B, bc="reflecting"):
     """Ghosted (h, hu, hv, B) from interior eta0 and B: B's ghosts follow the wall rule,
     h0 = max(0, eta0 - B), hu0 = hv0 = 0."""

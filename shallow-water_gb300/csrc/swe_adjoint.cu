@@ -444,6 +444,7 @@ __global__ void k_gauge(const T *h, const T *B, long long P, const int *gi, cons
         const double hk = eta_state<T>() ? (double)h[k] - (double)B[k] : (double)h[k];
         const double r = hk - obs[q];
         s += r * r;
+        if (!lam_h) continue;  // objective only
         lam_h[k] += (T)(2.0 * r);
         if (eta_state<T>()) gB[k] -= (T)(2.0 * r);
     }
@@ -770,6 +771,107 @@ void build_schedule(Adj<T> &A, int N, int S) {
     }
 }
 
+// Sum of the per-step gauge sums in reverse step order, the order in which the adjoint's
+// reverse sweep accumulates J.
+__global__ void k_sum_reverse(const double *Jk, int n, double *J) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s = 0.0;
+    for (int k = n - 1; k >= 0; --k) s += Jk[k];
+    *J = s;
+}
+
+// The objective alone (no gradient): one forward sweep from the context's state through
+// the context's stage buffers, each step's gauge sum kept, then summed in the adjoint's
+// order.  The same stage kernels, gauge sums and order as a gradient call, so J is
+// bitwise that call's J; central finite differences of it check the gradient.
+template <class T>
+int run_objective(swe_ctx *c, int n_steps, double dt, int n_gauges, const int *gauge_i,
+                  const int *gauge_j, const double *h_obs, double *J, double *ms) {
+    Adj<T> A;
+    A.c = c;
+    A.fe = c->field_elems;
+    A.ng = n_gauges;
+    A.dt = dt;
+    const size_t fb = (A.fe * sizeof(T) + 255) / 256 * 256;
+    const size_t nobs = (size_t)n_steps * n_gauges + 1;
+    const size_t bytes = 3 * fb + 2 * 256 * (((size_t)n_gauges + 1) * sizeof(int) / 256 + 1) +
+                         (nobs * sizeof(double) + 255) / 256 * 256 + 512 +
+                         ((size_t)n_steps * sizeof(double) + 255) / 256 * 256;
+    char *base = nullptr;
+    if (cudaMalloc(&base, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        c->err = "swe_adjoint_gauge: out of device memory";
+        return SWE_ERR_CUDA;
+    }
+    char *p = base;
+    auto take = [&](size_t n) {
+        char *q = p;
+        p += (n + 255) / 256 * 256;
+        return q;
+    };
+    for (int f = 0; f < 3; ++f) A.W[f] = (T *)take(A.fe * sizeof(T));
+    A.gi = (int *)take(sizeof(int) * (n_gauges + 1));
+    A.gj = (int *)take(sizeof(int) * (n_gauges + 1));
+    A.obs = (double *)take(sizeof(double) * nobs);
+    A.J = (double *)take(sizeof(double));
+    A.speed = (unsigned long long *)take(2 * sizeof(unsigned long long));
+    double *Jk = (double *)take((size_t)n_steps * sizeof(double));
+    cudaStream_t st = c->stream;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) e = cudaMemsetAsync(Jk, 0, (size_t)n_steps * sizeof(double), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(A.speed, 0, 2 * sizeof(unsigned long long), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->flags, 0, sizeof(int), st);
+    if (e == cudaSuccess && n_gauges > 0) {
+        e = cudaMemcpyAsync(A.gi, gauge_i, sizeof(int) * n_gauges, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(A.gj, gauge_j, sizeof(int) * n_gauges, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(A.obs, h_obs, sizeof(double) * (nobs - 1), cudaMemcpyHostToDevice, st);
+    }
+    T *Un[3] = {static_cast<T *>(c->Un[0]), static_cast<T *>(c->Un[1]), static_cast<T *>(c->Un[2])};
+    if (e == cudaSuccess) e = copy_state(A, A.W, Un);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+    for (int k = 0; k < n_steps && e == cudaSuccess; ++k) {
+        e = forward_step(A, A.W, A.W, false);
+        if (e == cudaSuccess) {
+            k_gauge<T><<<1, 32, 0, st>>>(A.W[0], static_cast<const T *>(c->B), c->pitch, A.gi,
+                                         A.gj, A.ng, A.obs + (size_t)k * A.ng, nullptr, nullptr,
+                                         Jk + k);
+            ++c->launches;
+            e = cudaGetLastError();
+        }
+    }
+    if (e == cudaSuccess) {
+        k_sum_reverse<<<1, 32, 0, st>>>(Jk, n_steps, A.J);
+        ++c->launches;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+    double Jh = 0.0;
+    int flags = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&Jh, A.J, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flags, c->flags, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    float t = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(base);
+    if (e != cudaSuccess) {
+        c->err = std::string("swe_adjoint_gauge: ") + cudaGetErrorString(e);
+        return SWE_ERR_CUDA;
+    }
+    *J = Jh;
+    if (ms) *ms = t;
+    if (flags & FLAG_NONFINITE) {
+        c->err = "non-finite state detected in GB300 adjoint";
+        return SWE_ERR_NONFINITE;
+    }
+    return SWE_OK;
+}
+
 // The whole adjoint on a context whose state is of type T.
 template <class T>
 int run_adjoint(swe_ctx *c, int n_steps, double dt, int n_gauges, const int *gauge_i,
@@ -917,8 +1019,8 @@ extern "C" int swe_adjoint_gauge(swe_ctx *c, int n_steps, double dt, int n_gauge
     if (!c) return SWE_ERR_BAD_ARG;
     if (!c->uploaded || n_steps < 1 || !(dt > 0.0) ||
         n_gauges < 0 || (n_gauges > 0 && (!gauge_i || !gauge_j || !h_obs)) ||
-        (n_snapshots < 0 && n_snapshots != SWE_ADJ_TAPE_ALL) ||
-        !J || !grad_h || !grad_hu || !grad_hv || !grad_B) {
+        (n_snapshots < 0 && n_snapshots != SWE_ADJ_TAPE_ALL) || !J ||
+        (!grad_h + !grad_hu + !grad_hv + !grad_B) % 4 != 0) {
         c->err = "swe_adjoint_gauge: bad argument (needs an uploaded context)";
         return SWE_ERR_BAD_ARG;
     }
@@ -936,7 +1038,11 @@ extern "C" int swe_adjoint_gauge(swe_ctx *c, int n_steps, double dt, int n_gauge
             return SWE_ERR_BAD_ARG;
         }
     if (cudaSetDevice(c->p.device) != cudaSuccess) return SWE_ERR_CUDA;
-    if (c->p.precision == SWE_PRECISION_FP32_MIXED)
+    const bool f32 = c->p.precision == SWE_PRECISION_FP32_MIXED;
+    if (!grad_h)  // every gradient pointer NULL: the objective alone
+        return f32 ? run_objective<float>(c, n_steps, dt, n_gauges, gauge_i, gauge_j, h_obs, J, ms)
+                   : run_objective<double>(c, n_steps, dt, n_gauges, gauge_i, gauge_j, h_obs, J, ms);
+    if (f32)
         return run_adjoint<float>(c, n_steps, dt, n_gauges, gauge_i, gauge_j, h_obs, n_snapshots,
                                   J, grad_h, grad_hu, grad_hv, grad_B, ms);
     return run_adjoint<double>(c, n_steps, dt, n_gauges, gauge_i, gauge_j, h_obs, n_snapshots, J,

@@ -178,3 +178,73 @@ def test_fp32_checkpoint_budget_does_not_change_the_gradient(gpu_lib, sw, proble
         assert r["J"] == base["J"]
         for k in ("grad_h", "grad_hu", "grad_hv", "grad_B"):
             assert np.array_equal(r[k], base[k]), (snaps, k)
+
+
+# ---- The finite-difference check at the adjoint workload's grid ---------------------------
+# 1024^2, 16 seeded Gaussians of bed, eta0 = 1 + 8 seeded bumps, 64 gauges, observations
+# from a forward run with a perturbed surface and bed; 20 steps of the CPU oracle (the
+# reference's algorithm) per evaluation, central differences with eps = 1e-6 along 16
+# random smooth directions in the initial depth and the bed.
+#
+# Far from the bumps the surface and the bed are flat to rounding: minmod there compares
+# slopes of ~1e-16 and max(b-, b+) beds of ~1e-30, so the evaluation point itself sits on
+# kinks that any perturbation above rounding crosses; a central difference then averages
+# the one-sided derivatives, while the adjoint takes the branch the forward took.  On this
+# problem the agreement is ~1e-5 (median) relative to |FD| and ~1e-5 relative to the
+# projection's absolute terms.  With 1e-3 noise in the surface and the bed, which moves
+# those ties away from rounding level, the same check agrees within 1e-6: in the median
+# relative to |FD|, and for every direction relative to the projection's absolute terms
+# (a direction whose projection nearly cancels has |FD| far below its terms; one of the
+# 16 here is 3e-5 relative to |FD| and 3e-8 relative to its terms).
+def adjoint_workload(problems, n, steps, noise, seed=2033):
+    rng = np.random.default_rng(seed)
+    B, _ = problems.gaussian_sum_bathymetry(n, n, n=16, rng=rng, bc="reflecting")
+    bumps, _ = problems.gaussian_sum_bathymetry(n, n, n=8, rng=rng, width=(0.02, 0.1),
+                                                amp=(-0.05, 0.05), bc="reflecting")
+    if noise:
+        B = B + noise * rng.standard_normal(B.shape)
+        problems.fill_scalar_ghosts(B, "reflecting")
+        bumps = bumps + noise * rng.standard_normal(B.shape)
+    h = np.maximum(0.0, 1.0 + bumps - B)
+    gauges = np.stack([rng.integers(0, n, 64), rng.integers(0, n, 64)], axis=1)
+    return h, B, bumps, gauges, rng
+
+
+@pytest.mark.parametrize("noise", [0.0, 1e-3], ids=["stated", "noise-1e-3"])
+def test_adjoint_against_oracle_fd_at_1024(gpu_lib, sw, port, problems, noise):
+    n, steps, eps = 1024, 20, 1e-6
+    h, B, bumps, gauges, rng = adjoint_workload(problems, n, steps, noise)
+    z = np.zeros_like(h)
+    with sw.Solver(n, n) as s:
+        s.upload(h, z, z, B)
+        dt = 0.5 * s.stable_dt()
+        s.upload(np.maximum(0.0, 1.0 + 1.05 * bumps - 1.02 * B), z, z, 1.02 * B)
+        obs = sw.adjoint.gauge_series(s, steps, dt, gauges)
+        s.upload(h, z, z, B)
+        r = sw.adjoint.gauge_misfit_gradient(s, steps, dt, gauges, obs, "tape")
+        J_gpu, _ = sw.adjoint.gauge_misfit(s, steps, dt, gauges, obs)
+    p = port.grid(n, n)
+    J0 = oracle_J(port, p, h, z, z, B, steps, dt, gauges, obs)
+    assert abs(J0 - r["J"]) <= 1e-12 * J0
+    assert J_gpu == r["J"]  # the objective-only call: bitwise the gradient call's J
+    rel, rel_abs = [], []
+    for _ in range(16):
+        dh = problems.gaussian_sum_bathymetry(n, n, n=4, rng=rng, width=(0.1, 0.3),
+                                              amp=(-1.0, 1.0))[0]
+        dB = problems.gaussian_sum_bathymetry(n, n, n=4, rng=rng, width=(0.1, 0.3),
+                                              amp=(-1.0, 1.0), bc="reflecting")[0]
+        dh = np.where(h > 0, dh, 0.0)
+        fd = (oracle_J(port, p, h + eps * dh, z, z, B + eps * dB, steps, dt, gauges, obs) -
+              oracle_J(port, p, h - eps * dh, z, z, B - eps * dB, steps, dt, gauges, obs)) / (2 * eps)
+        terms = (r["grad_h"] * dh, r["grad_B"] * dB)
+        ad = float(sum(t.sum() for t in terms))
+        rel.append(abs(fd - ad) / abs(fd))
+        rel_abs.append(abs(fd - ad) / float(sum(np.abs(t).sum() for t in terms)))
+    print(f"noise {noise}: |FD - adjoint| / |FD| median {np.median(rel):.3g} max {max(rel):.3g}; "
+          f"/ abs terms max {max(rel_abs):.3g}")
+    if noise:
+        assert np.median(rel) <= FD_REL, rel
+        assert max(rel_abs) <= FD_REL, rel_abs
+    else:
+        assert np.median(rel) <= 1e-4 and max(rel) <= 1e-3, rel
+        assert max(rel_abs) <= 5e-5, rel_abs
