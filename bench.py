@@ -75,8 +75,11 @@ def parse():
                     help="fixed SHAPE:GRID for every precision instead of the autotuner")
     ap.add_argument("--adj-n", type=int, default=1024)
     ap.add_argument("--adj-steps", type=int, default=200)
-    ap.add_argument("--acc-n", type=int, default=2048)
-    ap.add_argument("--acc-steps", type=int, default=500)
+    ap.add_argument("--adj-fd-dirs", type=int, default=16,
+                    help="random directions of the adjoint's finite-difference check (0: none)")
+    ap.add_argument("--acc-n", type=int, default=16384,
+                    help="grid of the FP32-mixed accuracy check (default: the timed size)")
+    ap.add_argument("--acc-steps", type=int, default=100)
     ap.add_argument("--snap-steps", type=int, default=30)
     ap.add_argument("--snap-every", type=int, default=10)
     ap.add_argument("--snap-dir", default="",
@@ -233,10 +236,11 @@ def cpu_threads() -> int:
         return os.cpu_count() or 1
 
 
-def time_cpu_port(h, hu, hv, B, n, steps, warmup):
-    """Times the CPU restatement of the reference (all host threads) on in-place copies."""
+def time_cpu_port(h, hu, hv, B, n, steps, warmup, threads=0):
+    """Times the CPU restatement of the reference on in-place copies (threads 0: all host
+    threads, as omp_solver; 1: one core, as HPC_solver)."""
     from oracle import port
-    p = port.grid(n, n, 1.0, 1.0, cfl=0.45, bc=port.BC_TRANSMISSIVE, threads=0)
+    p = port.grid(n, n, 1.0, 1.0, cfl=0.45, bc=port.BC_TRANSMISSIVE, threads=threads)
     a = [np.array(x, copy=True) for x in (h, hu, hv)]
     ws = port.Workspace(p)
     if warmup:
@@ -276,31 +280,42 @@ def form_fp32(args, sw, fp64_gcups):
            "hbm_frac_of_measured": 108 * n * n / (ms / 1e3) / 1e9 / peaks()[0],
            "bytes_per_cell_update": 108, "speedup_vs_fp64": gcups / fp64_gcups,
            "issue_roofline": issue_roofline(gcups, F32_WARP_INST_PER_CELL_UPDATE)}
+    # Accuracy against an FP64 run of the same grid (the timed size by default), each form
+    # with its own adaptive dt; the mass drift of each over the run (the FP64 run's own
+    # drift is the flow through the transmissive walls) and their difference at the end.
     m, K = args.acc_n, args.acc_steps
     h, hu, hv, B = workload(m, args.seed)
     with sw.Solver(m, m, bc="transmissive") as s64, \
             sw.Solver(m, m, bc="transmissive", precision="fp32_mixed") as s32:
         s64.upload(h, hu, hv, B)
         s32.upload(h, hu, hv, B)
+        m64_0, m32_0 = s64.totals()[0], s32.totals()[0]
         s64.step(K)
         s32.step(K)
+        m64_1, m32_1 = s64.totals()[0], s32.totals()[0]
+        del h, hu, hv, B
         a, b = s64.download(), s32.download()
-        m0 = s64.totals()
         out["accuracy_vs_fp64"] = {
             "grid": [m, m], "steps": K, "dt": "adaptive, each form its own",
             "l1_h": rel_l1(b[0], a[0]), "linf_h": rel_linf(b[0], a[0]),
-            "l1_hu": rel_l1(b[1], a[1]), "l1_hv": rel_l1(b[2], a[2]),
-            "t_fp64": s64.time, "t_fp32": s32.time, "mass_fp64": m0[0]}
-    Bl, _ = importlib.import_module("shallow-water_gb300.problems").gaussian_sum_bathymetry(
-        m, m, n=16, seed=args.seed, bc="transmissive")
+            "l1_hu": rel_l1(b[1], a[1]), "linf_hu": rel_linf(b[1], a[1]),
+            "l1_hv": rel_l1(b[2], a[2]), "linf_hv": rel_linf(b[2], a[2]),
+            "t_fp64": s64.time, "t_fp32": s32.time,
+            "mass_drift_fp32": (m32_1 - m32_0) / m32_0,
+            "mass_drift_fp64": (m64_1 - m64_0) / m64_0,
+            "mass_fp32_vs_fp64": (m32_1 - m64_1) / m64_1,
+            "note": "norms relative to the FP64 field's L1 / Linf over the interior; the hv "
+                    "field is driven by the bathymetry alone and is ~1e3 smaller than hu"}
+        del a, b
     P = importlib.import_module("shallow-water_gb300.problems")
+    Bl, _ = P.gaussian_sum_bathymetry(m, m, n=16, seed=args.seed, bc="transmissive")
     hl, hul, hvl = P.lake_at_rest(Bl, 1.0)
     with sw.Solver(m, m, bc="transmissive", precision="fp32_mixed") as s:
         s.upload(hl, hul, hvl, Bl)
-        s.step(200, 0.5 * s.stable_dt())
+        s.step(K, 0.5 * s.stable_dt())
         l = s.download()
         wet = hl[2:-2, 2:-2] > 1e-3
-        out["lake_at_rest"] = {"grid": [m, m], "steps": 200,
+        out["lake_at_rest"] = {"grid": [m, m], "steps": K,
                                "max_abs_hu_hv_wet": float(max(np.abs(l[1][2:-2, 2:-2][wet]).max(),
                                                               np.abs(l[2][2:-2, 2:-2][wet]).max())),
                                "dry_cells": int((~wet).sum())}
@@ -360,11 +375,14 @@ def form_adjoint(args, sw):
     h = np.maximum(0.0, eta0 - B)
     z = np.zeros_like(h)
     gauges = np.stack([rng.integers(0, n, 64), rng.integers(0, n, 64)], axis=1)
-    obs = h[gauges[:, 0] + 2, gauges[:, 1] + 2][None, :] + 1e-3 * rng.standard_normal((K, 64))
     snaps = max(1, int(round(np.sqrt(K))))
     with sw.Solver(n, n) as s:
         s.upload(h, z, z, B)
         dt = 0.5 * s.stable_dt()
+        # observations: the gauges of a forward run from a perturbed surface and bed
+        s.upload(np.maximum(0.0, 1.0 + 1.05 * bumps - 1.02 * B), z, z, 1.02 * B)
+        obs = sw.adjoint.gauge_series(s, K, dt, gauges)
+        s.upload(h, z, z, B)
         s.step(K, dt)
         fwd_ms = s.last_step_ms()
         s.upload(h, z, z, B)
@@ -413,7 +431,56 @@ def form_adjoint(args, sw):
         "J_rel_diff_vs_fp64": abs(q["J"] - r["J"]) / abs(r["J"]),
         "directional_derivative_rel_diff_vs_fp64": dir_rel,
         "fp64_directional_change_under_1e-7_initial_perturbation": self_rel}
+    if args.adj_fd_dirs > 0:
+        out["fd_agreement"] = adjoint_fd(args, sw, P, n, K, dt, h, B, gauges, obs, r, q, rng)
+        # the same check with 1e-3 noise in the initial surface and the bed (a fresh
+        # adjoint), which removes the flat regions whose rounding-level slopes and bed
+        # differences put kinks of minmod and max(b-, b+) at the evaluation point itself
+        rn = np.random.default_rng(args.seed + 11)
+        Bn = B + 1e-3 * rn.standard_normal(B.shape)
+        P.fill_scalar_ghosts(Bn, "reflecting")
+        hn = np.maximum(0.0, eta0 + 1e-3 * rn.standard_normal(B.shape) - Bn)
+        with sw.Solver(n, n) as s:
+            s.upload(hn, z, z, Bn)
+            rr = sw.adjoint.gauge_misfit_gradient(s, K, dt, gauges, obs, "tape")
+        out["fd_agreement_noise_1e-3"] = adjoint_fd(args, sw, P, n, K, dt, hn, Bn, gauges, obs,
+                                                    rr, None, rng)
     return out
+
+
+def adjoint_fd(args, sw, P, n, K, dt, h, B, gauges, obs, r64, r32, rng, eps=1e-6):
+    """Central finite differences of J (the FP64 forward, bitwise the reference
+    solver's) along random smooth directions in the initial depth and the bed, against
+    the adjoints' directional derivatives: relative to |FD|, and to the sum of the
+    absolute terms of the projection (the scale of the cancellation in it)."""
+    z = np.zeros_like(h)
+    fds, a64, a32, scale = [], [], [], []
+    with sw.Solver(n, n) as s:
+        for _ in range(args.adj_fd_dirs):
+            dh = P.gaussian_sum_bathymetry(n, n, n=4, rng=rng, width=(0.1, 0.3), amp=(-1.0, 1.0))[0]
+            dB = P.gaussian_sum_bathymetry(n, n, n=4, rng=rng, width=(0.1, 0.3), amp=(-1.0, 1.0),
+                                           bc="reflecting")[0]
+            dh = np.where(h > 0, dh, 0.0)  # wet cells only: h0 = max(0, eta0 - B)
+            J = []
+            for sg in (1.0, -1.0):
+                s.upload(h + sg * eps * dh, z, z, B + sg * eps * dB)
+                J.append(sw.adjoint.gauge_misfit(s, K, dt, gauges, obs)[0])
+            fds.append((J[0] - J[1]) / (2 * eps))
+            a64.append(float((r64["grad_h"] * dh).sum() + (r64["grad_B"] * dB).sum()))
+            scale.append(float(np.abs(r64["grad_h"] * dh).sum() + np.abs(r64["grad_B"] * dB).sum()))
+            if r32 is not None:
+                a32.append(float((r32["grad_h"] * dh).sum() + (r32["grad_B"] * dB).sum()))
+    fds = np.array(fds)
+    rel = np.abs(np.array(a64) - fds) / np.abs(fds)
+    rel_s = np.abs(np.array(a64) - fds) / np.array(scale)
+    res = {"eps": eps, "directions": args.adj_fd_dirs, "grid": n, "steps": K,
+           "median": float(np.median(rel)), "max": float(rel.max()),
+           "median_vs_abs_terms": float(np.median(rel_s)), "max_vs_abs_terms": float(rel_s.max()),
+           "of": "FP64 adjoint against central FD of the FP64 forward's J"}
+    if a32:
+        rel32 = np.abs(np.array(a32) - fds) / np.abs(fds)
+        res.update({"fp32_median": float(np.median(rel32)), "fp32_max": float(rel32.max())})
+    return res
 
 
 def form_sanity(args, sw):
@@ -721,10 +788,66 @@ def run_gb300(args, dist: Dist):
             "kind": "port",
             "sample": f"{n}^2 workload from t=0, {s_cpu} full RK3 steps, C restatement of "
                       "HPC_solver/omp_solver (oracle/swe_oracle.c), OpenMP on all host threads"}
+        # The single-core figure, HPC_solver's configuration: one full-grid step.
+        secs1 = time_cpu_port(h, hu, hv, B, n, 1, 0, threads=1)
+        line["cpu_baseline_1core"] = {
+            "value": cells / secs1 / 1e9, "unit": "GCUPS", "cores": 1, "kind": "port",
+            "sample": f"{n}^2 workload from t=0, 1 full RK3 step, one thread"}
     if dist.rank == 0 and dist.world == 1 and not args.no_forms:
         line["forms"] = run_forms(args, sw, value)
+        # Last in the line, so that a reader keeping only the end of the output keeps it.
+        line["forms_summary"] = forms_summary(line)
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def forms_summary(line: dict) -> dict:
+    """The figures of the forms, flat and short, for the end of the line."""
+    f = line.get("forms", {})
+
+    def get(*path):
+        d = f
+        for k in path:
+            if not isinstance(d, dict) or k not in d:
+                return None
+            d = d[k]
+        return d
+
+    def r(x, nd=4):
+        return None if x is None else float(f"{x:.{nd}g}")
+
+    fd = get("adjoint", "fd_agreement") or {}
+    return {
+        "fp64_gcups": r(line.get("value")),
+        "fp64_pipe_frac": r(line.get("fp64_pipe_roofline", {}).get("frac")),
+        "fp64_hbm_frac": r(line.get("roofline", {}).get("frac")),
+        "fp32_gcups": r(get("fp32_mixed", "gcups")),
+        "fp32_hbm_frac": r(get("fp32_mixed", "hbm_frac_of_measured")),
+        "fp32_vs_fp64": r(get("fp32_mixed", "speedup_vs_fp64")),
+        "fp32_acc_grid_steps": [get("fp32_mixed", "accuracy_vs_fp64", "grid", 0),
+                                get("fp32_mixed", "accuracy_vs_fp64", "steps")],
+        "fp32_l1_h": r(get("fp32_mixed", "accuracy_vs_fp64", "l1_h"), 3),
+        "fp32_linf_h": r(get("fp32_mixed", "accuracy_vs_fp64", "linf_h"), 3),
+        "fp32_l1_hu": r(get("fp32_mixed", "accuracy_vs_fp64", "l1_hu"), 3),
+        "fp32_l1_hv": r(get("fp32_mixed", "accuracy_vs_fp64", "l1_hv"), 3),
+        "fp32_mass_drift": r(get("fp32_mixed", "accuracy_vs_fp64", "mass_drift_fp32"), 3),
+        "fp64_mass_drift": r(get("fp32_mixed", "accuracy_vs_fp64", "mass_drift_fp64"), 3),
+        "fp32_lake_max": r(get("fp32_mixed", "lake_at_rest", "max_abs_hu_hv_wet"), 3),
+        "ens_fp64_gcups": r(get("ensemble", "fp64", "gcups")),
+        "ens_fp32_gcups": r(get("ensemble", "fp32_mixed", "gcups")),
+        "ens_fp32_hbm_frac": r(get("ensemble", "fp32_mixed", "hbm_frac_of_measured")),
+        "adj_ratio_sqrt": r(get("adjoint", "ratio")),
+        "adj_ratio_tape": r(get("adjoint", "ratio_tape")),
+        "adj32_ratio_sqrt": r(get("adjoint", "fp32_mixed", "ratio")),
+        "adj_fd": {k: (r(v, 3) if isinstance(v, float) else v) for k, v in fd.items()
+                   if k in ("eps", "directions", "grid", "steps", "median", "max",
+                            "fp32_median", "fp32_max")},
+        "adj_fd_noise_1e-3": [r(get("adjoint", "fd_agreement_noise_1e-3", "median"), 3),
+                              r(get("adjoint", "fd_agreement_noise_1e-3", "max"), 3)],
+        "cpu_gcups": r(line.get("cpu_baseline", {}).get("value")),
+        "cpu_cores": line.get("cpu_baseline", {}).get("cores"),
+        "cpu_1core_gcups": r(line.get("cpu_baseline_1core", {}).get("value")),
+    }
 
 
 def main():
