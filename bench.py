@@ -38,13 +38,15 @@ BYTES_PER_CELL_FP64 = 216  # algorithmic bytes per cell-update: 56 + 80 + 80 (st
 # ncu capture of this bench at 8192^2 (dram__bytes_read.sum + dram__bytes_write.sum).
 NCU_TRAFFIC_BYTES_PER_CELL_LAUNCH = 71.7
 # FP64 lane operations (DADD + DMUL + DFMA) per cell update, three stages, from the
-# ncu thread-level instruction counts of the stage kernel (484.9), less the one add that
-# the one-division wave speed of stage 3 saves; the pipe executes 2 per clock per SM, so
-# its peak is 2 x SMs x clock.  The cell update's products (dt x L and the RK weights:
-# 3 + 6 + 9 per cell update on this grid, whose 1/dx is a power of two) run correctly
-# rounded on the integer pipes; they are counted as operations of the scheme.
-FP64_OPS_PER_CELL_UPDATE = 483.9
+# ncu thread-level instruction counts of the stage kernel as it runs (strips of 4 tiles:
+# 448.7 on the FP64 pipe), plus the cell update's products (dt x L and the RK weights:
+# 3 + 6 + 9 per cell update on this grid, whose 1/dx is a power of two), which run
+# correctly rounded on the integer pipes and are counted as operations of the scheme.
+# The pipe executes 2 per clock per SM, so its peak is 2 x SMs x clock.
+FP64_OPS_PER_CELL_UPDATE = 466.7
 FP64_OPS_ON_INTEGER_PIPES = 18
+# The same count for lone 8x32 tiles (2.16 interfaces per cell instead of 2.06).
+FP64_OPS_PER_CELL_UPDATE_LONE_TILES = 483.9
 # Warp instructions per cell update (the three stages) of the FP32 kernels, from their
 # ncu captures: the single-grid stage kernel (15.7 + 15.9 + 17.4) and the ensemble stage
 # kernel (17.6 + 16.9 + 18.6).  Both are bound by instruction issue, 4 warp instructions
@@ -210,6 +212,7 @@ def fp64_pipe(gcups: float, dev: int):
             "frac": achieved / peak, "ops_per_cell_update": FP64_OPS_PER_CELL_UPDATE,
             "of_which_on_integer_pipes": FP64_OPS_ON_INTEGER_PIPES,
             "fp64_pipe_busy_frac": gcups * (FP64_OPS_PER_CELL_UPDATE - FP64_OPS_ON_INTEGER_PIPES) / peak,
+            "frac_at_lone_tile_ops": gcups * FP64_OPS_PER_CELL_UPDATE_LONE_TILES / peak,
             "peak_source": f"2 x {sms} SMs x {mhz:.0f} MHz"}
 
 
@@ -504,11 +507,25 @@ def form_sanity(args, sw):
 
 
 def form_slabs(args, sw):
-    """The headline grid as two x-slabs on this one GPU (slabs.SlabGrid: per-stage
-    interface exchange through host memory, one global CFL dt per step) against one
-    context: the cost of the decomposition's exchange and stage-by-stage stepping."""
+    """The headline grid as x-slabs on this one GPU, against one context: the
+    single-process slab group (swe_slabs: device-side exchange overlapped with each
+    stage's inner tile rows, device-side CFL max) with 2 and 4 slabs, and the host-staged
+    SlabGrid (swe_stage + swe_halo through host memory) with 2."""
     n, K = args.n, 3
     h, hu, hv, B = workload(n, args.seed)
+    out = {"grid": [n, n], "steps": K}
+    for parts in (2, 4):
+        with sw.slabs.DeviceSlabGrid(n, n, bc="transmissive", parts=parts) as grid:
+            grid.upload(h, hu, hv, B)
+            grid.step(1)
+            l0 = grid.kernel_launches()
+            grid.step(K)
+            ms = grid.last_step_ms()
+            out[f"device_{parts}"] = {
+                "parts": parts, "ms_per_step": ms / K, "gcups": n * n * K / (ms / 1e3) / 1e9,
+                "launches_per_step": (grid.kernel_launches() - l0) / K,
+                "exchange": "2 rows x 3 fields per interface per stage, cudaMemcpyPeerAsync "
+                            "on the sending slab's stream, overlapped with inner tile rows"}
     grid = sw.slabs.SlabGrid(n, n, bc="transmissive", parts=2)
     try:
         grid.upload(h, hu, hv, B)
@@ -518,9 +535,11 @@ def form_slabs(args, sw):
         secs = time.perf_counter() - t0
     finally:
         grid.close()
-    return {"grid": [n, n], "parts": 2, "steps": K, "ms_per_step_wall": secs * 1e3 / K,
-            "gcups": n * n * K / secs / 1e9,
-            "exchange": "2 rows x 3 fields per interface per stage, through host memory"}
+    out["host_staged_2"] = {"parts": 2, "ms_per_step_wall": secs * 1e3 / K,
+                            "gcups": n * n * K / secs / 1e9,
+                            "exchange": "2 rows x 3 fields per interface per stage, through "
+                                        "host memory"}
+    return out
 
 
 def form_snapshots(args, sw):
@@ -808,9 +827,12 @@ def forms_summary(line: dict) -> dict:
     def get(*path):
         d = f
         for k in path:
-            if not isinstance(d, dict) or k not in d:
+            if isinstance(d, list) and isinstance(k, int) and k < len(d):
+                d = d[k]
+            elif isinstance(d, dict) and k in d:
+                d = d[k]
+            else:
                 return None
-            d = d[k]
         return d
 
     def r(x, nd=4):
@@ -841,9 +863,10 @@ def forms_summary(line: dict) -> dict:
         "adj32_ratio_sqrt": r(get("adjoint", "fp32_mixed", "ratio")),
         "adj_fd": {k: (r(v, 3) if isinstance(v, float) else v) for k, v in fd.items()
                    if k in ("eps", "directions", "grid", "steps", "median", "max",
-                            "fp32_median", "fp32_max")},
-        "adj_fd_noise_1e-3": [r(get("adjoint", "fd_agreement_noise_1e-3", "median"), 3),
-                              r(get("adjoint", "fd_agreement_noise_1e-3", "max"), 3)],
+                            "max_vs_abs_terms", "fp32_median", "fp32_max")},
+        "adj_fd_noise_1e-3": {k: r(get("adjoint", "fd_agreement_noise_1e-3", k), 3)
+                              for k in ("median", "max", "max_vs_abs_terms")},
+        "slabs_device_2_gcups": r(get("slabs", "device_2", "gcups")),
         "cpu_gcups": r(line.get("cpu_baseline", {}).get("value")),
         "cpu_cores": line.get("cpu_baseline", {}).get("cores"),
         "cpu_1core_gcups": r(line.get("cpu_baseline_1core", {}).get("value")),

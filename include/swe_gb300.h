@@ -292,6 +292,32 @@ int swe_adjoint_gauge(swe_ctx *ctx, int n_steps, double dt, int n_gauges, const 
                       double *grad_h, double *grad_hu, double *grad_hv, double *grad_B,
                       double *ms);
 
+/* ---- One grid over several GPUs of this process ---------------------------------------
+ * The grid's rows split into `parts` x-slabs as evenly as possible (build_subdomains,
+ * cuda_solver_4gpu.hpp:281-304), slab k on devices[k] (NULL: all on p->device; several
+ * slabs may share a device).  A step keeps everything on the devices: every stage runs
+ * first on each slab's inner tile rows, then on its two edge tile rows once the
+ * neighbours' interface rows have arrived; each slab sends the two rows next to each
+ * interface of the buffer it wrote to its neighbours with cudaMemcpyPeerAsync on its own
+ * stream (the reference synchronises every device and calls cudaMemcpyPeer,
+ * exchange_one_array, cuda_solver_4gpu.hpp:480-505); after stage 3 the slabs' max wave
+ * speeds are gathered by 8-byte peer copies and maxed on every device, so all slabs take
+ * the same dt.  Results are bitwise those of one context over the whole grid.  FP64
+ * fused scheme only (SWE_ERR_UNSUPPORTED otherwise).  Arrays are the whole grid's,
+ * ghosted, host layout. */
+typedef struct swe_slabs swe_slabs; /* opaque */
+int swe_slabs_create(const swe_params *p, int parts, const int *devices, swe_slabs **out);
+void swe_slabs_destroy(swe_slabs *g);
+int swe_slabs_upload(swe_slabs *g, const double *h, const double *hu, const double *hv,
+                     const double *B);
+int swe_slabs_download(swe_slabs *g, double *h, double *hu, double *hv);
+/* As swe_step: dt > 0 fixed, else the grid's adaptive CFL dt; t_inout advanced. */
+int swe_slabs_step(swe_slabs *g, int n_steps, double dt, double *t_inout);
+/* Device time of the last swe_slabs_step (events on slab 0's stream, joined by all). */
+int swe_slabs_last_step_ms(const swe_slabs *g, double *ms);
+long long swe_slabs_kernel_launches(const swe_slabs *g);
+const char *swe_slabs_last_error(const swe_slabs *g);
+
 /* ---- Batched ensembles ---------------------------------------------------------------
  * Many independent grids of uneven sizes advanced together: one launch per RK stage
  * covers every instance (a flat work list of (instance, tile) pairs), each instance

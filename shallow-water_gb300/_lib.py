@@ -47,6 +47,9 @@ EXPORTS = (
     "swe_sanity_log_close", "swe_sanity_log_destroy", "swe_sanity_log_last_error",
     "swe_params_size", "swe_snapshot_params_size", "swe_selftest_wait_timeout",
     "swe_test_preset_timeout", "swe_ens_test_preset_timeout",
+    "swe_slabs_create", "swe_slabs_destroy", "swe_slabs_upload", "swe_slabs_download",
+    "swe_slabs_step", "swe_slabs_last_step_ms", "swe_slabs_kernel_launches",
+    "swe_slabs_last_error",
 )
 TOTALS_NOALLOC_MAX_BLOCKS = 1024
 ADJ_TAPE_ALL = -1  # n_snapshots value of swe_adjoint_gauge's tape mode
@@ -196,6 +199,23 @@ def lib(path: str = LIB_PATH):
     L.swe_ens_test_preset_timeout.restype = ctypes.c_int
     L.swe_ens_last_error.argtypes = [vp]
     L.swe_ens_last_error.restype = ctypes.c_char_p
+    L.swe_slabs_create.argtypes = [ctypes.POINTER(SweParams), ctypes.c_int, ip,
+                                   ctypes.POINTER(vp)]
+    L.swe_slabs_create.restype = ctypes.c_int
+    L.swe_slabs_destroy.argtypes = [vp]
+    L.swe_slabs_destroy.restype = None
+    L.swe_slabs_upload.argtypes = [vp, dp, dp, dp, dp]
+    L.swe_slabs_upload.restype = ctypes.c_int
+    L.swe_slabs_download.argtypes = [vp, dp, dp, dp]
+    L.swe_slabs_download.restype = ctypes.c_int
+    L.swe_slabs_step.argtypes = [vp, ctypes.c_int, ctypes.c_double, dp]
+    L.swe_slabs_step.restype = ctypes.c_int
+    L.swe_slabs_last_step_ms.argtypes = [vp, dp]
+    L.swe_slabs_last_step_ms.restype = ctypes.c_int
+    L.swe_slabs_kernel_launches.argtypes = [vp]
+    L.swe_slabs_kernel_launches.restype = ctypes.c_longlong
+    L.swe_slabs_last_error.argtypes = [vp]
+    L.swe_slabs_last_error.restype = ctypes.c_char_p
     cp = ctypes.c_char_p
     L.swe_snapshot_open.argtypes = [cp, ctypes.POINTER(SnapshotParams), ctypes.POINTER(vp)]
     L.swe_snapshot_open.restype = ctypes.c_int

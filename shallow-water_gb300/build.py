@@ -31,6 +31,7 @@ UNITS = {
     "swe_output.cu": [],
     "swe_ncfile.cpp": [],
     "swe_api.cu": [],
+    "swe_slabs.cu": [],
 }
 
 

@@ -166,8 +166,10 @@ int step_modular(swe_ctx *c, int n_steps, double dt, double *t_inout) {
     return SWE_OK;
 }
 
+}  // namespace
+
 // Launch parameters shared by every stage of a context (buffers set per stage).
-StageParams stage_params(swe_ctx *c, double dt) {
+StageParams swe::ctx_stage_params(swe_ctx *c, double dt) {
     StageParams sp{};
     sp.B = c->B;
     sp.Nx = c->p.Nx;
@@ -194,6 +196,8 @@ StageParams stage_params(swe_ctx *c, double dt) {
     sp.halo_hi = c->p.x_halo_hi;
     return sp;
 }
+
+namespace {
 
 // Max wave speed of U^n into the slot the next step reads.
 int refresh_speed(swe_ctx *c) {
@@ -496,7 +500,7 @@ int swe_step(swe_ctx *c, int n_steps, double dt, double *t_inout) {
     st = clear_flags(c);
     if (st) return st;
 
-    StageParams sp = stage_params(c, dt);
+    StageParams sp = ctx_stage_params(c, dt);
     CK(cudaEventRecord(c->ev0, c->stream));
     for (int s = 0; s < n_steps; ++s) {
         sp.slot_read = (int)(c->steps_done & 1);
@@ -625,7 +629,7 @@ int swe_step_host(swe_ctx *c, const double *h, const double *hu, const double *h
     // reduces its max wave speed and computes L(U^n) on the tile rows it completes.
     const double *src[4] = {h, hu, hv, B};
     void *dst[4] = {c->Un[0], c->Un[1], c->Un[2], c->B};
-    StageParams sp = stage_params(c, dt);
+    StageParams sp = ctx_stage_params(c, dt);
     sp.slot_read = 0;
     sp.slot_write = 1;
     sp.log_index = 0;
@@ -730,7 +734,7 @@ int swe_stage(swe_ctx *c, int stage, double dt) {
     if (modular(c)) return fail(c, SWE_ERR_UNSUPPORTED, "swe_stage: fused scheme only");
     int st = set_device(c);
     if (st) return st;
-    StageParams sp = stage_params(c, dt);
+    StageParams sp = ctx_stage_params(c, dt);
     sp.slot_read = (int)(c->steps_done & 1);
     sp.slot_write = sp.slot_read ^ 1;
     sp.t_accum = nullptr;

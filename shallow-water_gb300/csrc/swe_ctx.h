@@ -47,4 +47,7 @@ struct swe_ctx {
 namespace swe {
 // k with x == 2^k when x is a normal power of two with |k| <= 64, else 127.
 int pow2_exponent(double x);
+// Launch parameters shared by every stage of a context (buffers, slots and log index are
+// set per stage by the caller); dt > 0 fixes the step, otherwise it is adaptive.
+StageParams ctx_stage_params(swe_ctx *c, double dt);
 }  // namespace swe

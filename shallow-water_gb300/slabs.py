@@ -12,14 +12,26 @@ those ghost rows as stored.  One step is
 
 which is bitwise the step of the whole grid: every interface flux sees the same stencil
 values, and the global max speed is an exact max.  The exchange is the only
-communication besides one max-reduction of the speed per step; with ``comm=None`` all
-slabs live in this process and rows are copied directly.
+communication besides one max-reduction of the speed per step.
+
+Two drivers:
+
+- :class:`DeviceSlabGrid` (one process, one or several GPUs; the reference's 4-GPU
+  model): the library's ``swe_slabs_*``, which keeps the exchange and the max-reduction
+  on the devices (peer copies overlapped with each stage's inner tile rows, events
+  between the slabs' streams, no host round trip per step).
+- :class:`SlabGrid`: one slab per process (``comm``, a torch.distributed group) or
+  every slab here (``comm=None``), stepped stage by stage through ``swe_stage`` with the
+  interface rows passed through host arrays.
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 
-from .solver import Solver
+from . import _lib as L
+from .solver import Solver, SweError, _BC, _dp, _ghosted
 
 
 def partition(Nx: int, parts: int):
@@ -169,3 +181,77 @@ class SlabGrid:
                 hi = r1 - r0 + (4 if k == self.parts - 1 else 2)
                 out[f][r0 + lo:r0 + hi] = arrs[f][lo:hi]
         return out
+
+
+class DeviceSlabGrid:
+    """A (Nx, Ny) grid as ``parts`` x-slabs of this process on ``devices`` (one per slab;
+    default all on ``device``), stepped by the library with device-side exchange."""
+
+    def __init__(self, Nx: int, Ny: int, Lx: float = 1.0, Ly: float = 1.0,
+                 g: float = 9.80665, cfl: float = 0.45, bc="reflecting", parts: int = 2,
+                 devices=None, device: int = 0):
+        self._lib = L.lib()
+        p = L.SweParams()
+        self._lib.swe_params_default(ctypes.byref(p))
+        p.Nx, p.Ny, p.Lx, p.Ly, p.g, p.cfl = Nx, Ny, Lx, Ly, g, cfl
+        p.bc = _BC[bc] if isinstance(bc, str) else int(bc)
+        p.device = device
+        self.Nx, self.Ny, self.parts = Nx, Ny, parts
+        devs = None
+        if devices is not None:
+            devs = (ctypes.c_int * parts)(*[int(d) for d in devices])
+        self._ctx = ctypes.c_void_p()
+        st = self._lib.swe_slabs_create(ctypes.byref(p), parts, devs, ctypes.byref(self._ctx))
+        if st != L.SWE_OK:
+            self._ctx = ctypes.c_void_p()
+            raise SweError(st, "swe_slabs_create: " + self._lib.swe_status_string(st).decode())
+        self.time = 0.0
+
+    def _check(self, st, what):
+        if st != L.SWE_OK:
+            msg = self._lib.swe_slabs_last_error(self._ctx).decode() if self._ctx else ""
+            raise SweError(st, f"{what}: {self._lib.swe_status_string(st).decode()}: {msg}")
+
+    def close(self):
+        if self._ctx:
+            self._lib.swe_slabs_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def upload(self, h, hu, hv, B):
+        arrs = [_ghosted(a, self.Nx, self.Ny, n) for a, n in ((h, "h"), (hu, "hu"), (hv, "hv"), (B, "B"))]
+        self._check(self._lib.swe_slabs_upload(self._ctx, *(_dp(a) for a in arrs)), "swe_slabs_upload")
+        self.time = 0.0
+
+    def download(self):
+        out = tuple(np.empty((self.Nx + 4, self.Ny + 4)) for _ in range(3))
+        self._check(self._lib.swe_slabs_download(self._ctx, *(_dp(a) for a in out)),
+                    "swe_slabs_download")
+        return out
+
+    def step(self, n_steps: int = 1, dt: float | None = None) -> float:
+        t = ctypes.c_double(self.time)
+        st = self._lib.swe_slabs_step(self._ctx, int(n_steps), float(dt or 0.0), ctypes.byref(t))
+        self.time = t.value
+        self._check(st, "swe_slabs_step")
+        return self.time
+
+    def last_step_ms(self) -> float:
+        v = ctypes.c_double()
+        self._check(self._lib.swe_slabs_last_step_ms(self._ctx, ctypes.byref(v)),
+                    "swe_slabs_last_step_ms")
+        return v.value
+
+    def kernel_launches(self) -> int:
+        return int(self._lib.swe_slabs_kernel_launches(self._ctx))

@@ -96,3 +96,52 @@ def test_slabs_gpu_bitwise(gpu_lib, sw, port, bc, parts):
     oracle, t_o = whole_grid(port, Nx, Ny, bc, steps)
     for a, b in zip(got, oracle):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bc", ["reflecting", "transmissive"])
+@pytest.mark.parametrize("parts", [2, 3, 4])
+def test_device_slabs_bitwise(gpu_lib, sw, port, bc, parts):
+    """The single-process slab group (device-side exchange overlapped with each stage's
+    inner tile rows, device-side max-speed gather) on one GPU: bitwise one context and
+    the oracle, adaptive dt over several calls; slabs of one and two tile rows included."""
+    Nx, Ny, steps = 70, 45, 15
+    h, hu, hv, B = so.case(Nx, Ny, bc, 5)
+    with sw.Solver(Nx, Ny, bc=bc) as s:
+        s.upload(h, hu, hv, B)
+        t_want = s.step(steps)
+        want = s.download()
+    with sw.slabs.DeviceSlabGrid(Nx, Ny, bc=bc, parts=parts) as grid:
+        grid.upload(h, hu, hv, B)
+        grid.step(4)
+        t = grid.step(steps - 4)
+        got = grid.download()
+    assert t == t_want
+    for a, b in zip(got, want):
+        assert np.array_equal(a, b)
+    oracle, t_o = whole_grid(port, Nx, Ny, bc, steps)
+    for a, b in zip(got, oracle):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.gpu
+def test_device_slabs_large_fixed_dt_and_thin_slabs(gpu_lib, sw, problems):
+    """A dam break over seeded bathymetry (TMA interior tiles, inner and edge launches of
+    several tile rows) and a grid whose slabs are 2-3 rows thick, with fixed dt."""
+    B, _ = problems.gaussian_sum_bathymetry(520, 300, n=16, seed=3, bc="transmissive")
+    h, hu, hv = problems.dam_break(B)
+    for Nx, parts in ((520, 3), (11, 4)):
+        Bs = np.ascontiguousarray(B[:Nx + 4])
+        hs, hus, hvs = (np.ascontiguousarray(a[:Nx + 4]) for a in (h, hu, hv))
+        with sw.Solver(Nx, 300, bc="transmissive") as s:
+            s.upload(hs, hus, hvs, Bs)
+            dt = 0.5 * s.stable_dt()
+            t_want = s.step(12, dt)
+            want = s.download()
+        with sw.slabs.DeviceSlabGrid(Nx, 300, bc="transmissive", parts=parts) as grid:
+            grid.upload(hs, hus, hvs, Bs)
+            t = grid.step(12, dt)
+            got = grid.download()
+        assert t == t_want
+        for a, b in zip(got, want):
+            assert np.array_equal(a, b), (Nx, parts)
