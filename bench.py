@@ -392,12 +392,23 @@ def form_adjoint(args, sw):
         r = sw.adjoint.gauge_misfit_gradient(s, K, dt, gauges, obs, snaps)
         r_all = sw.adjoint.gauge_misfit_gradient(s, K, dt, gauges, obs, K)
         r_tape = sw.adjoint.gauge_misfit_gradient(s, K, dt, gauges, obs, "tape")
+        r_seg = sw.adjoint.gauge_misfit_gradient(s, K, dt, gauges, obs, "segments")
+    seg_len = max(1, int(round(np.sqrt(K))))
+    cells = (n + 4) * (n + 4)
     out = {"grid": [n, n], "steps": K, "gauges": 64, "snapshots": snaps,
            "forward_ms": fwd_ms, "adjoint_ms": r["ms"], "ratio": r["ms"] / fwd_ms,
+           "snapshot_bytes": int(24 * (snaps + 1) * cells),
            "adjoint_ms_all_states_stored": r_all["ms"],
            "ratio_all_states_stored": r_all["ms"] / fwd_ms,
            "adjoint_ms_tape": r_tape["ms"], "ratio_tape": r_tape["ms"] / fwd_ms,
-           "tape_bytes": int((75 * K + 400) * (n + 4) * (n + 4))}
+           "tape_bytes": int((75 * K + 400) * cells),
+           "adjoint_ms_segments": r_seg["ms"], "ratio_segments": r_seg["ms"] / fwd_ms,
+           "segment_steps": seg_len,
+           "segments_bytes": int((24 * (-(-K // seg_len) + 1) + 75 * seg_len + 24) * cells),
+           "schedules_bitwise_equal": all(
+               x["J"] == r["J"] and all(np.array_equal(x[k], r[k]) for k in
+                                        ("grad_h", "grad_hu", "grad_hv", "grad_B"))
+               for x in (r_all, r_tape, r_seg))}
     # FP32-mixed: the same problem through the FP32 forward and the FP32 adjoint, and the
     # gradients' agreement with the FP64 adjoint (norm-wise, interior)
     with sw.Solver(n, n, precision="fp32_mixed") as s:
@@ -407,6 +418,7 @@ def form_adjoint(args, sw):
         s.upload(h, z, z, B)
         q = sw.adjoint.gauge_misfit_gradient(s, K, dt, gauges, obs, snaps)
         q_tape = sw.adjoint.gauge_misfit_gradient(s, K, dt, gauges, obs, "tape")
+        q_seg = sw.adjoint.gauge_misfit_gradient(s, K, dt, gauges, obs, "segments")
 
     # directional derivatives along smooth random directions (sums of Gaussian bumps):
     # the per-cell fields differ wherever a minmod or wave-speed branch flips between the
@@ -431,6 +443,7 @@ def form_adjoint(args, sw):
     out["fp32_mixed"] = {
         "forward_ms": fwd32, "adjoint_ms": q["ms"], "ratio": q["ms"] / fwd32,
         "adjoint_ms_tape": q_tape["ms"], "ratio_tape": q_tape["ms"] / fwd32,
+        "adjoint_ms_segments": q_seg["ms"], "ratio_segments": q_seg["ms"] / fwd32,
         "J_rel_diff_vs_fp64": abs(q["J"] - r["J"]) / abs(r["J"]),
         "directional_derivative_rel_diff_vs_fp64": dir_rel,
         "fp64_directional_change_under_1e-7_initial_perturbation": self_rel}
@@ -860,6 +873,7 @@ def forms_summary(line: dict) -> dict:
         "ens_fp32_hbm_frac": r(get("ensemble", "fp32_mixed", "hbm_frac_of_measured")),
         "adj_ratio_sqrt": r(get("adjoint", "ratio")),
         "adj_ratio_tape": r(get("adjoint", "ratio_tape")),
+        "adj_ratio_segments": r(get("adjoint", "ratio_segments")),
         "adj32_ratio_sqrt": r(get("adjoint", "fp32_mixed", "ratio")),
         "adj_fd": {k: (r(v, 3) if isinstance(v, float) else v) for k, v in fd.items()
                    if k in ("eps", "directions", "grid", "steps", "median", "max",

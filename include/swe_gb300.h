@@ -276,6 +276,12 @@ int swe_last_step_ms(const swe_ctx *ctx, double *ms);
  * schedule.  n_snapshots = SWE_ADJ_TAPE_ALL instead keeps every state and every step's
  * stage states and clamp masks from one forward sweep (device memory about
  * (75 n_steps + 400) bytes per cell), so the reverse sweep recomputes nothing.
+ * n_snapshots = SWE_ADJ_SEGMENTS stores the state every L = round(sqrt(n_steps)) steps in
+ * one forward sweep, then recomputes each segment of L steps once, last first, keeping
+ * its stage states, and reverses it: every step is advanced twice, in memory for
+ * ceil(n_steps / L) + 1 snapshots and a tape of L steps, about
+ * (24 n_steps / L + 75 L + 450) bytes per cell.  All schedules give the same J and
+ * gradients, bitwise.
  * Outputs, in the ghosted host layout with zero ghosts: J, dJ/dh^0,
  * dJ/dhu^0, dJ/dhv^0 and dJ/dB with the initial state held fixed, where the ghosts of B
  * are taken to follow the wall rule (mirror or copy of the interior).  ms (optional)
@@ -287,6 +293,7 @@ int swe_last_step_ms(const swe_ctx *ctx, double *ms);
  * call; n_snapshots is ignored): the objective that finite differences of J need.  Fused
  * scheme only.  No reference counterpart. */
 #define SWE_ADJ_TAPE_ALL (-1)
+#define SWE_ADJ_SEGMENTS (-2)
 int swe_adjoint_gauge(swe_ctx *ctx, int n_steps, double dt, int n_gauges, const int *gauge_i,
                       const int *gauge_j, const double *h_obs, int n_snapshots, double *J,
                       double *grad_h, double *grad_hu, double *grad_hv, double *grad_B,

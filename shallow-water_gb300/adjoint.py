@@ -24,7 +24,9 @@ def gauge_misfit_gradient(solver: Solver, steps: int, dt: float, gauges, h_obs,
     ``gauges`` is a sequence of (i, j) interior cells, ``h_obs`` a (steps, n_gauges)
     array.  ``snapshots`` stored states drive the binomial checkpoint schedule (default
     about sqrt(steps)); ``snapshots="tape"`` keeps every state and every step's stage
-    states instead (no recomputation, about 75 bytes per cell and step).  Returns a dict with J, grad_h, grad_hu, grad_hv, grad_B (ghosted
+    states instead (no recomputation, about 75 bytes per cell and step);
+    ``snapshots="segments"`` stores the state every sqrt(steps) steps and recomputes each
+    segment once with its stage states kept (every step advanced twice).  Returns a dict with J, grad_h, grad_hu, grad_hv, grad_B (ghosted
     arrays, zero ghosts; grad_B holds the initial state fixed) and ms (device time)."""
     g = np.asarray(gauges, dtype=np.int32).reshape(-1, 2)
     gi = np.ascontiguousarray(g[:, 0])
@@ -34,6 +36,8 @@ def gauge_misfit_gradient(solver: Solver, steps: int, dt: float, gauges, h_obs,
         snapshots = max(1, int(round(np.sqrt(steps))))
     elif snapshots == "tape":
         snapshots = L.ADJ_TAPE_ALL
+    elif snapshots == "segments":
+        snapshots = L.ADJ_SEGMENTS
     shape = (solver.Nx + 4, solver.Ny + 4)
     out = [np.zeros(shape) for _ in range(4)]
     J = ctypes.c_double()

@@ -31,6 +31,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <type_traits>
@@ -473,6 +474,8 @@ struct Adj {
     T *W[3], *Un1[3], *lam[3], *lamA[3], *lamB[3], *ln[3], *gB;
     T *cx, *cy;  // interface contributions of the stage being reversed
     bool tape = false;            // every state and every step's stage states kept
+    int seg_len = 0;              // segmented schedule: steps per segment (0: not used)
+    int nseg = 0;                 // segmented schedule: number of segments
     T *tU1 = nullptr, *tU2 = nullptr;  // tape: U^(1), U^(2) of step k at 3 k fields
     unsigned char *tmask = nullptr;    // tape: clamp masks of step k at 3 k fields
     unsigned char *mask[3];
@@ -681,35 +684,63 @@ cudaError_t store_slot(Adj<T> &A, int slot) {
 template <class T>
 T *tape_field(T *base, Adj<T> &A, int k, int f) { return base + ((size_t)k * 3 + f) * A.fe; }
 
-// Tape mode: one forward sweep keeps U^k in slot k and the stage states and clamp masks
-// of step k in the tape; the reverse sweep then recomputes nothing.
+// Steps [l, l + m) from U^l in snapshot slot `base`: one forward sweep keeps U^(l+j) in
+// slot base + j and the stage states and clamp masks of step l + j at tape position j;
+// the reverse sweep over them then recomputes nothing.  Tape mode is this over all steps
+// (l = 0, base = 0); the segmented schedule runs it once per segment.
 template <class T>
-cudaError_t taped(Adj<T> &A, int n) {
-    for (int k = 0; k < n; ++k) {
+cudaError_t tape_and_reverse(Adj<T> &A, int l, int m, int base) {
+    for (int j = 0; j < m; ++j) {
         T *W[3], *out[3], *U1[3], *U2[3];
         unsigned char *mk[3];
         for (int f = 0; f < 3; ++f) {
-            W[f] = slot_field(A, k, f);
-            out[f] = slot_field(A, k + 1, f);
-            U1[f] = tape_field(A.tU1, A, k, f);
-            U2[f] = tape_field(A.tU2, A, k, f);
-            mk[f] = A.tmask + ((size_t)k * 3 + f) * A.fe;
+            W[f] = slot_field(A, base + j, f);
+            out[f] = slot_field(A, base + j + 1, f);
+            U1[f] = tape_field(A.tU1, A, j, f);
+            U2[f] = tape_field(A.tU2, A, j, f);
+            mk[f] = A.tmask + ((size_t)j * 3 + f) * A.fe;
         }
         ACK(forward_step_into(A, W, out, U1, U2, mk));
     }
-    for (int k = n - 1; k >= 0; --k) {
+    for (int j = m - 1; j >= 0; --j) {
         T *Wk[3], *U1[3], *U2[3];
         const unsigned char *mk[3];
         for (int f = 0; f < 3; ++f) {
-            Wk[f] = slot_field(A, k, f);
-            U1[f] = tape_field(A.tU1, A, k, f);
-            U2[f] = tape_field(A.tU2, A, k, f);
-            mk[f] = A.tmask + ((size_t)k * 3 + f) * A.fe;
+            Wk[f] = slot_field(A, base + j, f);
+            U1[f] = tape_field(A.tU1, A, j, f);
+            U2[f] = tape_field(A.tU2, A, j, f);
+            mk[f] = A.tmask + ((size_t)j * 3 + f) * A.fe;
         }
-        ACK(gauge_source(A, slot_field(A, k + 1, 0), k));
+        ACK(gauge_source(A, slot_field(A, base + j + 1, 0), l + j));
         ACK(launch_adj(A, 3, U2, A.lam, mk[2], A.lamA));
         ACK(launch_adj(A, 2, U1, A.lamA, mk[1], A.lamB));
         ACK(launch_adj(A, 1, Wk, A.lamB, mk[0], A.lam));
+    }
+    return cudaSuccess;
+}
+
+template <class T>
+cudaError_t taped(Adj<T> &A, int n) { return tape_and_reverse(A, 0, n, 0); }
+
+// Segmented schedule: a first sweep stores U^(s L) in snapshot slot s for the segments
+// of L steps; each segment, last first, is then recomputed once from its snapshot with
+// its stage states taped (slots A.nseg + 1 + j), and reversed.  Every step is advanced
+// twice (the sweep and its segment's taped recomputation), with memory for
+// ceil(n / L) + 1 snapshots and a tape of L steps.
+template <class T>
+cudaError_t segmented(Adj<T> &A, int n) {
+    const int L = A.seg_len;
+    for (int k = 0; k + 1 < n; ++k) {  // the last step's end state is not needed
+        ACK(forward_step(A, A.W, A.W, false));
+        if ((k + 1) % L == 0) ACK(store_slot(A, (k + 1) / L));
+    }
+    const int base = A.nseg + 1;
+    for (int sg = A.nseg - 1; sg >= 0; --sg) {
+        const int l = sg * L, m = std::min(L, n - l);
+        T *src[3] = {slot_field(A, sg, 0), slot_field(A, sg, 1), slot_field(A, sg, 2)};
+        T *dst[3] = {slot_field(A, base, 0), slot_field(A, base, 1), slot_field(A, base, 2)};
+        ACK(copy_state(A, dst, src));
+        ACK(tape_and_reverse(A, l, m, base));
     }
     return cudaSuccess;
 }
@@ -881,7 +912,15 @@ int run_adjoint(swe_ctx *c, int n_steps, double dt, int n_gauges, const int *gau
     A.c = c;
     A.fe = c->field_elems;
     A.tape = n_snapshots == SWE_ADJ_TAPE_ALL;
-    A.S = A.tape ? n_steps : std::min(n_snapshots, n_steps);
+    if (n_snapshots == SWE_ADJ_SEGMENTS) {
+        A.seg_len = std::max(1, (int)std::lround(std::sqrt((double)n_steps)));
+        A.nseg = (n_steps + A.seg_len - 1) / A.seg_len;
+    }
+    // snapshot slots: the binomial schedule's; tape: every state; segmented: the segment
+    // starts plus the states of one taped segment
+    A.S = A.tape ? n_steps
+                 : (A.seg_len ? A.nseg + 1 + A.seg_len : std::min(n_snapshots, n_steps));
+    const int tape_steps = A.tape ? n_steps : A.seg_len;  // steps of stage states kept
     A.ng = n_gauges;
     A.dt = dt;
     const size_t fb = A.fe * sizeof(T);
@@ -892,9 +931,9 @@ int run_adjoint(swe_ctx *c, int n_steps, double dt, int n_gauges, const int *gau
     const size_t wide = eta_state<T>() ? rounded(A.fe * sizeof(double)) : 0;  // output staging
     const size_t bytes = rounded((size_t)(A.S + 1) * 3 * fb) + 19 * rounded(fb) + 3 * rounded(A.fe) +
                          rounded(cx_bytes) + rounded(cy_bytes) + wide +
-                         (A.tape ? 2 * rounded((size_t)n_steps * 3 * fb) +
-                                       rounded((size_t)n_steps * 3 * A.fe)
-                                 : 0) +
+                         (tape_steps ? 2 * rounded((size_t)tape_steps * 3 * fb) +
+                                           rounded((size_t)tape_steps * 3 * A.fe)
+                                     : 0) +
                          2 * rounded(sizeof(int) * (n_gauges + 1)) +
                          rounded(sizeof(double) * ((size_t)n_steps * n_gauges + 1)) +
                          rounded(sizeof(double)) + rounded(2 * sizeof(unsigned long long));
@@ -929,10 +968,10 @@ int run_adjoint(swe_ctx *c, int n_steps, double dt, int n_gauges, const int *gau
     A.cx = (T *)take(cx_bytes);
     A.cy = (T *)take(cy_bytes);
     double *widened = wide ? (double *)take(A.fe * sizeof(double)) : nullptr;
-    if (A.tape) {
-        A.tU1 = (T *)take((size_t)n_steps * 3 * fb);
-        A.tU2 = (T *)take((size_t)n_steps * 3 * fb);
-        A.tmask = (unsigned char *)take((size_t)n_steps * 3 * A.fe);
+    if (tape_steps) {
+        A.tU1 = (T *)take((size_t)tape_steps * 3 * fb);
+        A.tU2 = (T *)take((size_t)tape_steps * 3 * fb);
+        A.tmask = (unsigned char *)take((size_t)tape_steps * 3 * A.fe);
     }
     A.gi = (int *)take(sizeof(int) * (n_gauges + 1));
     A.gj = (int *)take(sizeof(int) * (n_gauges + 1));
@@ -958,9 +997,10 @@ int run_adjoint(swe_ctx *c, int n_steps, double dt, int n_gauges, const int *gau
     if (e == cudaSuccess) e = copy_state(A, A.W, Un);
     if (e == cudaSuccess) e = store_slot(A, 0);
     if (e != cudaSuccess) return fail(e);
-    if (!A.tape) build_schedule(A, n_steps, A.S);
+    if (!A.tape && !A.seg_len) build_schedule(A, n_steps, A.S);
     cudaEventRecord(e0, st);
-    e = A.tape ? taped(A, n_steps) : reverse(A, 0, n_steps, 0, A.S);
+    e = A.tape ? taped(A, n_steps)
+               : (A.seg_len ? segmented(A, n_steps) : reverse(A, 0, n_steps, 0, A.S));
     cudaEventRecord(e1, st);
     if (e != cudaSuccess) return fail(e);
     double Jh = 0.0;
@@ -1019,7 +1059,8 @@ extern "C" int swe_adjoint_gauge(swe_ctx *c, int n_steps, double dt, int n_gauge
     if (!c) return SWE_ERR_BAD_ARG;
     if (!c->uploaded || n_steps < 1 || !(dt > 0.0) ||
         n_gauges < 0 || (n_gauges > 0 && (!gauge_i || !gauge_j || !h_obs)) ||
-        (n_snapshots < 0 && n_snapshots != SWE_ADJ_TAPE_ALL) || !J ||
+        (n_snapshots < 0 && n_snapshots != SWE_ADJ_TAPE_ALL && n_snapshots != SWE_ADJ_SEGMENTS) ||
+        !J ||
         (!grad_h + !grad_hu + !grad_hv + !grad_B) % 4 != 0) {
         c->err = "swe_adjoint_gauge: bad argument (needs an uploaded context)";
         return SWE_ERR_BAD_ARG;

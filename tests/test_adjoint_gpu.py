@@ -102,7 +102,7 @@ def test_checkpoint_budget_does_not_change_the_gradient(gpu_lib, sw, problems):
     Nx, Ny, steps, dt = 20, 16, 13, 1e-3
     h, hu, hv, B, gauges, obs, _ = setup(problems, Nx, Ny, 0, steps, seed=23)
     base = gpu_adjoint(sw, h, hu, hv, B, Nx, Ny, steps, dt, gauges, obs, 0, snapshots=steps)
-    for snaps in (0, 1, 2, 4, "tape"):
+    for snaps in (0, 1, 2, 4, "tape", "segments"):
         r = gpu_adjoint(sw, h, hu, hv, B, Nx, Ny, steps, dt, gauges, obs, 0, snapshots=snaps)
         assert r["J"] == base["J"]
         for k in ("grad_h", "grad_hu", "grad_hv", "grad_B"):
@@ -172,7 +172,7 @@ def test_fp32_checkpoint_budget_does_not_change_the_gradient(gpu_lib, sw, proble
     h, hu, hv, B, gauges, obs, _ = setup(problems, Nx, Ny, 0, steps, seed=29)
     base = gpu_adjoint(sw, h, hu, hv, B, Nx, Ny, steps, dt, gauges, obs, 0, snapshots=steps,
                        precision="fp32_mixed")
-    for snaps in (0, 3, "tape"):
+    for snaps in (0, 3, "tape", "segments"):
         r = gpu_adjoint(sw, h, hu, hv, B, Nx, Ny, steps, dt, gauges, obs, 0, snapshots=snaps,
                         precision="fp32_mixed")
         assert r["J"] == base["J"]
