@@ -331,6 +331,157 @@ __global__ void __launch_bounds__((TI + 1) * TJ)
     }
 }
 
+// ---- Single grid: column sweeps --------------------------------------------------------
+//
+// Each warp owns 28 consecutive columns and one strip of F32_STRIP rows.  Lane l holds
+// column 28 g - 2 + l (lanes 0-1 and 30-31 are the neighbours' columns, the stencil
+// halo) and marches down the rows with a window of four rows of (eta, hu, hv, B) in
+// registers, loading each row once, straight from global memory: no shared-memory tile,
+// no barrier per tile.  At row r it computes the x-interface between rows r and r + 1
+// from its own window (the interface between r - 1 and r is the previous row's), and
+// the y-interface between its column and the next from row r of lanes l - 1 .. l + 2
+// (warp shuffles); the y-interface on its other side is lane l - 1's.  Lanes 2-29 then
+// update their cell.  Ghost cells are loaded through the same mirrored or clamped indices
+// as the tile loader, so every interface sees the values the tile kernel sees and the
+// arithmetic (face_flux_f32, the cell update) is the same.
+#ifndef SWE_F32_STRIP
+#define SWE_F32_STRIP 64
+#endif
+#ifndef SWE_F32_SINGLE_TILES
+#define SWE_F32_SINGLE_TILES 0  // 1: the single grid runs the tile kernel instead
+#endif
+constexpr int F32_COLS = 28, F32_WARPS = 4;
+
+struct RowF {
+    float e, u, v, b;
+};
+
+// Row ii (interior coordinates, possibly outside) of lane column jj, as the tile loader
+// stages it: ghosts mirror or clamp by the wall rule, B is read where it lies, and a
+// ghost's eta is its source cell's depth over the ghost's own bed.
+__device__ __forceinline__ RowF load_row_f32(const StageParams &p, int ii, int mj, bool fy,
+                                             int bj) {
+    bool fx;
+    const int mi = map_coord(ii, p.Nx, p.bc, fx);
+    const int bi = clamp_int(ii + NG, 0, p.Nx + 2 * NG - 1);
+    const long long k = (long long)(mi + NG) * p.pitch + (mj + NG);
+    const long long kb = (long long)bi * p.pitch + bj;
+    const float *Bg = static_cast<const float *>(p.B);
+    RowF r;
+    const float e = static_cast<const float *>(p.hs)[k];
+    const float u = static_cast<const float *>(p.hus)[k];
+    const float v = static_cast<const float *>(p.hvs)[k];
+    r.b = Bg[kb];
+    const float bsrc = kb == k ? r.b : Bg[k];
+    r.e = (r.b == bsrc) ? e : (e - bsrc) + r.b;
+    r.u = fx ? -u : u;
+    r.v = fy ? -v : v;
+    return r;
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(32 * F32_WARPS)
+    k_stage_f32_cols(const StageParams p) {
+    bool aborted;
+    const BlockDt bd = stage_dt_f32(p, aborted);
+    if (aborted) return;  // an earlier wait of this call gave up
+    const float dt = bd.f;
+    const int lane = threadIdx.x & 31;
+    const int grp = blockIdx.x * F32_WARPS + (threadIdx.x >> 5);
+    const int jj = grp * F32_COLS - NG + lane;  // this lane's column
+    bool fy;
+    const int mj = map_coord(jj, p.Ny, p.bc, fy);
+    const int bj = clamp_int(jj + NG, 0, p.Ny + 2 * NG - 1);
+    const bool out_col = lane >= NG && lane < NG + F32_COLS && jj < p.Ny;
+    const int r0 = blockIdx.y * SWE_F32_STRIP, r1 = min(r0 + SWE_F32_STRIP, p.Nx);
+    const float g = p.gf, half_g = p.half_gf, idx = p.inv_dxf, idy = p.inv_dyf;
+    const long long P = p.pitch;
+    float speed = 0.f;
+    if (grp * F32_COLS < p.Ny) {
+        // window: rows r - 1, r, r + 1, r + 2 for the x-interface between r and r + 1
+        RowF w0 = load_row_f32(p, r0 - 2, mj, fy, bj), w1 = load_row_f32(p, r0 - 1, mj, fy, bj);
+        RowF w2 = load_row_f32(p, r0, mj, fy, bj), w3 = load_row_f32(p, r0 + 1, mj, fy, bj);
+        FaceF xlo{};  // the x-interface below row r
+        for (int r = r0 - 1; r < r1; ++r) {
+            const RowF nx = load_row_f32(p, r + 3, mj, fy, bj);  // in flight during the row
+            const FaceF xhi = face_flux_f32(g, half_g, w0.e, w1.e, w2.e, w3.e, w0.u, w1.u, w2.u,
+                                            w3.u, w0.v, w1.v, w2.v, w3.v, w1.b, w2.b);
+            if (r >= r0) {
+                // row r is w1; the y-interface between this column and the next
+                const unsigned all = 0xffffffffu;
+                const float em1 = __shfl_up_sync(all, w1.e, 1), ep1 = __shfl_down_sync(all, w1.e, 1);
+                const float ep2 = __shfl_down_sync(all, w1.e, 2);
+                const float vm1 = __shfl_up_sync(all, w1.v, 1), vp1 = __shfl_down_sync(all, w1.v, 1);
+                const float vp2 = __shfl_down_sync(all, w1.v, 2);
+                const float um1 = __shfl_up_sync(all, w1.u, 1), up1 = __shfl_down_sync(all, w1.u, 1);
+                const float up2 = __shfl_down_sync(all, w1.u, 2);
+                const float bp1 = __shfl_down_sync(all, w1.b, 1);
+                const FaceF yhi = face_flux_f32(g, half_g, em1, w1.e, ep1, ep2, vm1, w1.v, vp1,
+                                                vp2, um1, w1.u, up1, up2, w1.b, bp1);
+                FaceF ylo;  // the y-interface on the other side is the previous lane's
+                ylo.fh = __shfl_up_sync(all, yhi.fh, 1);
+                ylo.fqt = __shfl_up_sync(all, yhi.fqt, 1);
+                ylo.fqn_m = __shfl_up_sync(all, yhi.fqn_m, 1);
+                ylo.fqn_p = __shfl_up_sync(all, yhi.fqn_p, 1);
+                if (out_col) {
+                    const float rh = -idx * (xhi.fh - xlo.fh) - idy * (yhi.fh - ylo.fh);
+                    const float rhu = -idx * (xhi.fqn_m - xlo.fqn_p) - idy * (yhi.fqt - ylo.fqt);
+                    const float rhv = -idx * (xhi.fqt - xlo.fqt) - idy * (yhi.fqn_m - ylo.fqn_p);
+                    const long long k = (long long)(r + NG) * P + (jj + NG);
+                    const float se = w1.e, su = w1.u, sv = w1.v, b = w1.b;
+                    float oe, ou, ov;
+                    if (STAGE == 1) {
+                        oe = se + dt * rh;
+                        ou = su + dt * rhu;
+                        ov = sv + dt * rhv;
+                    } else {
+                        const float ne = static_cast<const float *>(p.hn)[k];
+                        const float nu = static_cast<const float *>(p.hun)[k];
+                        const float nv = static_cast<const float *>(p.hvn)[k];
+                        if (STAGE == 2) {
+                            oe = 0.75f * ne + 0.25f * (se + dt * rh);
+                            ou = 0.75f * nu + 0.25f * (su + dt * rhu);
+                            ov = 0.75f * nv + 0.25f * (sv + dt * rhv);
+                        } else {
+                            const float c = 2.f / 3.f;  // see stage_tile_f32
+                            oe = ne + c * ((se + dt * rh) - ne);
+                            ou = nu + c * ((su + dt * rhu) - nu);
+                            ov = nv + c * ((sv + dt * rhv) - nv);
+                        }
+                    }
+                    const bool clamped = oe - b < H_FLOORF;
+                    if (clamped) {  // enforce_positivity on h = eta - B
+                        oe = b + H_FLOORF;
+                        ou = 0.f;
+                        ov = 0.f;
+                    }
+                    if (p.mask) p.mask[k] = clamped ? 1 : 0;  // for the adjoint
+                    if (!(fabsf(oe) + fabsf(ou) + fabsf(ov) < INFINITY))
+                        atomicOr(p.flags, FLAG_NONFINITE);
+                    static_cast<float *>(p.ho)[k] = oe;
+                    static_cast<float *>(p.huo)[k] = ou;
+                    static_cast<float *>(p.hvo)[k] = ov;
+                    if (STAGE == 3) speed = fmaxf(speed, cell_speed_f32(g, oe - b, ou, ov));
+                }
+            }
+            xlo = xhi;
+            w0 = w1;
+            w1 = w2;
+            w2 = w3;
+            w3 = nx;
+        }
+    }
+    if (STAGE == 1 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+        p.speed[p.slot_write] = 0ull;
+        if (p.dt_log) p.dt_log[p.log_index] = (double)dt;
+    }
+    if (STAGE == 3) {
+        block_max_to_slot_f(speed, p.speed + p.slot_write);
+        if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && p.t_accum)
+            *p.t_accum += (double)dt;
+    }
+}
+
 #ifndef SWE_ENS_F32_THREADS_PER_SM
 #define SWE_ENS_F32_THREADS_PER_SM 2016  // seven 8x32 tiles, the single-grid occupancy
 #endif
@@ -498,6 +649,17 @@ unsigned grid_for(long long n, int num_sms) {
 
 cudaError_t launch_stage_f32(int stage, const StageParams &p, const StageMaps *maps,
                              cudaStream_t s) {
+#if !SWE_F32_SINGLE_TILES
+    (void)maps;  // the column sweeps read global memory directly
+    const int groups = (p.Ny + F32_COLS - 1) / F32_COLS;
+    const dim3 grid_c((groups + F32_WARPS - 1) / F32_WARPS, (p.Nx + SWE_F32_STRIP - 1) / SWE_F32_STRIP);
+    switch (stage) {
+        case 1: k_stage_f32_cols<1><<<grid_c, 32 * F32_WARPS, 0, s>>>(p); break;
+        case 2: k_stage_f32_cols<2><<<grid_c, 32 * F32_WARPS, 0, s>>>(p); break;
+        default: k_stage_f32_cols<3><<<grid_c, 32 * F32_WARPS, 0, s>>>(p); break;
+    }
+    return cudaGetLastError();
+#endif
     constexpr int TI = TILE_I_F32, TJ = TILE_J_F32, NT = (TI + 1) * TJ;
     const dim3 grid((p.Ny + TJ - 1) / TJ, (p.Nx + TI - 1) / TI);
     StageMaps none;
