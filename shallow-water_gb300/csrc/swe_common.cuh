@@ -83,7 +83,11 @@ struct EnsParams {
     const void *maps;
 };
 
-enum : int { SHAPE_8x32 = 0, SHAPE_8x16 = 1, SHAPE_4x64 = 2, SHAPE_16x32 = 3, SHAPE_8x64 = 4 };
+enum : int { SHAPE_8x32 = 0, SHAPE_8x16 = 1, SHAPE_4x64 = 2, SHAPE_16x32 = 3, SHAPE_8x64 = 4,
+             SHAPE_COLS = 5 };
+// SHAPE_COLS (FP32 form): a work item is a strip of F32_STRIP_ROWS rows by F32_COL_BLOCK
+// columns, swept by column warps (swe_fp32.cu).
+constexpr int F32_STRIP_ROWS = 64, F32_COL_BLOCK = 112;
 
 // StageParams of instance q inside an ensemble launch.
 __device__ __forceinline__ StageParams ens_view(const EnsParams &e, int q) {

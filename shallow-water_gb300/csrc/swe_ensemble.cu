@@ -96,12 +96,15 @@ void shape_dims(int shape, int &TI, int &TJ) {
         case SHAPE_4x64: TI = 4; TJ = 64; break;
         case SHAPE_16x32: TI = 16; TJ = 32; break;
         case SHAPE_8x64: TI = 8; TJ = 64; break;
+        case SHAPE_COLS: TI = F32_STRIP_ROWS; TJ = F32_COL_BLOCK; break;
         default: TI = 8; TJ = 32; break;
     }
 }
 
 bool shape_ok(const swe_ens *c, int shape) {
-    if (c->f32) return shape == SHAPE_8x32 || shape == SHAPE_16x32 || shape == SHAPE_8x64;
+    if (c->f32)
+        return shape == SHAPE_8x32 || shape == SHAPE_16x32 || shape == SHAPE_8x64 ||
+               shape == SHAPE_COLS;
     return shape == SHAPE_8x32 || shape == SHAPE_8x16 || shape == SHAPE_4x64;
 }
 
@@ -188,7 +191,12 @@ int build_tiles(swe_ens *c) {
     ECK(cudaStreamSynchronize(c->stream));
     c->total_tiles = (int)total;
     destroy_graphs(c);
-    if (c->f32) build_maps(c, TI, TJ);
+    if (c->f32 && c->shape != SHAPE_COLS) {
+        build_maps(c, TI, TJ);
+    } else if (c->d_maps) {  // the column sweeps read global memory directly
+        cudaFree(c->d_maps);
+        c->d_maps = nullptr;
+    }
     return SWE_OK;
 }
 
@@ -616,13 +624,14 @@ int swe_ens_tune(swe_ens *c, int steps, double *best_ms) try {
         return SWE_OK;
     };
     const int shapes64[] = {SHAPE_8x32, SHAPE_8x16, SHAPE_4x64};
-    const int shapes32[] = {SHAPE_8x32, SHAPE_16x32, SHAPE_8x64};
+    const int shapes32[] = {SHAPE_COLS, SHAPE_8x32, SHAPE_16x32, SHAPE_8x64};
     const int *shapes = c->f32 ? shapes32 : shapes64;
+    const int n_shapes = c->f32 ? 4 : 3;
     // 0: one CTA per tile; 1 / 2: a persistent grid of every resident CTA / half of them
     const int grids[] = {0, 1, 2};
     double best = 1e300;
     int best_shape = c->shape, best_grid = c->grid;
-    for (int si = 0; si < 3; ++si) {
+    for (int si = 0; si < n_shapes; ++si) {
         for (int gm : grids) {
             int g = 0;
             if (gm > 0) {

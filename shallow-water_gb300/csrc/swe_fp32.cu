@@ -25,6 +25,7 @@
 #include "swe_launch.h"
 #include "swe_tma.cuh"
 
+#include <algorithm>
 #include <cstring>
 
 namespace swe {
@@ -345,12 +346,13 @@ __global__ void __launch_bounds__((TI + 1) * TJ)
 // as the tile loader, so every interface sees the values the tile kernel sees and the
 // arithmetic (face_flux_f32, the cell update) is the same.
 #ifndef SWE_F32_STRIP
-#define SWE_F32_STRIP 64
+#define SWE_F32_STRIP F32_STRIP_ROWS
 #endif
 #ifndef SWE_F32_SINGLE_TILES
 #define SWE_F32_SINGLE_TILES 0  // 1: the single grid runs the tile kernel instead
 #endif
 constexpr int F32_COLS = 28, F32_WARPS = 4;
+static_assert(F32_COLS * F32_WARPS == F32_COL_BLOCK, "SHAPE_COLS work item width");
 
 struct RowF {
     float e, u, v, b;
@@ -379,98 +381,105 @@ __device__ __forceinline__ RowF load_row_f32(const StageParams &p, int ii, int m
     return r;
 }
 
+// One warp's sweep: column group grp (columns 28 grp .. 28 grp + 27), rows [r0, r1) of
+// the grid p describes; returns the lane's max wave speed of the new state (stage 3).
 template <int STAGE>
-__global__ void __launch_bounds__(32 * F32_WARPS)
-    k_stage_f32_cols(const StageParams p) {
-    bool aborted;
-    const BlockDt bd = stage_dt_f32(p, aborted);
-    if (aborted) return;  // an earlier wait of this call gave up
-    const float dt = bd.f;
+__device__ __forceinline__ float col_sweep_f32(const StageParams &p, int grp, int r0, int r1,
+                                               float dt) {
     const int lane = threadIdx.x & 31;
-    const int grp = blockIdx.x * F32_WARPS + (threadIdx.x >> 5);
     const int jj = grp * F32_COLS - NG + lane;  // this lane's column
     bool fy;
     const int mj = map_coord(jj, p.Ny, p.bc, fy);
     const int bj = clamp_int(jj + NG, 0, p.Ny + 2 * NG - 1);
     const bool out_col = lane >= NG && lane < NG + F32_COLS && jj < p.Ny;
-    const int r0 = blockIdx.y * SWE_F32_STRIP, r1 = min(r0 + SWE_F32_STRIP, p.Nx);
     const float g = p.gf, half_g = p.half_gf, idx = p.inv_dxf, idy = p.inv_dyf;
     const long long P = p.pitch;
     float speed = 0.f;
-    if (grp * F32_COLS < p.Ny) {
-        // window: rows r - 1, r, r + 1, r + 2 for the x-interface between r and r + 1
-        RowF w0 = load_row_f32(p, r0 - 2, mj, fy, bj), w1 = load_row_f32(p, r0 - 1, mj, fy, bj);
-        RowF w2 = load_row_f32(p, r0, mj, fy, bj), w3 = load_row_f32(p, r0 + 1, mj, fy, bj);
-        FaceF xlo{};  // the x-interface below row r
-        for (int r = r0 - 1; r < r1; ++r) {
-            const RowF nx = load_row_f32(p, r + 3, mj, fy, bj);  // in flight during the row
-            const FaceF xhi = face_flux_f32(g, half_g, w0.e, w1.e, w2.e, w3.e, w0.u, w1.u, w2.u,
-                                            w3.u, w0.v, w1.v, w2.v, w3.v, w1.b, w2.b);
-            if (r >= r0) {
-                // row r is w1; the y-interface between this column and the next
-                const unsigned all = 0xffffffffu;
-                const float em1 = __shfl_up_sync(all, w1.e, 1), ep1 = __shfl_down_sync(all, w1.e, 1);
-                const float ep2 = __shfl_down_sync(all, w1.e, 2);
-                const float vm1 = __shfl_up_sync(all, w1.v, 1), vp1 = __shfl_down_sync(all, w1.v, 1);
-                const float vp2 = __shfl_down_sync(all, w1.v, 2);
-                const float um1 = __shfl_up_sync(all, w1.u, 1), up1 = __shfl_down_sync(all, w1.u, 1);
-                const float up2 = __shfl_down_sync(all, w1.u, 2);
-                const float bp1 = __shfl_down_sync(all, w1.b, 1);
-                const FaceF yhi = face_flux_f32(g, half_g, em1, w1.e, ep1, ep2, vm1, w1.v, vp1,
-                                                vp2, um1, w1.u, up1, up2, w1.b, bp1);
-                FaceF ylo;  // the y-interface on the other side is the previous lane's
-                ylo.fh = __shfl_up_sync(all, yhi.fh, 1);
-                ylo.fqt = __shfl_up_sync(all, yhi.fqt, 1);
-                ylo.fqn_m = __shfl_up_sync(all, yhi.fqn_m, 1);
-                ylo.fqn_p = __shfl_up_sync(all, yhi.fqn_p, 1);
-                if (out_col) {
-                    const float rh = -idx * (xhi.fh - xlo.fh) - idy * (yhi.fh - ylo.fh);
-                    const float rhu = -idx * (xhi.fqn_m - xlo.fqn_p) - idy * (yhi.fqt - ylo.fqt);
-                    const float rhv = -idx * (xhi.fqt - xlo.fqt) - idy * (yhi.fqn_m - ylo.fqn_p);
-                    const long long k = (long long)(r + NG) * P + (jj + NG);
-                    const float se = w1.e, su = w1.u, sv = w1.v, b = w1.b;
-                    float oe, ou, ov;
-                    if (STAGE == 1) {
-                        oe = se + dt * rh;
-                        ou = su + dt * rhu;
-                        ov = sv + dt * rhv;
+    // window: rows r - 1, r, r + 1, r + 2 for the x-interface between r and r + 1
+    RowF w0 = load_row_f32(p, r0 - 2, mj, fy, bj), w1 = load_row_f32(p, r0 - 1, mj, fy, bj);
+    RowF w2 = load_row_f32(p, r0, mj, fy, bj), w3 = load_row_f32(p, r0 + 1, mj, fy, bj);
+    FaceF xlo{};  // the x-interface below row r
+    for (int r = r0 - 1; r < r1; ++r) {
+        const RowF nx = load_row_f32(p, r + 3, mj, fy, bj);  // in flight during the row
+        const FaceF xhi = face_flux_f32(g, half_g, w0.e, w1.e, w2.e, w3.e, w0.u, w1.u, w2.u,
+                                        w3.u, w0.v, w1.v, w2.v, w3.v, w1.b, w2.b);
+        if (r >= r0) {
+            // row r is w1; the y-interface between this column and the next
+            const unsigned all = 0xffffffffu;
+            const float em1 = __shfl_up_sync(all, w1.e, 1), ep1 = __shfl_down_sync(all, w1.e, 1);
+            const float ep2 = __shfl_down_sync(all, w1.e, 2);
+            const float vm1 = __shfl_up_sync(all, w1.v, 1), vp1 = __shfl_down_sync(all, w1.v, 1);
+            const float vp2 = __shfl_down_sync(all, w1.v, 2);
+            const float um1 = __shfl_up_sync(all, w1.u, 1), up1 = __shfl_down_sync(all, w1.u, 1);
+            const float up2 = __shfl_down_sync(all, w1.u, 2);
+            const float bp1 = __shfl_down_sync(all, w1.b, 1);
+            const FaceF yhi = face_flux_f32(g, half_g, em1, w1.e, ep1, ep2, vm1, w1.v, vp1, vp2,
+                                            um1, w1.u, up1, up2, w1.b, bp1);
+            FaceF ylo;  // the y-interface on the other side is the previous lane's
+            ylo.fh = __shfl_up_sync(all, yhi.fh, 1);
+            ylo.fqt = __shfl_up_sync(all, yhi.fqt, 1);
+            ylo.fqn_m = __shfl_up_sync(all, yhi.fqn_m, 1);
+            ylo.fqn_p = __shfl_up_sync(all, yhi.fqn_p, 1);
+            if (out_col) {
+                const float rh = -idx * (xhi.fh - xlo.fh) - idy * (yhi.fh - ylo.fh);
+                const float rhu = -idx * (xhi.fqn_m - xlo.fqn_p) - idy * (yhi.fqt - ylo.fqt);
+                const float rhv = -idx * (xhi.fqt - xlo.fqt) - idy * (yhi.fqn_m - ylo.fqn_p);
+                const long long k = (long long)(r + NG) * P + (jj + NG);
+                const float se = w1.e, su = w1.u, sv = w1.v, b = w1.b;
+                float oe, ou, ov;
+                if (STAGE == 1) {
+                    oe = se + dt * rh;
+                    ou = su + dt * rhu;
+                    ov = sv + dt * rhv;
+                } else {
+                    const float ne = static_cast<const float *>(p.hn)[k];
+                    const float nu = static_cast<const float *>(p.hun)[k];
+                    const float nv = static_cast<const float *>(p.hvn)[k];
+                    if (STAGE == 2) {
+                        oe = 0.75f * ne + 0.25f * (se + dt * rh);
+                        ou = 0.75f * nu + 0.25f * (su + dt * rhu);
+                        ov = 0.75f * nv + 0.25f * (sv + dt * rhv);
                     } else {
-                        const float ne = static_cast<const float *>(p.hn)[k];
-                        const float nu = static_cast<const float *>(p.hun)[k];
-                        const float nv = static_cast<const float *>(p.hvn)[k];
-                        if (STAGE == 2) {
-                            oe = 0.75f * ne + 0.25f * (se + dt * rh);
-                            ou = 0.75f * nu + 0.25f * (su + dt * rhu);
-                            ov = 0.75f * nv + 0.25f * (sv + dt * rhv);
-                        } else {
-                            const float c = 2.f / 3.f;  // see stage_tile_f32
-                            oe = ne + c * ((se + dt * rh) - ne);
-                            ou = nu + c * ((su + dt * rhu) - nu);
-                            ov = nv + c * ((sv + dt * rhv) - nv);
-                        }
+                        const float c = 2.f / 3.f;  // see stage_tile_f32
+                        oe = ne + c * ((se + dt * rh) - ne);
+                        ou = nu + c * ((su + dt * rhu) - nu);
+                        ov = nv + c * ((sv + dt * rhv) - nv);
                     }
-                    const bool clamped = oe - b < H_FLOORF;
-                    if (clamped) {  // enforce_positivity on h = eta - B
-                        oe = b + H_FLOORF;
-                        ou = 0.f;
-                        ov = 0.f;
-                    }
-                    if (p.mask) p.mask[k] = clamped ? 1 : 0;  // for the adjoint
-                    if (!(fabsf(oe) + fabsf(ou) + fabsf(ov) < INFINITY))
-                        atomicOr(p.flags, FLAG_NONFINITE);
-                    static_cast<float *>(p.ho)[k] = oe;
-                    static_cast<float *>(p.huo)[k] = ou;
-                    static_cast<float *>(p.hvo)[k] = ov;
-                    if (STAGE == 3) speed = fmaxf(speed, cell_speed_f32(g, oe - b, ou, ov));
                 }
+                const bool clamped = oe - b < H_FLOORF;
+                if (clamped) {  // enforce_positivity on h = eta - B
+                    oe = b + H_FLOORF;
+                    ou = 0.f;
+                    ov = 0.f;
+                }
+                if (p.mask) p.mask[k] = clamped ? 1 : 0;  // for the adjoint
+                if (!(fabsf(oe) + fabsf(ou) + fabsf(ov) < INFINITY))
+                    atomicOr(p.flags, FLAG_NONFINITE);
+                static_cast<float *>(p.ho)[k] = oe;
+                static_cast<float *>(p.huo)[k] = ou;
+                static_cast<float *>(p.hvo)[k] = ov;
+                if (STAGE == 3) speed = fmaxf(speed, cell_speed_f32(g, oe - b, ou, ov));
             }
-            xlo = xhi;
-            w0 = w1;
-            w1 = w2;
-            w2 = w3;
-            w3 = nx;
         }
+        xlo = xhi;
+        w0 = w1;
+        w1 = w2;
+        w2 = w3;
+        w3 = nx;
     }
+    return speed;
+}
+
+template <int STAGE>
+__global__ void __launch_bounds__(32 * F32_WARPS) k_stage_f32_cols(const StageParams p) {
+    bool aborted;
+    const BlockDt bd = stage_dt_f32(p, aborted);
+    if (aborted) return;  // an earlier wait of this call gave up
+    const float dt = bd.f;
+    const int grp = blockIdx.x * F32_WARPS + (threadIdx.x >> 5);
+    const int r0 = blockIdx.y * SWE_F32_STRIP, r1 = min(r0 + SWE_F32_STRIP, p.Nx);
+    float speed = 0.f;
+    if (grp * F32_COLS < p.Ny) speed = col_sweep_f32<STAGE>(p, grp, r0, r1, dt);
     if (STAGE == 1 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
         p.speed[p.slot_write] = 0ull;
         if (p.dt_log) p.dt_log[p.log_index] = (double)dt;
@@ -479,6 +488,70 @@ __global__ void __launch_bounds__(32 * F32_WARPS)
         block_max_to_slot_f(speed, p.speed + p.slot_write);
         if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && p.t_accum)
             *p.t_accum += (double)dt;
+    }
+}
+
+// Ensemble form of the column sweeps: work item = (instance, block of F32_WARPS column
+// groups, strip of SWE_F32_STRIP rows), the SHAPE_COLS tiles of the work list.  The
+// schedule is the tile kernel's: one CTA per item, or contiguous shares of the list, with
+// the instance's view, dt and first-item duties set up once per instance met.
+template <int STAGE>
+__global__ void __launch_bounds__(32 * F32_WARPS) k_ens_stage_f32_cols(const EnsParams e) {
+    __shared__ StageParams s_p;
+    __shared__ int s_q, s_t, s_ntiles, s_abort;
+    __shared__ float s_dtf;
+    const int total = e.total_tiles;
+    int T0 = blockIdx.x, T1 = blockIdx.x + 1;
+    if ((int)gridDim.x < total) {
+        const int per = (total + (int)gridDim.x - 1) / (int)gridDim.x;
+        T0 = blockIdx.x * per;
+        T1 = min(total, T0 + per);
+    }
+    for (int T = T0; T < T1; ++T) {
+        if (threadIdx.x == 0) {
+            int q = s_q, t = s_t + 1;
+            const bool fresh = T == T0 || t == s_ntiles;
+            if (T == T0) {
+                q = e.tile_inst[T];
+                t = T - e.inst[q].tile_base;
+            } else if (t == s_ntiles) {
+                q = q + 1;  // the work list holds the instances' items in instance order
+                t = 0;
+            }
+            if (fresh) {
+                s_p = ens_view(e, q);
+                s_ntiles = ((e.inst[q].Nx + SWE_F32_STRIP - 1) / SWE_F32_STRIP) * e.inst[q].tiles_j;
+                double dt = e.dt_fixed;
+                if (!(dt > 0.0)) {
+                    const double ms = __longlong_as_double((long long)s_p.speed[s_p.slot_read]);
+                    dt = (ms <= EPS) ? 1.0e100 : s_p.cfl_min_dxdy / ms;
+                }
+                s_dtf = (float)dt;
+            }
+            s_q = q;
+            s_t = t;
+            s_abort = tma::timeout_set(e.flags);
+        }
+        __syncthreads();
+        if (s_abort) return;  // the call has failed: the launch ends
+        const StageParams &p = s_p;
+        const int q = s_q, t = s_t;
+        const int tiles_j = e.inst[q].tiles_j;
+        const int ti = t / tiles_j, tj = t - (t / tiles_j) * tiles_j;
+        const float dt = s_dtf;
+        const int grp = tj * F32_WARPS + (threadIdx.x >> 5);
+        const int r0 = ti * SWE_F32_STRIP, r1 = min(r0 + SWE_F32_STRIP, p.Nx);
+        float speed = 0.f;
+        if (grp * F32_COLS < p.Ny) speed = col_sweep_f32<STAGE>(p, grp, r0, r1, dt);
+        if (STAGE == 1 && t == 0 && threadIdx.x == 0) {
+            p.speed[p.slot_write] = 0ull;
+            if (e.dt_last) e.dt_last[q] = (double)dt;  // the FP32 dt the update applied
+        }
+        if (STAGE == 3) {
+            block_max_to_slot_f(speed, p.speed + p.slot_write);
+            if (t == 0 && threadIdx.x == 0) e.t[q] += (double)dt;
+        }
+        __syncthreads();  // the next item reuses the view
     }
 }
 
@@ -700,6 +773,16 @@ static int ens_resident_f32() {
 
 int ens_resident_per_sm_f32(int shape) {
     switch (shape) {
+        case SHAPE_COLS: {
+            int n1 = 0, n2 = 0, n3 = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_ens_stage_f32_cols<1>, 32 * F32_WARPS, 0) ||
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_ens_stage_f32_cols<2>, 32 * F32_WARPS, 0) ||
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n3, k_ens_stage_f32_cols<3>, 32 * F32_WARPS, 0)) {
+                cudaGetLastError();
+                return 0;
+            }
+            return std::min(n1, std::min(n2, n3));
+        }
         case SHAPE_8x32: return ens_resident_f32<8, 32>();
         case SHAPE_16x32: return ens_resident_f32<16, 32>();
         case SHAPE_8x64: return ens_resident_f32<8, 64>();
@@ -710,6 +793,13 @@ int ens_resident_per_sm_f32(int shape) {
 cudaError_t launch_ens_stage_f32(int shape, int stage, const EnsParams &e, int grid,
                                  cudaStream_t s) {
     switch (shape) {
+        case SHAPE_COLS:
+            switch (stage) {
+                case 1: k_ens_stage_f32_cols<1><<<grid, 32 * F32_WARPS, 0, s>>>(e); break;
+                case 2: k_ens_stage_f32_cols<2><<<grid, 32 * F32_WARPS, 0, s>>>(e); break;
+                default: k_ens_stage_f32_cols<3><<<grid, 32 * F32_WARPS, 0, s>>>(e); break;
+            }
+            return cudaGetLastError();
         case SHAPE_8x32: return ens_launch_f32<8, 32>(stage, e, grid, s);
         case SHAPE_16x32: return ens_launch_f32<16, 32>(stage, e, grid, s);
         case SHAPE_8x64: return ens_launch_f32<8, 64>(stage, e, grid, s);

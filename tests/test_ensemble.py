@@ -38,7 +38,7 @@ def test_fp64_ensemble_matches_oracle_per_instance(gpu_lib, sw, port, problems):
 @pytest.mark.parametrize("precision", ["fp64", "fp32_mixed"])
 def test_every_schedule_gives_identical_results(gpu_lib, sw, problems, precision):
     mem = members(problems, SIZES, seed=11)
-    shapes = ["8x32", "8x16", "4x64"] if precision == "fp64" else ["8x32", "16x32", "8x64"]
+    shapes = ["8x32", "8x16", "4x64"] if precision == "fp64" else ["8x32", "16x32", "8x64", "cols"]
     results = []
     for shape in shapes:
         for grid in (0, 152, 608):
