@@ -358,21 +358,79 @@ struct RowF {
     float e, u, v, b;
 };
 
+// Where the column sweep finds a grid's fields and constants.  GridAcc: one context's
+// stage, all in the kernel's parameters (constant bank).  EnsAcc: one ensemble
+// instance, its fields at a byte offset from the ensemble's pools (parameters) and its
+// sizes in registers.
+struct GridAcc {
+    const StageParams &p;
+    __device__ int Nx() const { return p.Nx; }
+    __device__ int Ny() const { return p.Ny; }
+    __device__ long long pitch() const { return p.pitch; }
+    __device__ int bc() const { return p.bc; }
+    __device__ float idx() const { return p.inv_dxf; }
+    __device__ float idy() const { return p.inv_dyf; }
+    __device__ float g() const { return p.gf; }
+    __device__ float half_g() const { return p.half_gf; }
+    __device__ const float *src(int f) const {
+        return static_cast<const float *>(f == 0 ? p.hs : (f == 1 ? p.hus : p.hvs));
+    }
+    __device__ const float *n(int f) const {
+        return static_cast<const float *>(f == 0 ? p.hn : (f == 1 ? p.hun : p.hvn));
+    }
+    __device__ float *out(int f) const {
+        return static_cast<float *>(f == 0 ? p.ho : (f == 1 ? p.huo : p.hvo));
+    }
+    __device__ const float *B() const { return static_cast<const float *>(p.B); }
+    __device__ unsigned char *mask() const { return p.mask; }
+    __device__ int *flags() const { return p.flags; }
+};
+
+struct EnsAcc {
+    const EnsParams &e;
+    long long off;  // bytes
+    int nx, ny;
+    long long pt;
+    float ix, iy;
+    __device__ int Nx() const { return nx; }
+    __device__ int Ny() const { return ny; }
+    __device__ long long pitch() const { return pt; }
+    __device__ int bc() const { return e.bc; }
+    __device__ float idx() const { return ix; }
+    __device__ float idy() const { return iy; }
+    __device__ float g() const { return e.gf; }
+    __device__ float half_g() const { return e.half_gf; }
+    __device__ const float *src(int f) const {
+        return reinterpret_cast<const float *>(static_cast<const char *>(e.src[f]) + off);
+    }
+    __device__ const float *n(int f) const {
+        return reinterpret_cast<const float *>(static_cast<const char *>(e.n[f]) + off);
+    }
+    __device__ float *out(int f) const {
+        return reinterpret_cast<float *>(static_cast<char *>(e.out[f]) + off);
+    }
+    __device__ const float *B() const {
+        return reinterpret_cast<const float *>(static_cast<const char *>(e.B) + off);
+    }
+    __device__ unsigned char *mask() const { return nullptr; }
+    __device__ int *flags() const { return e.flags; }
+};
+
 // Row ii (interior coordinates, possibly outside) of lane column jj, as the tile loader
 // stages it: ghosts mirror or clamp by the wall rule, B is read where it lies, and a
 // ghost's eta is its source cell's depth over the ghost's own bed.
-__device__ __forceinline__ RowF load_row_f32(const StageParams &p, int ii, int mj, bool fy,
-                                             int bj) {
+template <class Acc>
+__device__ __forceinline__ RowF load_row_f32(const Acc &a, int ii, int mj, bool fy, int bj) {
     bool fx;
-    const int mi = map_coord(ii, p.Nx, p.bc, fx);
-    const int bi = clamp_int(ii + NG, 0, p.Nx + 2 * NG - 1);
-    const long long k = (long long)(mi + NG) * p.pitch + (mj + NG);
-    const long long kb = (long long)bi * p.pitch + bj;
-    const float *Bg = static_cast<const float *>(p.B);
+    const int mi = map_coord(ii, a.Nx(), a.bc(), fx);
+    const int bi = clamp_int(ii + NG, 0, a.Nx() + 2 * NG - 1);
+    const long long k = (long long)(mi + NG) * a.pitch() + (mj + NG);
+    const long long kb = (long long)bi * a.pitch() + bj;
+    const float *Bg = a.B();
     RowF r;
-    const float e = static_cast<const float *>(p.hs)[k];
-    const float u = static_cast<const float *>(p.hus)[k];
-    const float v = static_cast<const float *>(p.hvs)[k];
+    const float e = a.src(0)[k];
+    const float u = a.src(1)[k];
+    const float v = a.src(2)[k];
     r.b = Bg[kb];
     const float bsrc = kb == k ? r.b : Bg[k];
     r.e = (r.b == bsrc) ? e : (e - bsrc) + r.b;
@@ -382,25 +440,23 @@ __device__ __forceinline__ RowF load_row_f32(const StageParams &p, int ii, int m
 }
 
 // One warp's sweep: column group grp (columns 28 grp .. 28 grp + 27), rows [r0, r1) of
-// the grid p describes; returns the lane's max wave speed of the new state (stage 3).
-template <int STAGE>
-__device__ __forceinline__ float col_sweep_f32(const StageParams &p, int grp, int r0, int r1,
-                                               float dt) {
+// the grid a describes; returns the lane's max wave speed of the new state (stage 3).
+template <int STAGE, class Acc>
+__device__ __forceinline__ float col_sweep_f32(const Acc &a, int grp, int r0, int r1, float dt) {
     const int lane = threadIdx.x & 31;
     const int jj = grp * F32_COLS - NG + lane;  // this lane's column
     bool fy;
-    const int mj = map_coord(jj, p.Ny, p.bc, fy);
-    const int bj = clamp_int(jj + NG, 0, p.Ny + 2 * NG - 1);
-    const bool out_col = lane >= NG && lane < NG + F32_COLS && jj < p.Ny;
-    const float g = p.gf, half_g = p.half_gf, idx = p.inv_dxf, idy = p.inv_dyf;
-    const long long P = p.pitch;
+    const int mj = map_coord(jj, a.Ny(), a.bc(), fy);
+    const int bj = clamp_int(jj + NG, 0, a.Ny() + 2 * NG - 1);
+    const bool out_col = lane >= NG && lane < NG + F32_COLS && jj < a.Ny();
+    const float g = a.g(), half_g = a.half_g(), idx = a.idx(), idy = a.idy();
     float speed = 0.f;
     // window: rows r - 1, r, r + 1, r + 2 for the x-interface between r and r + 1
-    RowF w0 = load_row_f32(p, r0 - 2, mj, fy, bj), w1 = load_row_f32(p, r0 - 1, mj, fy, bj);
-    RowF w2 = load_row_f32(p, r0, mj, fy, bj), w3 = load_row_f32(p, r0 + 1, mj, fy, bj);
+    RowF w0 = load_row_f32(a, r0 - 2, mj, fy, bj), w1 = load_row_f32(a, r0 - 1, mj, fy, bj);
+    RowF w2 = load_row_f32(a, r0, mj, fy, bj), w3 = load_row_f32(a, r0 + 1, mj, fy, bj);
     FaceF xlo{};  // the x-interface below row r
     for (int r = r0 - 1; r < r1; ++r) {
-        const RowF nx = load_row_f32(p, r + 3, mj, fy, bj);  // in flight during the row
+        const RowF nx = load_row_f32(a, r + 3, mj, fy, bj);  // in flight during the row
         const FaceF xhi = face_flux_f32(g, half_g, w0.e, w1.e, w2.e, w3.e, w0.u, w1.u, w2.u,
                                         w3.u, w0.v, w1.v, w2.v, w3.v, w1.b, w2.b);
         if (r >= r0) {
@@ -424,7 +480,7 @@ __device__ __forceinline__ float col_sweep_f32(const StageParams &p, int grp, in
                 const float rh = -idx * (xhi.fh - xlo.fh) - idy * (yhi.fh - ylo.fh);
                 const float rhu = -idx * (xhi.fqn_m - xlo.fqn_p) - idy * (yhi.fqt - ylo.fqt);
                 const float rhv = -idx * (xhi.fqt - xlo.fqt) - idy * (yhi.fqn_m - ylo.fqn_p);
-                const long long k = (long long)(r + NG) * P + (jj + NG);
+                const long long k = (long long)(r + NG) * a.pitch() + (jj + NG);
                 const float se = w1.e, su = w1.u, sv = w1.v, b = w1.b;
                 float oe, ou, ov;
                 if (STAGE == 1) {
@@ -432,9 +488,7 @@ __device__ __forceinline__ float col_sweep_f32(const StageParams &p, int grp, in
                     ou = su + dt * rhu;
                     ov = sv + dt * rhv;
                 } else {
-                    const float ne = static_cast<const float *>(p.hn)[k];
-                    const float nu = static_cast<const float *>(p.hun)[k];
-                    const float nv = static_cast<const float *>(p.hvn)[k];
+                    const float ne = a.n(0)[k], nu = a.n(1)[k], nv = a.n(2)[k];
                     if (STAGE == 2) {
                         oe = 0.75f * ne + 0.25f * (se + dt * rh);
                         ou = 0.75f * nu + 0.25f * (su + dt * rhu);
@@ -452,12 +506,13 @@ __device__ __forceinline__ float col_sweep_f32(const StageParams &p, int grp, in
                     ou = 0.f;
                     ov = 0.f;
                 }
-                if (p.mask) p.mask[k] = clamped ? 1 : 0;  // for the adjoint
+                unsigned char *mask = a.mask();
+                if (mask) mask[k] = clamped ? 1 : 0;  // for the adjoint
                 if (!(fabsf(oe) + fabsf(ou) + fabsf(ov) < INFINITY))
-                    atomicOr(p.flags, FLAG_NONFINITE);
-                static_cast<float *>(p.ho)[k] = oe;
-                static_cast<float *>(p.huo)[k] = ou;
-                static_cast<float *>(p.hvo)[k] = ov;
+                    atomicOr(a.flags(), FLAG_NONFINITE);
+                a.out(0)[k] = oe;
+                a.out(1)[k] = ou;
+                a.out(2)[k] = ov;
                 if (STAGE == 3) speed = fmaxf(speed, cell_speed_f32(g, oe - b, ou, ov));
             }
         }
@@ -479,7 +534,7 @@ __global__ void __launch_bounds__(32 * F32_WARPS) k_stage_f32_cols(const StagePa
     const int grp = blockIdx.x * F32_WARPS + (threadIdx.x >> 5);
     const int r0 = blockIdx.y * SWE_F32_STRIP, r1 = min(r0 + SWE_F32_STRIP, p.Nx);
     float speed = 0.f;
-    if (grp * F32_COLS < p.Ny) speed = col_sweep_f32<STAGE>(p, grp, r0, r1, dt);
+    if (grp * F32_COLS < p.Ny) speed = col_sweep_f32<STAGE>(GridAcc{p}, grp, r0, r1, dt);
     if (STAGE == 1 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
         p.speed[p.slot_write] = 0ull;
         if (p.dt_log) p.dt_log[p.log_index] = (double)dt;
@@ -495,8 +550,15 @@ __global__ void __launch_bounds__(32 * F32_WARPS) k_stage_f32_cols(const StagePa
 // groups, strip of SWE_F32_STRIP rows), the SHAPE_COLS tiles of the work list.  The
 // schedule is the tile kernel's: one CTA per item, or contiguous shares of the list, with
 // the instance's view, dt and first-item duties set up once per instance met.
+// Eight 128-thread CTAs per SM (64 registers): the per-instance addresses otherwise take
+// the ensemble sweep to 94 registers and 13.8 GCUPS on the 512-instance workload; with
+// the cap it runs at 18.6 (6 CTAs: 16.3).
+#ifndef SWE_ENS_F32_COL_MIN_BLOCKS
+#define SWE_ENS_F32_COL_MIN_BLOCKS 8
+#endif
 template <int STAGE>
-__global__ void __launch_bounds__(32 * F32_WARPS) k_ens_stage_f32_cols(const EnsParams e) {
+__global__ void __launch_bounds__(32 * F32_WARPS, SWE_ENS_F32_COL_MIN_BLOCKS)
+    k_ens_stage_f32_cols(const EnsParams e) {
     __shared__ StageParams s_p;
     __shared__ int s_q, s_t, s_ntiles, s_abort;
     __shared__ float s_dtf;
@@ -536,13 +598,15 @@ __global__ void __launch_bounds__(32 * F32_WARPS) k_ens_stage_f32_cols(const Ens
         if (s_abort) return;  // the call has failed: the launch ends
         const StageParams &p = s_p;
         const int q = s_q, t = s_t;
-        const int tiles_j = e.inst[q].tiles_j;
+        const EnsInst &I = e.inst[q];
+        const EnsAcc acc{e, I.off * e.elem, I.Nx, I.Ny, I.pitch, I.inv_dxf, I.inv_dyf};
+        const int tiles_j = I.tiles_j;
         const int ti = t / tiles_j, tj = t - (t / tiles_j) * tiles_j;
         const float dt = s_dtf;
         const int grp = tj * F32_WARPS + (threadIdx.x >> 5);
-        const int r0 = ti * SWE_F32_STRIP, r1 = min(r0 + SWE_F32_STRIP, p.Nx);
+        const int r0 = ti * SWE_F32_STRIP, r1 = min(r0 + SWE_F32_STRIP, acc.nx);
         float speed = 0.f;
-        if (grp * F32_COLS < p.Ny) speed = col_sweep_f32<STAGE>(p, grp, r0, r1, dt);
+        if (grp * F32_COLS < acc.ny) speed = col_sweep_f32<STAGE>(acc, grp, r0, r1, dt);
         if (STAGE == 1 && t == 0 && threadIdx.x == 0) {
             p.speed[p.slot_write] = 0ull;
             if (e.dt_last) e.dt_last[q] = (double)dt;  // the FP32 dt the update applied
