@@ -57,63 +57,97 @@ struct FaceF {
     float fh, fqt, fqn_m, fqn_p;
 };
 
+// The FP32 arithmetic below is written with explicit roundings (__fadd_rn, __fmul_rn,
+// fmaf): which products the compiler would fuse depends on the code around an inlined
+// copy, and every kernel that evaluates an interface or a cell update (the tile kernels,
+// the column sweeps, the ensemble forms) must give the same bits.
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+
 // One interface from the 4-cell stencil (m1, c0 | p1, p2) of eta, qn (normal momentum),
 // qt (tangential momentum) and the bathymetry of the two adjacent cells.
 __device__ __forceinline__ FaceF face_flux_f32(float g, float half_g, float e_m1, float e_0,
                                                float e_p1, float e_p2, float n_m1, float n_0,
                                                float n_p1, float n_p2, float t_m1, float t_0,
                                                float t_p1, float t_p2, float b_m, float b_p) {
-    const float eta_m = e_0 + 0.5f * minmodf(e_0 - e_m1, e_p1 - e_0);
-    const float eta_p = e_p1 - 0.5f * minmodf(e_p1 - e_0, e_p2 - e_p1);
-    const float qn_m = n_0 + 0.5f * minmodf(n_0 - n_m1, n_p1 - n_0);
-    const float qt_m = t_0 + 0.5f * minmodf(t_0 - t_m1, t_p1 - t_0);
-    const float qn_p = n_p1 - 0.5f * minmodf(n_p1 - n_0, n_p2 - n_p1);
-    const float qt_p = t_p1 - 0.5f * minmodf(t_p1 - t_0, t_p2 - t_p1);
+    const float eta_m = fmaf(0.5f, minmodf(fsub(e_0, e_m1), fsub(e_p1, e_0)), e_0);
+    const float eta_p = fmaf(-0.5f, minmodf(fsub(e_p1, e_0), fsub(e_p2, e_p1)), e_p1);
+    const float qn_m = fmaf(0.5f, minmodf(fsub(n_0, n_m1), fsub(n_p1, n_0)), n_0);
+    const float qt_m = fmaf(0.5f, minmodf(fsub(t_0, t_m1), fsub(t_p1, t_0)), t_0);
+    const float qn_p = fmaf(-0.5f, minmodf(fsub(n_p1, n_0), fsub(n_p2, n_p1)), n_p1);
+    const float qt_p = fmaf(-0.5f, minmodf(fsub(t_p1, t_0), fsub(t_p2, t_p1)), t_p1);
     const float b_star = fmaxf(b_m, b_p);
-    const float h_m = fmaxf(eta_m - b_m, 0.f);
-    const float h_p = fmaxf(eta_p - b_p, 0.f);
-    const float hs_m = fmaxf(eta_m - b_star, 0.f);
-    const float hs_p = fmaxf(eta_p - b_star, 0.f);
+    const float h_m = fmaxf(fsub(eta_m, b_m), 0.f);
+    const float h_p = fmaxf(fsub(eta_p, b_p), 0.f);
+    const float hs_m = fmaxf(fsub(eta_m, b_star), 0.f);
+    const float hs_p = fmaxf(fsub(eta_p, b_star), 0.f);
     const float ih_m = h_m > EPSF ? rcp_approx(h_m) : 0.f;
     const float ih_p = h_p > EPSF ? rcp_approx(h_p) : 0.f;
-    const float un_m = qn_m * ih_m, ut_m = qt_m * ih_m;
-    const float un_p = qn_p * ih_p, ut_p = qt_p * ih_p;
+    const float un_m = fmul(qn_m, ih_m), ut_m = fmul(qt_m, ih_m);
+    const float un_p = fmul(qn_p, ih_p), ut_p = fmul(qt_p, ih_p);
     // left / right hydrostatic states and their advective fluxes
-    const float qnL = hs_m * un_m, qtL = hs_m * ut_m;
-    const float qnR = hs_p * un_p, qtR = hs_p * ut_p;
-    const float aLn = qnL * un_m, aLt = qnL * ut_m;
-    const float aRn = qnR * un_p, aRt = qnR * ut_p;
-    const float cL = sqrt_approx(g * hs_m), cR = sqrt_approx(g * hs_p);
+    const float qnL = fmul(hs_m, un_m), qtL = fmul(hs_m, ut_m);
+    const float qnR = fmul(hs_p, un_p), qtR = fmul(hs_p, ut_p);
+    const float aLn = fmul(qnL, un_m), aLt = fmul(qnL, ut_m);
+    const float aRn = fmul(qnR, un_p), aRt = fmul(qnR, ut_p);
+    const float cL = sqrt_approx(fmul(g, hs_m)), cR = sqrt_approx(fmul(g, hs_p));
     // HLL with the wave speeds clamped to sL- = min(sL, 0), sR+ = max(sR, 0) covers the
     // three regimes without branches: sL >= 0 gives D = 0 (F* = F_L), sR <= 0 gives
     // D = dF (F* = F_R).  At a mirrored wall sL = -sR and k is exactly -1/2, so the wall
     // mass flux cancels exactly.
-    const float sLm = fminf(fminf(un_m - cL, un_p - cR), 0.f);
-    const float sRp = fmaxf(fmaxf(un_m + cL, un_p + cR), 0.f);
-    const float den = sRp - sLm;
-    const float k = (sLm + sRp == 0.f) ? (den > 0.f ? -0.5f : 0.f)
-                                       : sLm * rcp_approx(fmaxf(den, 1e-30f));
-    const float dFh = qnR - qnL;
-    const float dFn = (aRn - aLn) + half_g * (hs_p - hs_m) * (hs_p + hs_m);
-    const float dFt = aRt - aLt;
-    const float Dh = k * (sRp * (hs_p - hs_m) - dFh);
-    const float Dn = k * (sRp * (qnR - qnL) - dFn);
-    const float Dt = k * (sRp * (qtR - qtL) - dFt);
+    const float sLm = fminf(fminf(fsub(un_m, cL), fsub(un_p, cR)), 0.f);
+    const float sRp = fmaxf(fmaxf(fadd(un_m, cL), fadd(un_p, cR)), 0.f);
+    const float den = fsub(sRp, sLm);
+    const float k = (fadd(sLm, sRp) == 0.f) ? (den > 0.f ? -0.5f : 0.f)
+                                           : fmul(sLm, rcp_approx(fmaxf(den, 1e-30f)));
+    const float dhs = fsub(hs_p, hs_m);
+    const float dFh = fsub(qnR, qnL);
+    const float dFn = fmaf(fmul(half_g, dhs), fadd(hs_p, hs_m), fsub(aRn, aLn));
+    const float dFt = fsub(aRt, aLt);
+    // F* = F_L + D with D = k (s_R+ dU - dF), each fused into one rounding: F* is often
+    // much smaller than F_L and D, and a rounded product would leave an error of the size
+    // of F_L in it.
     // fqn_m = F*_n + g/2 (h_m^2 - hs_m^2) = aLn + Dn + g/2 h_m^2
     // fqn_p = F*_n + g/2 (h_p^2 - hs_p^2) = aLn + Dn + g/2 (hs_m^2 - hs_p^2) + g/2 h_p^2
     FaceF f;
-    f.fh = qnL + Dh;
-    f.fqt = aLt + Dt;
-    const float base = aLn + Dn;
-    f.fqn_m = base + half_g * h_m * h_m;
-    f.fqn_p = (base + half_g * (hs_m - hs_p) * (hs_m + hs_p)) + half_g * h_p * h_p;
+    f.fh = fmaf(k, fmaf(sRp, dhs, -dFh), qnL);
+    f.fqt = fmaf(k, fmaf(sRp, fsub(qtR, qtL), -dFt), aLt);
+    const float base = fmaf(k, fmaf(sRp, fsub(qnR, qnL), -dFn), aLn);
+    f.fqn_m = fmaf(fmul(half_g, h_m), h_m, base);
+    f.fqn_p = fmaf(fmul(half_g, h_p), h_p,
+                   fmaf(fmul(half_g, fsub(hs_m, hs_p)), fadd(hs_m, hs_p), base));
     return f;
 }
 
 __device__ __forceinline__ float cell_speed_f32(float g, float h, float hu, float hv) {
     const float ih = h > EPSF ? rcp_approx(h) : 0.f;
-    const float c = sqrt_approx(g * fmaxf(h, 0.f));
-    return fmaxf(fabsf(hu * ih) + c, fabsf(hv * ih) + c);
+    const float c = sqrt_approx(fmul(g, fmaxf(h, 0.f)));
+    return fmaxf(fadd(fabsf(fmul(hu, ih)), c), fadd(fabsf(fmul(hv, ih)), c));
+}
+
+// A ghost cell's eta: the source cell's depth over the ghost's own bed (eta itself where
+// the beds agree, so a flat surface stays bitwise flat).
+__device__ __forceinline__ float ghost_eta(float e, float bsrc, float b) {
+    return (b == bsrc) ? e : fadd(fsub(e, bsrc), b);
+}
+
+// The flux divergence of one cell from its four interfaces (apply_divergence's
+// -inv_dx (right - left) - inv_dy (top - bottom)).
+__device__ __forceinline__ float divergence(float idx, float idy, float xhi, float xlo,
+                                            float yhi, float ylo) {
+    return fmaf(-idy, fsub(yhi, ylo), fmul(-idx, fsub(xhi, xlo)));
+}
+
+// Stage combine of one field: 1: s + dt L; 2: 3/4 n + 1/4 (s + dt L); 3: n + c (s' - n)
+// with c = fl(2/3), s' = s + dt L (the FP32 weights fl(1/3) + fl(2/3) exceed 1 by 3e-8,
+// which would add mass every step; these sum to 1).
+template <int STAGE>
+__device__ __forceinline__ float combine_f32(float s, float n, float dt, float L) {
+    const float e = fmaf(dt, L, s);
+    if (STAGE == 1) return e;
+    if (STAGE == 2) return fmaf(0.75f, n, fmul(0.25f, e));
+    return fmaf(2.f / 3.f, fsub(e, n), n);
 }
 
 __device__ __forceinline__ void block_max_to_slot_f(float v, unsigned long long *slot) {
@@ -214,9 +248,7 @@ __device__ __forceinline__ float stage_tile_f32(const StageParams &p, int i0, in
             const float b = Bg[(long long)bi * P + bj];
             // A ghost holds the interior cell's depth over its own bed: eta_g = h_src + B_g
             // (eta itself where the beds agree, so a flat surface stays bitwise flat).
-            const float bsrc = Bg[k];
-            const float e = es[k];
-            s_e[r][c] = (b == bsrc) ? e : (e - bsrc) + b;
+            s_e[r][c] = ghost_eta(es[k], Bg[k], b);
             const float u = us[k], v = vs[k];
             s_u[r][c] = fx ? -u : u;
             s_v[r][c] = fy ? -v : v;
@@ -258,40 +290,27 @@ __device__ __forceinline__ float stage_tile_f32(const StageParams &p, int i0, in
     float speed = 0.f;
     if (inside) {
         const float idx = p.inv_dxf, idy = p.inv_dyf;
-        const float rh = -idx * (s_xf[0][ty + 1][tx] - s_xf[0][ty][tx]) -
-                         idy * (s_yf[0][ty][tx + 1] - s_yf[0][ty][tx]);
-        const float rhu = -idx * (s_xf[2][ty + 1][tx] - s_xf[3][ty][tx]) -
-                          idy * (s_yf[1][ty][tx + 1] - s_yf[1][ty][tx]);
-        const float rhv = -idx * (s_xf[1][ty + 1][tx] - s_xf[1][ty][tx]) -
-                          idy * (s_yf[2][ty][tx + 1] - s_yf[3][ty][tx]);
+        const float rh = divergence(idx, idy, s_xf[0][ty + 1][tx], s_xf[0][ty][tx],
+                                    s_yf[0][ty][tx + 1], s_yf[0][ty][tx]);
+        const float rhu = divergence(idx, idy, s_xf[2][ty + 1][tx], s_xf[3][ty][tx],
+                                     s_yf[1][ty][tx + 1], s_yf[1][ty][tx]);
+        const float rhv = divergence(idx, idy, s_xf[1][ty + 1][tx], s_xf[1][ty][tx],
+                                     s_yf[2][ty][tx + 1], s_yf[3][ty][tx]);
         const long long k = (long long)(ii + NG) * P + (jj + NG);
         const float se = s_e[ty + NG][tx + NG], su = s_u[ty + NG][tx + NG];
         const float sv = s_v[ty + NG][tx + NG], b = s_b[ty + NG][tx + NG];
-        float oe, ou, ov;
-        if (STAGE == 1) {
-            oe = se + dt * rh;
-            ou = su + dt * rhu;
-            ov = sv + dt * rhv;
-        } else {
-            const float ne = static_cast<const float *>(p.hn)[k];
-            const float nu = static_cast<const float *>(p.hun)[k];
-            const float nv = static_cast<const float *>(p.hvn)[k];
-            if (STAGE == 2) {
-                oe = 0.75f * ne + 0.25f * (se + dt * rh);
-                ou = 0.75f * nu + 0.25f * (su + dt * rhu);
-                ov = 0.75f * nv + 0.25f * (sv + dt * rhv);
-            } else {
-                // 1/3 n + 2/3 s' as n + c (s' - n): the FP32 weights fl(1/3) + fl(2/3)
-                // exceed 1 by 3e-8, which would add mass every step; these sum to 1.
-                const float c = 2.f / 3.f;
-                oe = ne + c * ((se + dt * rh) - ne);
-                ou = nu + c * ((su + dt * rhu) - nu);
-                ov = nv + c * ((sv + dt * rhv) - nv);
-            }
+        float ne = 0.f, nu = 0.f, nv = 0.f;
+        if (STAGE != 1) {
+            ne = static_cast<const float *>(p.hn)[k];
+            nu = static_cast<const float *>(p.hun)[k];
+            nv = static_cast<const float *>(p.hvn)[k];
         }
-        const bool clamped = oe - b < H_FLOORF;
+        float oe = combine_f32<STAGE>(se, ne, dt, rh);
+        float ou = combine_f32<STAGE>(su, nu, dt, rhu);
+        float ov = combine_f32<STAGE>(sv, nv, dt, rhv);
+        const bool clamped = fsub(oe, b) < H_FLOORF;
         if (clamped) {  // enforce_positivity on h = eta - B
-            oe = b + H_FLOORF;
+            oe = fadd(b, H_FLOORF);
             ou = 0.f;
             ov = 0.f;
         }
@@ -300,7 +319,7 @@ __device__ __forceinline__ float stage_tile_f32(const StageParams &p, int i0, in
         static_cast<float *>(p.ho)[k] = oe;
         static_cast<float *>(p.huo)[k] = ou;
         static_cast<float *>(p.hvo)[k] = ov;
-        if (STAGE == 3) speed = cell_speed_f32(g, oe - b, ou, ov);
+        if (STAGE == 3) speed = cell_speed_f32(g, fsub(oe, b), ou, ov);
     }
     return speed;
 }
@@ -432,8 +451,7 @@ __device__ __forceinline__ RowF load_row_f32(const Acc &a, int ii, int mj, bool 
     const float u = a.src(1)[k];
     const float v = a.src(2)[k];
     r.b = Bg[kb];
-    const float bsrc = kb == k ? r.b : Bg[k];
-    r.e = (r.b == bsrc) ? e : (e - bsrc) + r.b;
+    r.e = ghost_eta(e, kb == k ? r.b : Bg[k], r.b);
     r.u = fx ? -u : u;
     r.v = fy ? -v : v;
     return r;
@@ -455,8 +473,21 @@ __device__ __forceinline__ float col_sweep_f32(const Acc &a, int grp, int r0, in
     RowF w0 = load_row_f32(a, r0 - 2, mj, fy, bj), w1 = load_row_f32(a, r0 - 1, mj, fy, bj);
     RowF w2 = load_row_f32(a, r0, mj, fy, bj), w3 = load_row_f32(a, r0 + 1, mj, fy, bj);
     FaceF xlo{};  // the x-interface below row r
+    // U^n of the lane's cell in row r (stages 2 and 3), loaded a row ahead; lanes without
+    // an output cell read their mapped column, which is inside the grid
+    auto load_n = [&](int r, float &ne, float &nu, float &nv) {
+        if (STAGE == 1 || r >= r1) return;
+        const long long k = (long long)(r + NG) * a.pitch() + (mj + NG);
+        ne = a.n(0)[k];
+        nu = a.n(1)[k];
+        nv = a.n(2)[k];
+    };
+    float ne = 0.f, nu = 0.f, nv = 0.f;
+    load_n(r0, ne, nu, nv);
     for (int r = r0 - 1; r < r1; ++r) {
         const RowF nx = load_row_f32(a, r + 3, mj, fy, bj);  // in flight during the row
+        float ne1 = 0.f, nu1 = 0.f, nv1 = 0.f;
+        if (r >= r0) load_n(r + 1, ne1, nu1, nv1);
         const FaceF xhi = face_flux_f32(g, half_g, w0.e, w1.e, w2.e, w3.e, w0.u, w1.u, w2.u,
                                         w3.u, w0.v, w1.v, w2.v, w3.v, w1.b, w2.b);
         if (r >= r0) {
@@ -477,32 +508,17 @@ __device__ __forceinline__ float col_sweep_f32(const Acc &a, int grp, int r0, in
             ylo.fqn_m = __shfl_up_sync(all, yhi.fqn_m, 1);
             ylo.fqn_p = __shfl_up_sync(all, yhi.fqn_p, 1);
             if (out_col) {
-                const float rh = -idx * (xhi.fh - xlo.fh) - idy * (yhi.fh - ylo.fh);
-                const float rhu = -idx * (xhi.fqn_m - xlo.fqn_p) - idy * (yhi.fqt - ylo.fqt);
-                const float rhv = -idx * (xhi.fqt - xlo.fqt) - idy * (yhi.fqn_m - ylo.fqn_p);
+                const float rh = divergence(idx, idy, xhi.fh, xlo.fh, yhi.fh, ylo.fh);
+                const float rhu = divergence(idx, idy, xhi.fqn_m, xlo.fqn_p, yhi.fqt, ylo.fqt);
+                const float rhv = divergence(idx, idy, xhi.fqt, xlo.fqt, yhi.fqn_m, ylo.fqn_p);
                 const long long k = (long long)(r + NG) * a.pitch() + (jj + NG);
-                const float se = w1.e, su = w1.u, sv = w1.v, b = w1.b;
-                float oe, ou, ov;
-                if (STAGE == 1) {
-                    oe = se + dt * rh;
-                    ou = su + dt * rhu;
-                    ov = sv + dt * rhv;
-                } else {
-                    const float ne = a.n(0)[k], nu = a.n(1)[k], nv = a.n(2)[k];
-                    if (STAGE == 2) {
-                        oe = 0.75f * ne + 0.25f * (se + dt * rh);
-                        ou = 0.75f * nu + 0.25f * (su + dt * rhu);
-                        ov = 0.75f * nv + 0.25f * (sv + dt * rhv);
-                    } else {
-                        const float c = 2.f / 3.f;  // see stage_tile_f32
-                        oe = ne + c * ((se + dt * rh) - ne);
-                        ou = nu + c * ((su + dt * rhu) - nu);
-                        ov = nv + c * ((sv + dt * rhv) - nv);
-                    }
-                }
-                const bool clamped = oe - b < H_FLOORF;
+                const float b = w1.b;
+                float oe = combine_f32<STAGE>(w1.e, ne, dt, rh);
+                float ou = combine_f32<STAGE>(w1.u, nu, dt, rhu);
+                float ov = combine_f32<STAGE>(w1.v, nv, dt, rhv);
+                const bool clamped = fsub(oe, b) < H_FLOORF;
                 if (clamped) {  // enforce_positivity on h = eta - B
-                    oe = b + H_FLOORF;
+                    oe = fadd(b, H_FLOORF);
                     ou = 0.f;
                     ov = 0.f;
                 }
@@ -513,7 +529,7 @@ __device__ __forceinline__ float col_sweep_f32(const Acc &a, int grp, int r0, in
                 a.out(0)[k] = oe;
                 a.out(1)[k] = ou;
                 a.out(2)[k] = ov;
-                if (STAGE == 3) speed = fmaxf(speed, cell_speed_f32(g, oe - b, ou, ov));
+                if (STAGE == 3) speed = fmaxf(speed, cell_speed_f32(g, fsub(oe, b), ou, ov));
             }
         }
         xlo = xhi;
@@ -521,6 +537,11 @@ __device__ __forceinline__ float col_sweep_f32(const Acc &a, int grp, int r0, in
         w1 = w2;
         w2 = w3;
         w3 = nx;
+        if (r >= r0) {
+            ne = ne1;
+            nu = nu1;
+            nv = nv1;
+        }
     }
     return speed;
 }
