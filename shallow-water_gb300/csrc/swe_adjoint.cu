@@ -101,8 +101,11 @@ __device__ __forceinline__ void w_at(const AdjParams<T> &a, int i, int j, T w[3]
 // row i.  The stencil is staged exactly as the forward kernel stages it: the state of
 // ghost cells from the mirrored (reflecting, normal momentum negated) or clamped
 // (transmissive) interior cell, B where it lies, ghosts included.
+#ifndef SWE_ADJ_FACES_MIN_BLOCKS
+#define SWE_ADJ_FACES_MIN_BLOCKS 1
+#endif
 template <class T, int STAGE, int DIR>
-__global__ void __launch_bounds__(AFT) k_adj_faces(const AdjParams<T> a) {
+__global__ void __launch_bounds__(AFT, SWE_ADJ_FACES_MIN_BLOCKS) k_adj_faces(const AdjParams<T> a) {
     const int t = blockIdx.x * AFT + threadIdx.x;
     const int along = DIR == 0 ? a.Ny : a.Ny + 1;  // contiguous index range
     if (t >= along) return;

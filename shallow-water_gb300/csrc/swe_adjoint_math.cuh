@@ -190,12 +190,13 @@ SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceI
     const T de0 = in.e[1] - in.e[0], de1 = in.e[2] - in.e[1], de2 = in.e[3] - in.e[2];
     const T dn0 = in.n[1] - in.n[0], dn1 = in.n[2] - in.n[1], dn2 = in.n[3] - in.n[2];
     const T dt0 = in.t[1] - in.t[0], dt1 = in.t[2] - in.t[1], dt2 = in.t[3] - in.t[2];
-    const T eta_m = in.e[1] + half * msel_(de0, de1, s_em);
-    const T eta_p = in.e[2] - half * msel_(de1, de2, s_ep);
-    const T qn_m = in.n[1] + half * msel_(dn0, dn1, s_nm);
-    const T qt_m = in.t[1] + half * msel_(dt0, dt1, s_tm);
-    const T qn_p = in.n[2] - half * msel_(dn1, dn2, s_np);
-    const T qt_p = in.t[2] - half * msel_(dt1, dt2, s_tp);
+    // halving is exact: an integer-pipe exponent step for double
+    const T eta_m = in.e[1] + half_(msel_(de0, de1, s_em));
+    const T eta_p = in.e[2] - half_(msel_(de1, de2, s_ep));
+    const T qn_m = in.n[1] + half_(msel_(dn0, dn1, s_nm));
+    const T qt_m = in.t[1] + half_(msel_(dt0, dt1, s_tm));
+    const T qn_p = in.n[2] - half_(msel_(dn1, dn2, s_np));
+    const T qt_p = in.t[2] - half_(msel_(dt1, dt2, s_tp));
     const bool bstar_is_p = lt_(in.bm, in.bp);  // std::max(bm, bp) == (bm < bp) ? bp : bm
     const T bs = bstar_is_p ? in.bp : in.bm;
     const T xm = eta_m - in.bm, xp = eta_p - in.bp;
@@ -220,8 +221,9 @@ SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceI
     const bool sL_is2 = lt_(a2, a1), sR_is2 = lt_(b1, b2);
     const T sL = sL_is2 ? a2 : a1, sR = sR_is2 ? b2 : b1;
     const T hg = half * g;
-    const T FL[3] = {qnL, qnL * unL + hg * hL * hL, qnL * utL};
-    const T FR[3] = {qnR, qnR * unR + hg * hR * hR, qnR * utR};
+    // g/2 h^2 as (g h) h / 2: the halving is exact, so these are (g/2 h) h bit for bit
+    const T FL[3] = {qnL, qnL * unL + half_(ghL * hL), qnL * utL};
+    const T FR[3] = {qnR, qnR * unR + half_(ghR * hR), qnR * utR};
     const T UL[3] = {hL, qnL, qtL}, UR[3] = {hR, qnR, qtR};
     const int regime = !lt_(sL, T(0)) ? 0 : (!lt_(T(0), sR) ? 1 : 2);
 
