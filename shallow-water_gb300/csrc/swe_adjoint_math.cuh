@@ -240,20 +240,22 @@ SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceI
     } else {
         // F = (sR FL - sL FR + sL sR dU) / (sR - sL) with dU = UR - UL, G = FR - FL:
         // dF/dsR = sL (G - sL dU) / (sR - sL)^2, dF/dsL = sR (sR dU - G) / (sR - sL)^2
+        // with A = sum dF G and S = sum dF dU: sum dF (G - sL dU) = A - sL S and
+        // sum dF (sR dU - G) = sR S - A
         const T inv = rcp_(sR - sL);
         const T sLi = sL * inv, sRi = sR * inv, sLsRi = sL * sRi;
-        T gR = 0, gL = 0;
+        T A = 0, S = 0;
         for (int c = 0; c < 3; ++c) {
             const T dU = UR[c] - UL[c], G = FR[c] - FL[c];
             dFL[c] = dF[c] * sRi;
             dFR[c] = -dF[c] * sLi;
             dUR[c] = dF[c] * sLsRi;
             dUL[c] = -dUR[c];
-            gR += dF[c] * (G - sL * dU);
-            gL += dF[c] * (sR * dU - G);
+            A += dF[c] * G;
+            S += dF[c] * dU;
         }
-        dsR = gR * sLi * inv;
-        dsL = gL * sRi * inv;
+        dsR = (A - sL * S) * (sLi * inv);
+        dsL = (sR * S - A) * (sRi * inv);
     }
     T dunL = 0, dunR = 0, dcL = 0, dcR = 0;
     if (sL_is2) {
