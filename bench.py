@@ -48,11 +48,11 @@ FP64_OPS_ON_INTEGER_PIPES = 18
 # The same count for lone 8x32 tiles (2.16 interfaces per cell instead of 2.06).
 FP64_OPS_PER_CELL_UPDATE_LONE_TILES = 483.9
 # Warp instructions per cell update (the three stages) of the FP32 kernels, from their
-# ncu captures: the single-grid stage kernel (15.7 + 15.9 + 17.4) and the ensemble stage
-# kernel (17.6 + 16.9 + 18.6).  Both are bound by instruction issue, 4 warp instructions
-# per clock per SM.
-F32_WARP_INST_PER_CELL_UPDATE = 49.0
-F32_ENS_WARP_INST_PER_CELL_UPDATE = 53.1
+# ncu captures: the single grid's column sweeps (13.7 + 14.6 + 15.5) and the ensemble's
+# column sweeps (14.5 + 16.5 + 16.9).  Both are bound by instruction issue (4 warp
+# instructions per clock per SM) and load latency.
+F32_WARP_INST_PER_CELL_UPDATE = 43.9
+F32_ENS_WARP_INST_PER_CELL_UPDATE = 48.0
 
 
 def parse():

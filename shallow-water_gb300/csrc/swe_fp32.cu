@@ -21,6 +21,13 @@
 //
 // Layout: eta, hu, hv, B are FP32 ghosted arrays with the same pitch rule as the FP64
 // form.  The wall boundary condition is applied by mirrored indices while loading.
+//
+// Kernels: the single grid runs column sweeps (k_stage_f32_cols: a warp marches 28
+// columns down a strip of rows with a register window).  Ensembles run the same sweeps
+// over work items of 64 x 112 cells (SHAPE_COLS), or tile kernels (8x32, 16x32, 8x64
+// tiles staged in shared memory, interior tiles by TMA); the autotuner picks.  Every
+// kernel evaluates the interfaces and cell updates with the same explicitly rounded
+// arithmetic, so all of them give the same bits.
 #include "swe_common.cuh"
 #include "swe_launch.h"
 #include "swe_tma.cuh"
@@ -324,33 +331,6 @@ __device__ __forceinline__ float stage_tile_f32(const StageParams &p, int i0, in
     return speed;
 }
 
-template <int TI, int TJ, int STAGE>
-__global__ void __launch_bounds__((TI + 1) * TJ)
-    k_stage_f32(const StageParams p, const __grid_constant__ CUtensorMap tm_e,
-                const __grid_constant__ CUtensorMap tm_u, const __grid_constant__ CUtensorMap tm_v,
-                const __grid_constant__ CUtensorMap tm_b, const int use_tma) {
-    __shared__ __align__(8) uint64_t s_bar;
-    if (use_tma && threadIdx.x == 0) tma::mbar_init(&s_bar, 1);  // visible after stage_dt
-    bool aborted;
-    const BlockDt bd = stage_dt_f32(p, aborted);
-    if (aborted) return;  // an earlier wait of this call gave up
-    const float dt = bd.f;
-    const tma::TileMaps maps{&tm_e, &tm_u, &tm_v, &tm_b};
-    tma::Pipe pipe{&s_bar, 0u};
-    const float speed = stage_tile_f32<TI, TJ, STAGE>(p, blockIdx.y * TI, blockIdx.x * TJ, dt,
-                                                      use_tma ? &maps : nullptr, pipe, aborted);
-    if (aborted) return;
-    if (STAGE == 1 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
-        p.speed[p.slot_write] = 0ull;
-        if (p.dt_log) p.dt_log[p.log_index] = (double)dt;
-    }
-    if (STAGE == 3) {
-        block_max_to_slot_f(speed, p.speed + p.slot_write);
-        if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && p.t_accum)
-            *p.t_accum += (double)dt;
-    }
-}
-
 // ---- Single grid: column sweeps --------------------------------------------------------
 //
 // Each warp owns 28 consecutive columns and one strip of F32_STRIP rows.  Lane l holds
@@ -366,9 +346,6 @@ __global__ void __launch_bounds__((TI + 1) * TJ)
 // arithmetic (face_flux_f32, the cell update) is the same.
 #ifndef SWE_F32_STRIP
 #define SWE_F32_STRIP F32_STRIP_ROWS
-#endif
-#ifndef SWE_F32_SINGLE_TILES
-#define SWE_F32_SINGLE_TILES 0  // 1: the single grid runs the tile kernel instead
 #endif
 constexpr int F32_COLS = 28, F32_WARPS = 4;
 static_assert(F32_COLS * F32_WARPS == F32_COL_BLOCK, "SHAPE_COLS work item width");
@@ -813,27 +790,13 @@ unsigned grid_for(long long n, int num_sms) {
 
 cudaError_t launch_stage_f32(int stage, const StageParams &p, const StageMaps *maps,
                              cudaStream_t s) {
-#if !SWE_F32_SINGLE_TILES
     (void)maps;  // the column sweeps read global memory directly
     const int groups = (p.Ny + F32_COLS - 1) / F32_COLS;
-    const dim3 grid_c((groups + F32_WARPS - 1) / F32_WARPS, (p.Nx + SWE_F32_STRIP - 1) / SWE_F32_STRIP);
+    const dim3 grid((groups + F32_WARPS - 1) / F32_WARPS, (p.Nx + SWE_F32_STRIP - 1) / SWE_F32_STRIP);
     switch (stage) {
-        case 1: k_stage_f32_cols<1><<<grid_c, 32 * F32_WARPS, 0, s>>>(p); break;
-        case 2: k_stage_f32_cols<2><<<grid_c, 32 * F32_WARPS, 0, s>>>(p); break;
-        default: k_stage_f32_cols<3><<<grid_c, 32 * F32_WARPS, 0, s>>>(p); break;
-    }
-    return cudaGetLastError();
-#endif
-    constexpr int TI = TILE_I_F32, TJ = TILE_J_F32, NT = (TI + 1) * TJ;
-    const dim3 grid((p.Ny + TJ - 1) / TJ, (p.Nx + TI - 1) / TI);
-    StageMaps none;
-    std::memset(&none, 0, sizeof none);
-    const StageMaps &m = maps ? *maps : none;
-    const int use = maps ? 1 : 0;
-    switch (stage) {
-        case 1: k_stage_f32<TI, TJ, 1><<<grid, NT, 0, s>>>(p, m.e, m.u, m.v, m.b, use); break;
-        case 2: k_stage_f32<TI, TJ, 2><<<grid, NT, 0, s>>>(p, m.e, m.u, m.v, m.b, use); break;
-        default: k_stage_f32<TI, TJ, 3><<<grid, NT, 0, s>>>(p, m.e, m.u, m.v, m.b, use); break;
+        case 1: k_stage_f32_cols<1><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
+        case 2: k_stage_f32_cols<2><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
+        default: k_stage_f32_cols<3><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
     }
     return cudaGetLastError();
 }
