@@ -528,7 +528,7 @@ __device__ __forceinline__ float col_sweep_f32(const Acc &a, int grp, int r0, in
 #ifndef SWE_F32_COL_MIN_BLOCKS
 #define SWE_F32_COL_MIN_BLOCKS 8
 #endif
-template <int STAGE>
+template <int STAGE, int STRIP>
 __global__ void __launch_bounds__(32 * F32_WARPS, SWE_F32_COL_MIN_BLOCKS)
     k_stage_f32_cols(const StageParams p) {
     bool aborted;
@@ -536,7 +536,7 @@ __global__ void __launch_bounds__(32 * F32_WARPS, SWE_F32_COL_MIN_BLOCKS)
     if (aborted) return;  // an earlier wait of this call gave up
     const float dt = bd.f;
     const int grp = blockIdx.x * F32_WARPS + (threadIdx.x >> 5);
-    const int r0 = blockIdx.y * SWE_F32_STRIP, r1 = min(r0 + SWE_F32_STRIP, p.Nx);
+    const int r0 = blockIdx.y * STRIP, r1 = min(r0 + STRIP, p.Nx);
     float speed = 0.f;
     if (grp * F32_COLS < p.Ny) speed = col_sweep_f32<STAGE>(GridAcc{p}, grp, r0, r1, dt);
     if (STAGE == 1 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
@@ -792,11 +792,29 @@ cudaError_t launch_stage_f32(int stage, const StageParams &p, const StageMaps *m
                              cudaStream_t s) {
     (void)maps;  // the column sweeps read global memory directly
     const int groups = (p.Ny + F32_COLS - 1) / F32_COLS;
-    const dim3 grid((groups + F32_WARPS - 1) / F32_WARPS, (p.Nx + SWE_F32_STRIP - 1) / SWE_F32_STRIP);
-    switch (stage) {
-        case 1: k_stage_f32_cols<1><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
-        case 2: k_stage_f32_cols<2><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
-        default: k_stage_f32_cols<3><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
+    // Strips of SWE_F32_STRIP rows, shorter on small grids so that there are warps enough
+    // to fill the GPU (a strip costs four extra row loads; 1024^2 in strips of 64 rows
+    // would be 160 CTAs).
+    static_assert(SWE_F32_STRIP == 64, "the strip lengths compiled below");
+    int strip = SWE_F32_STRIP;
+    const long long kWarps = 8192;
+    while (strip > 8 && (long long)groups * ((p.Nx + strip - 1) / strip) < kWarps) strip /= 2;
+    const dim3 grid((groups + F32_WARPS - 1) / F32_WARPS, (p.Nx + strip - 1) / strip);
+    switch (stage * 1000 + strip) {  // the strip length is a template parameter: a loop
+                                     // bound known to the compiler is worth 10% at 16384^2
+        case 1064: k_stage_f32_cols<1, 64><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
+        case 1032: k_stage_f32_cols<1, 32><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
+        case 1016: k_stage_f32_cols<1, 16><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
+        case 1008: k_stage_f32_cols<1, 8><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
+        case 2064: k_stage_f32_cols<2, 64><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
+        case 2032: k_stage_f32_cols<2, 32><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
+        case 2016: k_stage_f32_cols<2, 16><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
+        case 2008: k_stage_f32_cols<2, 8><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
+        case 3064: k_stage_f32_cols<3, 64><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
+        case 3032: k_stage_f32_cols<3, 32><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
+        case 3016: k_stage_f32_cols<3, 16><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
+        case 3008: k_stage_f32_cols<3, 8><<<grid, 32 * F32_WARPS, 0, s>>>(p); break;
+        default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }
