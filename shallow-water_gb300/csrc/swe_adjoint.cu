@@ -64,6 +64,7 @@ struct AdjParams {
     long long pitch;
     int bc;
     T inv_dx, inv_dy, g, dt;
+    T kx, ky;  // the stage's source weight x dt x 1/dx (1/dy): divergence to flux adjoint
 };
 
 template <class T>
@@ -94,6 +95,19 @@ __device__ __forceinline__ void w_at(const AdjParams<T> &a, int i, int j, T w[3]
     w[0] = f * a.lo_h[k];
     w[1] = f * a.lo_hu[k];
     w[2] = f * a.lo_hv[k];
+}
+
+// The stage output's adjoint at interior cell (i, j), zero where the stage clamped the
+// depth and outside; k_adj_faces scales its differences by the stage's kx or ky.
+template <class T>
+__device__ __forceinline__ void lo_at(const AdjParams<T> &a, int i, int j, T l[3]) {
+    l[0] = l[1] = l[2] = T(0);
+    if (i < 0 || i >= a.Nx || j < 0 || j >= a.Ny) return;
+    const long long k = (long long)(i + NG) * a.pitch + (j + NG);
+    if (a.mask[k]) return;
+    l[0] = a.lo_h[k];
+    l[1] = a.lo_hu[k];
+    l[2] = a.lo_hv[k];
 }
 
 // One interface per thread.  DIR 0: x-interface f in [-1, Nx - 1] between rows f and
@@ -134,21 +148,21 @@ __global__ void __launch_bounds__(AFT, SWE_ADJ_FACES_MIN_BLOCKS) k_adj_faces(con
         if (q == 1) in.bm = b;
         if (q == 2) in.bp = b;
     }
-    T wm[3], wp[3];
+    T lm[3], lp[3];
     if (DIR == 0) {
-        w_at<T, STAGE>(a, f, o, wm);
-        w_at<T, STAGE>(a, f + 1, o, wp);
+        lo_at(a, f, o, lm);
+        lo_at(a, f + 1, o, lp);
     } else {
-        w_at<T, STAGE>(a, o, f, wm);
-        w_at<T, STAGE>(a, o, f + 1, wp);
+        lo_at(a, o, f, lm);
+        lo_at(a, o, f + 1, lp);
     }
-    const T inv = DIR == 0 ? a.inv_dx : a.inv_dy;
+    const T k = DIR == 0 ? a.kx : a.ky;
     const int n = DIR == 0 ? 1 : 2, tg = DIR == 0 ? 2 : 1;  // normal / tangential field
     adj::FaceOut<T> d;
-    d.fh = inv * (wp[0] - wm[0]);
-    d.fqt = inv * (wp[tg] - wm[tg]);
-    d.fqn_m = -inv * wm[n];
-    d.fqn_p = inv * wp[n];
+    d.fh = k * (lp[0] - lm[0]);
+    d.fqt = k * (lp[tg] - lm[tg]);
+    d.fqn_m = -k * lm[n];
+    d.fqn_p = k * lp[n];
     adj::FaceIn<T> ad;
     adj::face_vjp(in, a.g, T(EPS), d, ad);
     T *C = DIR == 0 ? a.cx : a.cy;
@@ -216,7 +230,6 @@ __device__ __forceinline__ void gather_dir(const AdjParams<T> &a, int ca, int ot
             const long long x = at(f);
             const T ce = C[k * pl + x], cn = C[(4 + k) * pl + x];
             acc_h += ce;
-            if (!eta_state<T>()) acc_B += ce;  // eta = h + B read at the interface
             acc_qn += fl[q] ? -cn : cn;
             acc_qt += C[(8 + k) * pl + x];
         }
@@ -235,6 +248,7 @@ __global__ void __launch_bounds__(AGT) k_adj_gather(const AdjParams<T> a) {
     T acc_h = T(0), acc_hu = T(0), acc_hv = T(0), acc_B = T(0);
     gather_dir<T, 0>(a, ci, cj, acc_h, acc_hu, acc_hv, acc_B);
     gather_dir<T, 1>(a, cj, ci, acc_h, acc_hv, acc_hu, acc_B);
+    if (!eta_state<T>()) acc_B += acc_h;  // every interface read eta = h + B
     const long long k = (long long)(ci + NG) * a.pitch + (cj + NG);
     const bool m = a.mask[k];
     // a clamped FP32 cell is eta = B + floor: its eta adjoint goes to B
@@ -593,6 +607,11 @@ cudaError_t launch_adj(Adj<T> &A, int stage, T *const *state, T *const *lo,
     p.inv_dy = (T)c->inv_dy;
     p.g = (T)c->p.g;
     p.dt = (T)A.dt;
+    {
+        const double w = stage == 1 ? 1.0 : (stage == 2 ? 0.25 : 2.0 / 3.0);
+        p.kx = (T)(w * A.dt * c->inv_dx);
+        p.ky = (T)(w * A.dt * c->inv_dy);
+    }
     p.cx = A.cx;
     p.cy = A.cy;
     p.px = (long long)(c->p.Nx + 1) * c->p.Ny;
@@ -727,18 +746,21 @@ cudaError_t taped(Adj<T> &A, int n) { return tape_and_reverse(A, 0, n, 0); }
 
 // Segmented schedule: a first sweep stores U^(s L) in snapshot slot s for the segments
 // of L steps; each segment, last first, is then recomputed once from its snapshot with
-// its stage states taped (slots A.nseg + 1 + j), and reversed.  Every step is advanced
-// twice (the sweep and its segment's taped recomputation), with memory for
-// ceil(n / L) + 1 snapshots and a tape of L steps.
+// its stage states taped (slots A.nseg + 1 + j), and reversed.  Every step but those of
+// the last segment is advanced twice (the sweep and its segment's taped recomputation),
+// with memory for ceil(n / L) + 1 snapshots and a tape of L steps.
+// The first sweep stops at the last segment's start and that segment is taped and
+// reversed straight away, so its steps are advanced once only.
 template <class T>
 cudaError_t segmented(Adj<T> &A, int n) {
     const int L = A.seg_len;
-    for (int k = 0; k + 1 < n; ++k) {  // the last step's end state is not needed
+    const int last = A.nseg - 1;
+    for (int k = 0; k < last * L; ++k) {
         ACK(forward_step(A, A.W, A.W, false));
         if ((k + 1) % L == 0) ACK(store_slot(A, (k + 1) / L));
     }
     const int base = A.nseg + 1;
-    for (int sg = A.nseg - 1; sg >= 0; --sg) {
+    for (int sg = last; sg >= 0; --sg) {
         const int l = sg * L, m = std::min(L, n - l);
         T *src[3] = {slot_field(A, sg, 0), slot_field(A, sg, 1), slot_field(A, sg, 2)};
         T *dst[3] = {slot_field(A, base, 0), slot_field(A, base, 1), slot_field(A, base, 2)};

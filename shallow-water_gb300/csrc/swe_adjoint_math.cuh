@@ -178,13 +178,24 @@ SWE_HD T msel_(T a, T b, int &sel) {
 //
 // The forward part is recomputed for its branch decisions and intermediates with one
 // reciprocal per depth (q/h as q * (1/h)), the hydrostatic velocities (hs*u)/hs taken as
-// u (equal in exact arithmetic) and the wave speed from rsqrt; these differ from the
-// forward's rounding by an ulp, which matters only at exact ties of a branch test.  The
-// reverse sweep reuses the same reciprocals, so one interface costs three divisions and
-// two reciprocal square roots instead of two dozen divisions.
+// u (equal in exact arithmetic) and the wave speed from one root; these differ from the
+// forward's rounding by an ulp, which matters only at exact ties of a branch test.
+//
+// Reverse sweep.  Each side (L: the minus cell's hydrostatic state, R: the plus cell's)
+// has depth h, velocities u, v, and the flux velocities uc, vc (u, v where h > eps,
+// else 0): U = (h, h u, h v) and F = (h u, h u uc + g h^2 / 2, h u vc).  The HLL flux
+// is F* = aL FL + aR FR + bL UL + bR UR with (aL, aR, bL, bR) = (1, 0, 0, 0) if
+// sL >= 0, (0, 1, 0, 0) if sR <= 0, else (sR, -sL, -sL sR, sL sR) / (sR - sL).  With
+// the side sums P = dF . (1, u, v) and Pc = dF . (1, uc, vc),
+//   dF . F = h u Pc + dF1 g h^2 / 2   and   dF . U = h P,
+// so each side's adjoints are
+//   dh = a (u Pc + dF1 g h) + b P,   du = h (a (Pc + dF1 uc) + b dF1),
+//   dv = h dF2 (a uc + b),
+// and the HLL speed derivatives take the sums A = dF . (FR - FL) and
+// S = dF . (UR - UL) from the same P: no flux vector is formed.  One interface costs
+// three reciprocals and two roots on the integer pipe and about 100 FP64 operations.
 template <class T>
 SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceIn<T> &a) {
-    const T half = T(0.5);
     // ---- forward recomputation, keeping branch decisions ----
     int s_em, s_ep, s_nm, s_tm, s_np, s_tp;
     const T de0 = in.e[1] - in.e[0], de1 = in.e[2] - in.e[1], de2 = in.e[3] - in.e[2];
@@ -204,122 +215,71 @@ SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceI
     const T h_m = pm ? xm : T(0), h_p = pp ? xp : T(0);
     const bool wm = lt_(eps, h_m), wp = lt_(eps, h_p);
     const T rm = wm ? rcp_(h_m) : T(0), rp = wp ? rcp_(h_p) : T(0);
-    const T un_m = qn_m * rm, ut_m = qt_m * rm;
-    const T un_p = qn_p * rp, ut_p = qt_p * rp;
+    const T uL = qn_m * rm, vL = qt_m * rm, uR = qn_p * rp, vR = qt_p * rp;
     const T yL = eta_m - bs, yR = eta_p - bs;
     const bool pL = pos_(yL), pR = pos_(yR);
     const T hL = pL ? yL : T(0), hR = pR ? yR : T(0);
-    const T qnL = hL * un_m, qtL = hL * ut_m, qnR = hR * un_p, qtR = hR * ut_p;
     const bool wL = lt_(eps, hL), wR = lt_(eps, hR);
-    const T unL = wL ? un_m : T(0), utL = wL ? ut_m : T(0);
-    const T unR = wR ? un_p : T(0), utR = wR ? ut_p : T(0);
+    const T uLc = wL ? uL : T(0), uRc = wR ? uR : T(0);
     const T ghL = g * hL, ghR = g * hR;
     T cL, rcL, cR, rcR;
     speed_(ghL, cL, rcL);
     speed_(ghR, cR, rcR);
-    const T a1 = unL - cL, a2 = unR - cR, b1 = unL + cL, b2 = unR + cR;
+    const T a1 = uLc - cL, a2 = uRc - cR, b1 = uLc + cL, b2 = uRc + cR;
     const bool sL_is2 = lt_(a2, a1), sR_is2 = lt_(b1, b2);
     const T sL = sL_is2 ? a2 : a1, sR = sR_is2 ? b2 : b1;
-    const T hg = half * g;
-    // g/2 h^2 as (g h) h / 2: the halving is exact, so these are (g/2 h) h bit for bit
-    const T FL[3] = {qnL, qnL * unL + half_(ghL * hL), qnL * utL};
-    const T FR[3] = {qnR, qnR * unR + half_(ghR * hR), qnR * utR};
-    const T UL[3] = {hL, qnL, qtL}, UR[3] = {hR, qnR, qtR};
     const int regime = !lt_(sL, T(0)) ? 0 : (!lt_(T(0), sR) ? 1 : 2);
 
     // ---- reverse sweep ----
-    const T dF[3] = {d.fh, d.fqn_m + d.fqn_p, d.fqt};
-    T dh_m = g * h_m * d.fqn_m, dh_p = g * h_p * d.fqn_p;
-    T dhL = -ghL * d.fqn_m, dhR = -ghR * d.fqn_p;
-    T dFL[3] = {0, 0, 0}, dFR[3] = {0, 0, 0}, dUL[3] = {0, 0, 0}, dUR[3] = {0, 0, 0};
-    T dsL = 0, dsR = 0;
-    if (regime == 0) {
-        for (int c = 0; c < 3; ++c) dFL[c] = dF[c];
-    } else if (regime == 1) {
-        for (int c = 0; c < 3; ++c) dFR[c] = dF[c];
-    } else {
-        // F = (sR FL - sL FR + sL sR dU) / (sR - sL) with dU = UR - UL, G = FR - FL:
-        // dF/dsR = sL (G - sL dU) / (sR - sL)^2, dF/dsL = sR (sR dU - G) / (sR - sL)^2
-        // with A = sum dF G and S = sum dF dU: sum dF (G - sL dU) = A - sL S and
-        // sum dF (sR dU - G) = sR S - A
-        const T inv = rcp_(sR - sL);
-        const T sLi = sL * inv, sRi = sR * inv, sLsRi = sL * sRi;
-        T A = 0, S = 0;
-        for (int c = 0; c < 3; ++c) {
-            const T dU = UR[c] - UL[c], G = FR[c] - FL[c];
-            dFL[c] = dF[c] * sRi;
-            dFR[c] = -dF[c] * sLi;
-            dUR[c] = dF[c] * sLsRi;
-            dUL[c] = -dUR[c];
-            A += dF[c] * G;
-            S += dF[c] * dU;
-        }
-        dsR = (A - sL * S) * (sLi * inv);
-        dsL = (sR * S - A) * (sRi * inv);
+    const T dF0 = d.fh, dF1 = d.fqn_m + d.fqn_p, dF2 = d.fqt;
+    const T PL = dF0 + dF1 * uL + dF2 * vL, PR = dF0 + dF1 * uR + dF2 * vR;
+    const T PLc = wL ? PL : dF0, PRc = wR ? PR : dF0;
+    T aL = regime == 0 ? T(1) : T(0), aR = regime == 1 ? T(1) : T(0);
+    T bL = T(0), bR = T(0);
+    T duLs = T(0), dcL = T(0), duRs = T(0), dcR = T(0);  // through the wave speeds
+    if (regime == 2) {
+        const T W = rcp_(sR - sL);
+        const T sRW = sR * W, sLW = sL * W;
+        aL = sRW;
+        aR = -sLW;
+        bR = sL * sRW;
+        bL = -bR;
+        // dF*/dsR = sL (FR - FL - sL (UR - UL)) W^2, dF*/dsL = sR (sR (UR - UL) - FR + FL) W^2
+        const T S = hR * PR - hL * PL;
+        const T A = ((hR * uR) * PRc - (hL * uL) * PLc) + half_(dF1 * (ghR * hR - ghL * hL));
+        const T dsR = (A - sL * S) * (sLW * W);
+        const T dsL = (sR * S - A) * (sRW * W);
+        // sL = min(uLc - cL, uRc - cR), sR = max(uLc + cL, uRc + cR)
+        const T sum = dsL + dsR, diff = dsR - dsL;
+        const bool lL = !sL_is2, lR = !sR_is2;  // the speed taken from side L
+        duLs = lL ? (lR ? sum : dsL) : (lR ? dsR : T(0));
+        dcL = lL ? (lR ? diff : -dsL) : (lR ? dsR : T(0));
+        duRs = lL ? (lR ? T(0) : dsR) : (lR ? dsL : sum);
+        dcR = lL ? (lR ? T(0) : dsR) : (lR ? -dsL : diff);
     }
-    T dunL = 0, dunR = 0, dcL = 0, dcR = 0;
-    if (sL_is2) {
-        dunR += dsL;
-        dcR -= dsL;
-    } else {
-        dunL += dsL;
-        dcL -= dsL;
-    }
-    if (sR_is2) {
-        dunR += dsR;
-        dcR += dsR;
-    } else {
-        dunL += dsR;
-        dcL += dsR;
-    }
-    dhL += dcL * hg * rcL;  // dc/dh = g / (2 c)
-    dhR += dcR * hg * rcR;
-    // physical fluxes FL = (qnL, qnL unL + g/2 hL^2, qnL utL); U = (h, qn, qt)
-    const T dqnL = dFL[0] + dFL[1] * unL + dFL[2] * utL + dUL[1];
-    const T dqtL = dUL[2];
-    dunL += dFL[1] * qnL;
-    T dutL = dFL[2] * qnL;
-    dhL += dFL[1] * ghL + dUL[0];
-    const T dqnR = dFR[0] + dFR[1] * unR + dFR[2] * utR + dUR[1];
-    const T dqtR = dUR[2];
-    dunR += dFR[1] * qnR;
-    T dutR = dFR[2] * qnR;
-    dhR += dFR[1] * ghR + dUR[0];
-    // unL = un_m (wet L), qnL = hL un_m, ...
-    T dun_m = dqnL * hL + (wL ? dunL : T(0)), dut_m = dqtL * hL + (wL ? dutL : T(0));
-    T dun_p = dqnR * hR + (wR ? dunR : T(0)), dut_p = dqtR * hR + (wR ? dutR : T(0));
-    dhL += dqnL * un_m + dqtL * ut_m;
-    dhR += dqnR * un_p + dqtR * ut_p;
-    // hL = max(eta_m - bs, 0)
-    T deta_m = 0, deta_p = 0, dbs = 0;
-    if (pL) {
-        deta_m += dhL;
-        dbs -= dhL;
-    }
-    if (pR) {
-        deta_p += dhR;
-        dbs -= dhR;
-    }
-    // un_m = qn_m / h_m (wet)
-    const T dqn_m = dun_m * rm, dqt_m = dut_m * rm;
-    const T dqn_p = dun_p * rp, dqt_p = dut_p * rp;
-    dh_m -= (dun_m * un_m + dut_m * ut_m) * rm;
-    dh_p -= (dun_p * un_p + dut_p * ut_p) * rp;
-    // h_m = max(eta_m - bm, 0)
-    T dbm = 0, dbp = 0;
-    if (pm) {
-        deta_m += dh_m;
-        dbm -= dh_m;
-    }
-    if (pp) {
-        deta_p += dh_p;
-        dbp -= dh_p;
-    }
-    if (bstar_is_p)
-        dbp += dbs;
-    else
-        dbm += dbs;
-    // reconstructions: x_m = x1 + m(x1-x0, x2-x1)/2, x_p = x2 - m(x2-x1, x3-x2)/2
+    const T hg = half_(g);
+    // side L, then its hydrostatic correction g/2 (h_m^2 - hL^2) of the minus flux and
+    // the wave speed c = sqrt(g h) (dc/dh = g / (2 c))
+    const T aLP = aL * PLc, aLF = aL * dF1;
+    const T dhL = ((aLP * uL + (aLF * ghL + bL * PL)) - ghL * d.fqn_m) + dcL * (hg * rcL);
+    const T duL = hL * (aLF * uLc + (aLP + bL * dF1)) + (wL ? duLs : T(0));
+    const T dvL = (hL * dF2) * (aL * uLc + bL);
+    const T aRP = aR * PRc, aRF = aR * dF1;
+    const T dhR = ((aRP * uR + (aRF * ghR + bR * PR)) - ghR * d.fqn_p) + dcR * (hg * rcR);
+    const T duR = hR * (aRF * uRc + (aRP + bR * dF1)) + (wR ? duRs : T(0));
+    const T dvR = (hR * dF2) * (aR * uRc + bR);
+    // velocities u = q / h_m: dq = du / h_m, dh_m = -(du u + dv v) / h_m
+    const T dqn_m = duL * rm, dqt_m = dvL * rm, dqn_p = duR * rp, dqt_p = dvR * rp;
+    const T dh_m = (g * h_m) * d.fqn_m - (duL * uL + dvL * vL) * rm;
+    const T dh_p = (g * h_p) * d.fqn_p - (duR * uR + dvR * vR) * rp;
+    // hL = max(eta_m - bs, 0), h_m = max(eta_m - bm, 0), bs = max(bm, bp)
+    const T eL = pL ? dhL : T(0), eR = pR ? dhR : T(0);
+    const T em = pm ? dh_m : T(0), ep = pp ? dh_p : T(0);
+    const T deta_m = eL + em, deta_p = eR + ep;
+    const T dbs = -(eL + eR);
+    const T dstar = dbs - (bstar_is_p ? ep : em);  // the bed bs was taken from
+    a.bm = bstar_is_p ? -em : dstar;
+    a.bp = bstar_is_p ? dstar : -ep;
     // reconstructions x_m = x1 + m(x1-x0, x2-x1)/2 and x_p = x2 - m(x2-x1, x3-x2)/2, with
     // minmod selecting its first argument (sel 1), its second (sel 2) or zero (sel 0)
     auto recon = [&](T *ax, T dxm, int sm, T dxp, int sp) {
@@ -332,8 +292,6 @@ SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceI
     recon(a.e, deta_m, s_em, deta_p, s_ep);
     recon(a.n, dqn_m, s_nm, dqn_p, s_np);
     recon(a.t, dqt_m, s_tm, dqt_p, s_tp);
-    a.bm = dbm;
-    a.bp = dbp;
 }
 
 }  // namespace adj
