@@ -283,7 +283,11 @@ __global__ void __launch_bounds__(AGT) k_adj_gather(const AdjParams<T> a) {
 // shared memory in the two-pass gather's order, so the results are bitwise the same.
 // The interface contributions never reach HBM: about 70 bytes per cell and stage move
 // instead of about 300, which is what bounds the FP32 reverse sweep.
-constexpr int ATI = 8, ATJ = 32, ATT = ATI * ATJ;
+#ifndef SWE_ADJ_TILE_I
+#define SWE_ADJ_TILE_I 8
+#endif
+constexpr int ATI = SWE_ADJ_TILE_I, ATJ = 32, ATT = ATI * ATJ;
+constexpr int AT_MIN_BLOCKS = 1024 / ATT;  // 64 registers a thread
 
 template <class T>
 struct AdjTile {
@@ -294,7 +298,7 @@ struct AdjTile {
 };
 
 template <class T, int STAGE>
-__global__ void __launch_bounds__(ATT, 4) k_adj_tile(const AdjParams<T> a) {
+__global__ void __launch_bounds__(ATT, AT_MIN_BLOCKS) k_adj_tile(const AdjParams<T> a) {
     extern __shared__ __align__(16) unsigned char adj_smem[];
     AdjTile<T> &t = *reinterpret_cast<AdjTile<T> *>(adj_smem);
     const int tid = threadIdx.x;
