@@ -128,8 +128,18 @@ SWE_HD bool pos_(T a) {  // a > 0
 }
 template <class T>
 SWE_HD T rcp_(T a) {
-    if constexpr (std::is_same<T, double>::value) return sf::div_rn(1.0, a);
-    else return T(1) / a;
+    if constexpr (std::is_same<T, double>::value) {
+        return sf::div_rn(1.0, a);
+    } else {
+#if defined(__CUDA_ARCH__)
+        // FP32: the approximate reciprocal (about 1 ulp) of the FP32 forward's velocities
+        float r;
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(a));
+        return r;
+#else
+        return T(1) / a;
+#endif
+    }
 }
 template <class T>
 SWE_HD T half_(T a) {  // 0.5 * a, exact
