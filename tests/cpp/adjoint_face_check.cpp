@@ -1,13 +1,16 @@
 // Checks the interface VJP (shallow-water_gb300/csrc/swe_adjoint_math.cuh) against central
 // finite differences of the interface forward function, in FP64, on random states that
 // exercise every HLL regime, minmod branch and dry guard.  Points where a branch flips
-// inside the difference stencil (one-sided differences disagree) are skipped.  Built and
-// run by tests/test_adjoint_cpu.py.
+// inside the difference stencil (one-sided differences disagree) are skipped.  Then
+// against the textbook derivation of the same VJP (adjoint_face_textbook.h), which must
+// agree to rounding everywhere, nearly dry sides included.  Built and run by
+// tests/test_adjoint_cpu.py.
 #include <cmath>
 #include <cstdio>
 #include <random>
 
 #include "../../shallow-water_gb300/csrc/swe_adjoint_math.cuh"
+#include "adjoint_face_textbook.h"
 
 using namespace swe::adj;
 
@@ -76,5 +79,48 @@ int main(int argc, char **argv) {
     (void)regimes;
     std::printf("checked %ld partials, skipped %ld at kinks, worst rel err %.3g, %ld bad\n",
                 checked, skipped, worst, bad);
-    return bad ? 1 : 0;
+
+    // The two derivations, relative to the largest partial of each case.  Case kinds:
+    // subsonic and supersonic flow, a dry plus side, hydrostatic depths of 0 to 5e-9 on
+    // either side (below the 1e-8 wet threshold while the cell itself is wet), a dry
+    // minus cell.
+    long differ = 0;
+    double worst_tb = 0.0;
+    for (int c = 0; c < 12 * cases; ++c) {
+        FaceIn<double> in;
+        const int kind = c % 6;
+        const double flow = kind == 0 ? 6.0 : 0.4;
+        for (int k = 0; k < 4; ++k) {
+            in.e[k] = 1.0 + 0.2 * u(rng);
+            in.n[k] = flow * u(rng) + (kind == 0 ? 4.0 * ((c / 6) % 2 ? 1 : -1) : 0.0);
+            in.t[k] = 0.3 * u(rng);
+        }
+        in.bm = 0.3 * u(rng);
+        in.bp = 0.3 * u(rng);
+        if (kind == 1) in.bp = in.e[2] + 0.05 * std::fabs(u(rng));
+        if (kind == 2) {
+            for (int k = 0; k < 4; ++k) in.e[k] = in.e[1];
+            in.bp = in.e[1] - 0.5e-8 * std::fabs(u(rng));
+            in.bm = in.bp - 0.1;
+        }
+        if (kind == 3) {
+            for (int k = 0; k < 4; ++k) in.e[k] = in.e[2];
+            in.bm = in.e[2] - 0.5e-8 * std::fabs(u(rng));
+            in.bp = in.bm - 0.1;
+        }
+        if (kind == 4) in.bm = in.e[1] + 0.1;
+        FaceOut<double> w{u(rng), u(rng), u(rng), u(rng)};
+        FaceIn<double> a, b;
+        face_vjp(in, g, 1e-8, w, a);
+        swe::adj_textbook::face_vjp_textbook(in, g, 1e-8, w, b);
+        double scale = 1e-300, diff = 0.0;
+        for (int k = 0; k < 14; ++k) scale = std::fmax(scale, std::fabs(*slot(b, k)));
+        for (int k = 0; k < 14; ++k) diff = std::fmax(diff, std::fabs(*slot(a, k) - *slot(b, k)));
+        worst_tb = std::fmax(worst_tb, diff / scale);
+        if (diff > 1e-9 * scale && ++differ <= 10)
+            std::printf("case %d kind %d: the derivations differ by %.3g\n", c, kind, diff / scale);
+    }
+    std::printf("textbook derivation: %d cases, worst rel diff %.3g, %ld differ\n", 12 * cases,
+                worst_tb, differ);
+    return (bad || differ) ? 1 : 0;
 }

@@ -1,5 +1,6 @@
 """CPU checks of the discrete adjoint's building blocks, no GPU needed:
-the interface VJP against central differences, and the assembled adjoint (ghost folding,
+the interface VJP against central differences and against its textbook derivation
+(tests/cpp/adjoint_face_textbook.h), and the assembled adjoint (ghost folding,
 divergence, RK3 stages, positivity masks) of tests/cpp/adjoint_ref.cpp against central
 differences of the same forward, along random directions."""
 from __future__ import annotations
@@ -23,6 +24,8 @@ def test_interface_vjp_matches_finite_differences(tmp_path):
     r = subprocess.run([str(exe), "20000"], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout
     assert " 0 bad" in r.stdout
+    # and the per-side-sum derivation agrees with the textbook one to rounding
+    assert " 0 differ" in r.stdout
 
 
 def smooth_case(problems, Nx, Ny, bc, seed):
