@@ -115,8 +115,10 @@ __device__ __forceinline__ void lo_at(const AdjParams<T> &a, int i, int j, T l[3
 // row i.  The stencil is staged exactly as the forward kernel stages it: the state of
 // ghost cells from the mirrored (reflecting, normal momentum negated) or clamped
 // (transmissive) interior cell, B where it lies, ghosts included.
+// Five 128-thread CTAs per SM (at most 102 registers; the VJP needs 104 uncapped and does
+// not spill at 102): 1% faster than four; six and seven CTAs spill and are slower.
 #ifndef SWE_ADJ_FACES_MIN_BLOCKS
-#define SWE_ADJ_FACES_MIN_BLOCKS 1
+#define SWE_ADJ_FACES_MIN_BLOCKS 5
 #endif
 template <class T, int STAGE, int DIR>
 __global__ void __launch_bounds__(AFT, SWE_ADJ_FACES_MIN_BLOCKS) k_adj_faces(const AdjParams<T> a) {
