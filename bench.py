@@ -875,6 +875,8 @@ def forms_summary(line: dict) -> dict:
         "adj_ratio_tape": r(get("adjoint", "ratio_tape")),
         "adj_ratio_segments": r(get("adjoint", "ratio_segments")),
         "adj32_ratio_sqrt": r(get("adjoint", "fp32_mixed", "ratio")),
+        "adj32_ratio_tape": r(get("adjoint", "fp32_mixed", "ratio_tape")),
+        "adj32_ratio_segments": r(get("adjoint", "fp32_mixed", "ratio_segments")),
         "adj_fd": {k: (r(v, 3) if isinstance(v, float) else v) for k, v in fd.items()
                    if k in ("eps", "directions", "grid", "steps", "median", "max",
                             "max_vs_abs_terms", "fp32_median", "fp32_max")},

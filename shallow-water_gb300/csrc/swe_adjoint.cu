@@ -751,12 +751,11 @@ template <class T>
 cudaError_t taped(Adj<T> &A, int n) { return tape_and_reverse(A, 0, n, 0); }
 
 // Segmented schedule: a first sweep stores U^(s L) in snapshot slot s for the segments
-// of L steps; each segment, last first, is then recomputed once from its snapshot with
-// its stage states taped (slots A.nseg + 1 + j), and reversed.  Every step but those of
-// the last segment is advanced twice (the sweep and its segment's taped recomputation),
-// with memory for ceil(n / L) + 1 snapshots and a tape of L steps.
-// The first sweep stops at the last segment's start and that segment is taped and
-// reversed straight away, so its steps are advanced once only.
+// of L steps, up to the last segment's start; each segment, last first, is then
+// recomputed once from its snapshot with its stage states taped (slots A.nseg + 1 + j),
+// and reversed.  Every step is advanced twice (the sweep and its segment's taped
+// recomputation), except the last segment's, which are advanced once; memory holds
+// ceil(n / L) + 1 snapshots and a tape of L steps.
 template <class T>
 cudaError_t segmented(Adj<T> &A, int n) {
     const int L = A.seg_len;

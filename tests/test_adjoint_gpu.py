@@ -109,6 +109,20 @@ def test_checkpoint_budget_does_not_change_the_gradient(gpu_lib, sw, problems):
             assert np.array_equal(r[k], base[k]), (snaps, k)
 
 
+@pytest.mark.parametrize("steps", [1, 2, 3, 4, 9])
+def test_segmented_schedule_edge_lengths(gpu_lib, sw, problems, steps):
+    # one segment, segments of one step, a last segment of one step, whole segments only:
+    # the first sweep stops at the last segment's start, which is taped straight away
+    Nx, Ny, dt = 18, 14, 1e-3
+    h, hu, hv, B, gauges, obs, _ = setup(problems, Nx, Ny, 0, steps, seed=31 + steps)
+    base = gpu_adjoint(sw, h, hu, hv, B, Nx, Ny, steps, dt, gauges, obs, 0, snapshots=steps)
+    for snaps in ("tape", "segments"):
+        r = gpu_adjoint(sw, h, hu, hv, B, Nx, Ny, steps, dt, gauges, obs, 0, snapshots=snaps)
+        assert r["J"] == base["J"]
+        for k in ("grad_h", "grad_hu", "grad_hv", "grad_B"):
+            assert np.array_equal(r[k], base[k]), (snaps, k)
+
+
 def test_autograd_function_gradients(gpu_lib, sw, port, problems):
     import torch
     Nx, Ny, steps, dt = 24, 24, 12, 1e-3
