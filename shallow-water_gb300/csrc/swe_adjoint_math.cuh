@@ -202,8 +202,9 @@ SWE_HD T msel_(T a, T b, int &sel) {
 //   dh = a (u Pc + dF1 g h) + b P,   du = h (a (Pc + dF1 uc) + b dF1),
 //   dv = h dF2 (a uc + b),
 // and the HLL speed derivatives take the sums A = dF . (FR - FL) and
-// S = dF . (UR - UL) from the same P: no flux vector is formed.  One interface costs
-// three reciprocals and two roots on the integer pipe and about 100 FP64 operations.
+// S = dF . (UR - UL) from the same P: no flux vector is formed.  In double, one
+// interface costs three reciprocals and two roots on the integer pipe and about 125
+// FP64 operations; in float the reciprocals and roots are the approximate ones.
 template <class T>
 SWE_HD void face_vjp(const FaceIn<T> &in, T g, T eps, const FaceOut<T> &d, FaceIn<T> &a) {
     // ---- forward recomputation, keeping branch decisions ----
