@@ -38,14 +38,14 @@ BYTES_PER_CELL_FP64 = 216  # algorithmic bytes per cell-update: 56 + 80 + 80 (st
 # ncu capture of this bench at 8192^2 (dram__bytes_read.sum + dram__bytes_write.sum).
 NCU_TRAFFIC_BYTES_PER_CELL_LAUNCH = 71.7
 # FP64 lane operations (DADD + DMUL + DFMA) per cell update, three stages, from the
-# ncu thread-level instruction counts of the stage kernel as it runs (strips of 4 tiles:
-# 448.7 on the FP64 pipe), plus the cell update's products (dt x L and the RK weights:
+# ncu thread-level instruction counts of the stage kernel as it runs (strips of 6 tiles:
+# 446.8 on the FP64 pipe), plus the cell update's products (dt x L and the RK weights:
 # 3 + 6 + 9 per cell update on this grid, whose 1/dx is a power of two), which run
 # correctly rounded on the integer pipes and are counted as operations of the scheme.
 # The pipe executes 2 per clock per SM, so its peak is 2 x SMs x clock.
-FP64_OPS_PER_CELL_UPDATE = 466.7
+FP64_OPS_PER_CELL_UPDATE = 464.8
 FP64_OPS_ON_INTEGER_PIPES = 18
-# The same count for lone 8x32 tiles (2.16 interfaces per cell instead of 2.06).
+# The same count for lone 8x32 tiles (2.16 interfaces per cell instead of 2.05).
 FP64_OPS_PER_CELL_UPDATE_LONE_TILES = 483.9
 # Warp instructions per cell update (the three stages) of the FP32 kernels, from their
 # ncu captures: the single grid's column sweeps (13.7 + 14.6 + 15.5) and the ensemble's

@@ -530,12 +530,11 @@ constexpr int ens_min_blocks(int TI, int TJ) {
 
 // Tiles per CTA of the single-grid stage kernel: a CTA walks a strip of this many tiles
 // along x and carries each tile's last x-face row into the next, so that only one x-face
-// row in STRIP is computed twice: 2.06 interfaces per cell for 4 tiles, against 2.16 for
-// lone 8x32 tiles.  Longer strips save a little more and lose it to the last wave of
-// each launch, whose CTAs run STRIP tiles each (8192^2: 1.058 GCUPS for 4 tiles, 1.053
-// for 8, 1.052 for 16, 1.046 for lone tiles).
+// row in STRIP is computed twice: 2.05 interfaces per cell for 6 tiles, against 2.16 for
+// lone 8x32 tiles.  Measured at 8192^2 (GCUPS, the same bits for every length): lone
+// tiles 1.046, 3 tiles 1.050, 4 1.058, 5 1.057, 6 1.062, 7 1.054, 8 1.053, 16 1.052.
 #ifndef SWE_F64_STRIP
-#define SWE_F64_STRIP 4
+#define SWE_F64_STRIP 6
 #endif
 
 // Single grid: CTA (blockIdx.x, blockIdx.y) owns tile column blockIdx.x of the strip of
