@@ -335,10 +335,12 @@ const char *swe_slabs_last_error(const swe_slabs *g);
 typedef struct swe_ens swe_ens; /* opaque */
 
 /* Tile shapes (rows x columns) the ensemble kernels are compiled for.  FP64: 8x32, 8x16,
- * 4x64.  FP32-mixed: 8x32, 16x32, 8x64, and SWE_SHAPE_COLS: work items of 64 rows by
- * 112 columns swept by column warps (the single-grid FP32 kernel's scheme). */
+ * 4x64, and SWE_SHAPE_STRIP: work items of six 8x32 tiles along x walked by one CTA (the
+ * single-grid FP64 kernel's strips).  FP32-mixed: 8x32, 16x32, 8x64, and SWE_SHAPE_COLS:
+ * work items of 64 rows by 112 columns swept by column warps (the single-grid FP32
+ * kernel's scheme). */
 enum { SWE_SHAPE_8x32 = 0, SWE_SHAPE_8x16 = 1, SWE_SHAPE_4x64 = 2, SWE_SHAPE_16x32 = 3,
-       SWE_SHAPE_8x64 = 4, SWE_SHAPE_COLS = 5 };
+       SWE_SHAPE_8x64 = 4, SWE_SHAPE_COLS = 5, SWE_SHAPE_STRIP = 6 };
 
 /* n instances with interior sizes Nx[q] x Ny[q] and domain sizes Lx[q] x Ly[q] (NULL:
  * 1.0); g, cfl, bc, precision and device come from *base (its Nx, Ny, Lx, Ly are

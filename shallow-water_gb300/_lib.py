@@ -55,7 +55,7 @@ TOTALS_NOALLOC_MAX_BLOCKS = 1024
 ADJ_TAPE_ALL = -1  # n_snapshots value of swe_adjoint_gauge's tape mode
 ADJ_SEGMENTS = -2  # n_snapshots value of its segmented schedule (snapshots every sqrt(n) steps)
 
-SHAPES = {"8x32": 0, "8x16": 1, "4x64": 2, "16x32": 3, "8x64": 4, "cols": 5}
+SHAPES = {"8x32": 0, "8x16": 1, "4x64": 2, "16x32": 3, "8x64": 4, "cols": 5, "strip": 6}
 
 
 class SweParams(ctypes.Structure):

@@ -84,10 +84,13 @@ struct EnsParams {
 };
 
 enum : int { SHAPE_8x32 = 0, SHAPE_8x16 = 1, SHAPE_4x64 = 2, SHAPE_16x32 = 3, SHAPE_8x64 = 4,
-             SHAPE_COLS = 5 };
+             SHAPE_COLS = 5, SHAPE_STRIP = 6 };
 // SHAPE_COLS (FP32 form): a work item is a strip of F32_STRIP_ROWS rows by F32_COL_BLOCK
 // columns, swept by column warps (swe_fp32.cu).
 constexpr int F32_STRIP_ROWS = 64, F32_COL_BLOCK = 112;
+// SHAPE_STRIP (FP64 form): a work item is a strip of F64_STRIP_TILES 8x32 tiles along x,
+// walked by one CTA that carries each tile's last x-face row into the next (swe_fp64.cu).
+constexpr int F64_STRIP_TILES = 6;
 
 // StageParams of instance q inside an ensemble launch.
 __device__ __forceinline__ StageParams ens_view(const EnsParams &e, int q) {

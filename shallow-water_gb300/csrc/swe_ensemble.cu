@@ -97,6 +97,7 @@ void shape_dims(int shape, int &TI, int &TJ) {
         case SHAPE_16x32: TI = 16; TJ = 32; break;
         case SHAPE_8x64: TI = 8; TJ = 64; break;
         case SHAPE_COLS: TI = F32_STRIP_ROWS; TJ = F32_COL_BLOCK; break;
+        case SHAPE_STRIP: TI = 8 * F64_STRIP_TILES; TJ = 32; break;
         default: TI = 8; TJ = 32; break;
     }
 }
@@ -105,7 +106,8 @@ bool shape_ok(const swe_ens *c, int shape) {
     if (c->f32)
         return shape == SHAPE_8x32 || shape == SHAPE_16x32 || shape == SHAPE_8x64 ||
                shape == SHAPE_COLS;
-    return shape == SHAPE_8x32 || shape == SHAPE_8x16 || shape == SHAPE_4x64;
+    return shape == SHAPE_8x32 || shape == SHAPE_8x16 || shape == SHAPE_4x64 ||
+           shape == SHAPE_STRIP;
 }
 
 void destroy_graphs(swe_ens *c) {
@@ -623,10 +625,10 @@ int swe_ens_tune(swe_ens *c, int steps, double *best_ms) try {
         c->steps_done = steps0;
         return SWE_OK;
     };
-    const int shapes64[] = {SHAPE_8x32, SHAPE_8x16, SHAPE_4x64};
+    const int shapes64[] = {SHAPE_STRIP, SHAPE_8x32, SHAPE_8x16, SHAPE_4x64};
     const int shapes32[] = {SHAPE_COLS, SHAPE_8x32, SHAPE_16x32, SHAPE_8x64};
     const int *shapes = c->f32 ? shapes32 : shapes64;
-    const int n_shapes = c->f32 ? 4 : 3;
+    const int n_shapes = 4;
     // 0: one CTA per tile; 1 / 2: a persistent grid of every resident CTA / half of them
     const int grids[] = {0, 1, 2};
     double best = 1e300;

@@ -655,6 +655,51 @@ __global__ void __launch_bounds__((TI + 1) * TJ, ens_min_blocks(TI, TJ)) k_ens_s
     }
 }
 
+// SHAPE_STRIP: a work item is a strip of up to F64_STRIP_TILES 8x32 tiles along x of one
+// instance, walked as the single-grid kernel walks its strips (the last x-face row of a
+// tile carried into the next); the same schedule and per-instance duties as
+// k_ens_stage_f64.
+template <int STAGE>
+__global__ void __launch_bounds__(9 * 32, ens_min_blocks(8, 32)) k_ens_stage_f64_strip(const EnsParams e) {
+    __shared__ StageParams s_p;
+    __shared__ int s_t;
+    tma::Pipe pipe{nullptr, 0u};  // no TMA: every tile uses the mirrored-index loader
+    for (int T = blockIdx.x; T < e.total_tiles; T += gridDim.x) {
+        if (threadIdx.x == 0) {
+            const int q = e.tile_inst[T];
+            s_p = ens_view(e, q);
+            s_t = T - e.inst[q].tile_base;
+        }
+        __syncthreads();
+        const StageParams &p = s_p;
+        const int q = e.tile_inst[T];
+        const int t = s_t;
+        const int tiles_j = e.inst[q].tiles_j;
+        const int si = t / tiles_j, tj = t - (t / tiles_j) * tiles_j;
+        const int tr0 = si * F64_STRIP_TILES;
+        const int n = min(F64_STRIP_TILES, (p.Nx + 7) / 8 - tr0);
+        bool aborted;
+        const double dt = stage_dt<true>(p, aborted);
+        if (aborted) return;  // FLAG_TIMEOUT set: the call has failed, the launch ends
+        double speed = 0.0;
+#pragma unroll 1
+        for (int k = 0; k < n; ++k) {
+            const double v = stage_tile_f64<8, 32, STAGE, SWE_ENS_F64_SOFT_CU != 0>(
+                p, (tr0 + k) * 8, tj * 32, dt, nullptr, pipe, aborted, k > 0, k + 1 < n);
+            if constexpr (STAGE == 3) speed = dmax(speed, v);
+        }
+        if (STAGE == 1 && t == 0 && threadIdx.x == 0) {
+            p.speed[p.slot_write] = 0ull;
+            if (e.dt_last) e.dt_last[q] = dt;
+        }
+        if (STAGE == 3) {
+            block_max_to_slot(speed, p.speed + p.slot_write);
+            if (t == 0 && threadIdx.x == 0) e.t[q] += dt;
+        }
+        __syncthreads();  // the next item reuses the shared tile buffers
+    }
+}
+
 // Max wave speed of interior rows [i0, i1) of a state into one slot (after an upload,
 // whole or by bands of rows).
 __global__ void __launch_bounds__(256) k_max_speed_f64(const double *h, const double *hu,
@@ -848,8 +893,35 @@ static int ens_resident_f64() {
                     std::min(ens_resident_stage_f64<TI, TJ, 2>(), ens_resident_stage_f64<TI, TJ, 3>()));
 }
 
+template <int STAGE>
+static cudaError_t ens_launch_strip_stage(const EnsParams &e, int grid, cudaStream_t s) {
+    constexpr size_t smem = sizeof(TileF64<8, 32>) + 128;
+    static bool done[64];
+    const cudaError_t err = smem_opt_in(k_ens_stage_f64_strip<STAGE>, smem, done);
+    if (err != cudaSuccess) return err;
+    k_ens_stage_f64_strip<STAGE><<<grid, 9 * 32, smem, s>>>(e);
+    return cudaGetLastError();
+}
+
+template <int STAGE>
+static int ens_resident_strip_stage() {
+    constexpr size_t smem = sizeof(TileF64<8, 32>) + 128;
+    static bool done[64];
+    if (smem_opt_in(k_ens_stage_f64_strip<STAGE>, smem, done) != cudaSuccess) return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_ens_stage_f64_strip<STAGE>, 9 * 32,
+                                                      smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
 int ens_resident_per_sm_f64(int shape) {
     switch (shape) {
+        case SHAPE_STRIP:
+            return std::min(ens_resident_strip_stage<1>(),
+                            std::min(ens_resident_strip_stage<2>(), ens_resident_strip_stage<3>()));
         case SHAPE_8x32: return ens_resident_f64<8, 32>();
         case SHAPE_8x16: return ens_resident_f64<8, 16>();
         case SHAPE_4x64: return ens_resident_f64<4, 64>();
@@ -860,6 +932,10 @@ int ens_resident_per_sm_f64(int shape) {
 cudaError_t launch_ens_stage_f64(int shape, int stage, const EnsParams &e, int grid,
                                  cudaStream_t s) {
     switch (shape) {
+        case SHAPE_STRIP:
+            return stage == 1 ? ens_launch_strip_stage<1>(e, grid, s)
+                              : (stage == 2 ? ens_launch_strip_stage<2>(e, grid, s)
+                                            : ens_launch_strip_stage<3>(e, grid, s));
         case SHAPE_8x32: return ens_launch_f64<8, 32>(stage, e, grid, s);
         case SHAPE_8x16: return ens_launch_f64<8, 16>(stage, e, grid, s);
         case SHAPE_4x64: return ens_launch_f64<4, 64>(stage, e, grid, s);

@@ -38,7 +38,8 @@ def test_fp64_ensemble_matches_oracle_per_instance(gpu_lib, sw, port, problems):
 @pytest.mark.parametrize("precision", ["fp64", "fp32_mixed"])
 def test_every_schedule_gives_identical_results(gpu_lib, sw, problems, precision):
     mem = members(problems, SIZES, seed=11)
-    shapes = ["8x32", "8x16", "4x64"] if precision == "fp64" else ["8x32", "16x32", "8x64", "cols"]
+    shapes = (["8x32", "8x16", "4x64", "strip"] if precision == "fp64"
+              else ["8x32", "16x32", "8x64", "cols"])
     results = []
     for shape in shapes:
         for grid in (0, 152, 608):
@@ -80,7 +81,7 @@ def test_tuner_restores_state_and_picks_a_schedule(gpu_lib, sw, port, problems, 
         for q, m in enumerate(mem):
             ens.upload(q, *m)
         res = ens.tune(steps=1, cache=cache)
-        assert res["shape"] in ("8x32", "8x16", "4x64") and res["ms_per_step"] > 0
+        assert res["shape"] in ("8x32", "8x16", "4x64", "strip") and res["ms_per_step"] > 0
         assert not res["cached"]
         ens.step(5)
         for q, (nx, ny) in enumerate(SIZES):
