@@ -268,113 +268,132 @@ __device__ __forceinline__ int mirror(int i, int N, bool *flip) {
 #define SWE_MOD_MIN_BLOCKS 4
 #endif
 
+// Tiles per CTA: a CTA walks a strip of this many tiles along x and carries each tile's
+// last x-interface row into the next, so that one x-interface row in SWE_MOD_STRIP is
+// computed twice instead of one in TI.
+#ifndef SWE_MOD_STRIP
+#define SWE_MOD_STRIP 6
+#endif
+
 template <int RECON, int RIEMANN, bool BATHY>
 __global__ void __launch_bounds__(NT, SWE_MOD_MIN_BLOCKS) k_modular_stage(const ModParams p) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Tile &t = *reinterpret_cast<Tile *>(smem_raw);
     const int tid = threadIdx.x;
-    const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;  // interior coordinates
-    // Stage the tile and its halo.  Rows beyond the ghost layer (a ragged last tile) are
-    // never read by a needed interface; they are zero-filled.
-    for (int e = tid; e < RI * RJ; e += NT) {
-        const int r = e / RJ, c = e - r * RJ;
-        const int i = i0 + r - 2, j = j0 + c - 2;
-        double h = 0.0, hu = 0.0, hv = 0.0, b = 0.0;
-        if (i >= -2 && i < p.Nx + 2 && j >= -2 && j < p.Ny + 2) {
-            bool fx, fy;
-            const int mi = mirror(i, p.Nx, &fx), mj = mirror(j, p.Ny, &fy);
-            const long long k = (long long)(mi + NG) * p.P + (mj + NG);
-            h = p.hs[k];
-            hu = fx ? -p.hus[k] : p.hus[k];
-            hv = fy ? -p.hvs[k] : p.hvs[k];
-            if (BATHY) {
-                b = p.B[k];
-                h = h + b;  // W.h() += B (flux_assembly_bathy.hpp:26-27)
-            }
-        }
-        t.w[0][r][c] = h;
-        t.w[1][r][c] = hu;
-        t.w[2][r][c] = hv;
-        if (BATHY) t.b[r][c] = b;
-    }
-    __syncthreads();
-    bool fail = false;
-    // One interface per thread and direction: the x-interface between staged rows a+1 and
-    // a+2 (interior rows i0+a-1 and i0+a), then, for the first TI * (TJ + 1) threads, the
-    // y-interface between staged columns b+1 and b+2.  Both directions run through one
-    // copy of the interface code (a loop, not unrolled): two inlined copies of it
-    // stalled the kernel on instruction fetch.
+    const int tr0 = blockIdx.y * SWE_MOD_STRIP, j0 = blockIdx.x * TJ;
+    const int n_tiles = min(SWE_MOD_STRIP, (p.Nx + TI - 1) / TI - tr0);
+    bool fail = false, bad = false;
 #pragma unroll 1
-    for (int dir = 0; dir < 2; ++dir) {
-        int r, c, q0, q1;  // staged cell of the interface's minus side; shared slots
-        bool valid;
-        if (dir == 0) {
-            q0 = tid / TJ;
-            q1 = tid - q0 * TJ;
-            valid = i0 + q0 - 1 <= p.Nx - 1 && j0 + q1 < p.Ny;
-            r = q0 + 1;
-            c = q1 + 2;
-        } else {
-            q0 = tid / (TJ + 1);
-            q1 = tid - q0 * (TJ + 1);
-            valid = tid < TI * (TJ + 1) && i0 + q0 < p.Nx && j0 + q1 - 1 <= p.Ny - 1;
-            r = q0 + 2;
-            c = q1 + 1;
-        }
-        if (!valid) continue;
-        double f[4];
-        interface_flux<RECON, RIEMANN, BATHY>(dir, t, r, c, p.g, p.half_g, f, &fail);
-        if (dir == 0) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) t.fx[q][q0][q1] = f[q];
-        } else {
-            t.fy[0][q0][q1] = f[0];
-            t.fy[1][q0][q1] = f[3];  // hu
-            t.fy[2][q0][q1] = f[1];  // hv of G^-
-            t.fy[3][q0][q1] = f[2];  // hv of G^+
-        }
-    }
-    __syncthreads();
-    const int r = tid / TJ, c = tid - (tid / TJ) * TJ;
-    const int i = i0 + r, j = j0 + c;
-    bool bad = false;
-    if (r < TI && i < p.Nx && j < p.Ny) {
-        // FiniteVolumeBathy / FiniteVolume::apply_spatial_operator: F^-(i) - F^+(i-1)
-        // products by -1/dx and 1/dy: exact exponent shifts when they are powers of two
-        auto mx = [&](double a) {
-            return p.kx != 127 ? x64::neg(x64::scale2(a, p.kx, x64::neg(p.nidx))) : p.nidx * a;
-        };
-        auto my = [&](double a) { return p.ky != 127 ? x64::scale2(a, p.ky, p.idy) : p.idy * a; };
-        double rhs[3];
-        rhs[0] = mx(t.fx[0][r + 1][c] - t.fx[0][r][c]) - my(t.fy[0][r][c + 1] - t.fy[0][r][c]);
-        rhs[1] = mx(t.fx[1][r + 1][c] - t.fx[2][r][c]) - my(t.fy[1][r][c + 1] - t.fy[1][r][c]);
-        rhs[2] = mx(t.fx[3][r + 1][c] - t.fx[3][r][c]) - my(t.fy[2][r][c + 1] - t.fy[3][r][c]);
-        const long long k = (long long)(i + NG) * p.P + (j + NG);
-        const double *src[3] = {p.hs, p.hus, p.hvs}, *un[3] = {p.hn, p.hun, p.hvn};
-        double o[3];
-#pragma unroll
-        for (int f = 0; f < 3; ++f) {
-            const double s = src[f][k];
-            // 1.0 * s == s and 1.0 / 4.0 * s is an exponent shift, both exact
-            if (p.stage == 1)
-                o[f] = s + cu(p.dt, rhs[f]);                                       // compute_U1
-            else if (p.stage == 2)
-                o[f] = cu(3.0 / 4.0, un[f][k]) + x64::scale2(s, -2, 0.25) + cu(p.c2, rhs[f]);  // compute_U2
-            else
-                o[f] = cu(1.0 / 3.0, un[f][k]) + cu(2.0 / 3.0, s) + cu(p.c3, rhs[f]);  // compute_U_next
-        }
-        if (BATHY) {  // enforce_positivity (serial_solver.hpp:453-478)
-            if (x64::lt(o[0], H_FLOOR)) {
-                o[0] = H_FLOOR;
-                o[1] = 0.0;
-                o[2] = 0.0;
+    for (int kt = 0; kt < n_tiles; ++kt) {
+        const int i0 = (tr0 + kt) * TI;  // interior coordinates
+        // Stage the tile and its halo.  Rows beyond the ghost layer (a ragged last tile)
+        // are never read by a needed interface; they are zero-filled.
+        for (int e = tid; e < RI * RJ; e += NT) {
+            const int r = e / RJ, c = e - r * RJ;
+            const int i = i0 + r - 2, j = j0 + c - 2;
+            double h = 0.0, hu = 0.0, hv = 0.0, b = 0.0;
+            if (i >= -2 && i < p.Nx + 2 && j >= -2 && j < p.Ny + 2) {
+                bool fx, fy;
+                const int mi = mirror(i, p.Nx, &fx), mj = mirror(j, p.Ny, &fy);
+                const long long k = (long long)(mi + NG) * p.P + (mj + NG);
+                h = p.hs[k];
+                hu = fx ? -p.hus[k] : p.hus[k];
+                hv = fy ? -p.hvs[k] : p.hvs[k];
+                if (BATHY) {
+                    b = p.B[k];
+                    h = h + b;  // W.h() += B (flux_assembly_bathy.hpp:26-27)
+                }
             }
-            auto finite = [](double x) { return (x64::bits(x) & x64::ABS) < x64::INF_BITS; };
-            bad = !finite(o[0]) || !finite(o[1]) || !finite(o[2]);
+            t.w[0][r][c] = h;
+            t.w[1][r][c] = hu;
+            t.w[2][r][c] = hv;
+            if (BATHY) t.b[r][c] = b;
         }
-        p.ho[k] = o[0];
-        p.huo[k] = o[1];
-        p.hvo[k] = o[2];
+        __syncthreads();  // staged; the previous tile's carried row is in place
+        // One interface per thread and direction: the x-interface between staged rows a+1
+        // and a+2 (interior rows i0+a-1 and i0+a), then, for the first TI * (TJ + 1)
+        // threads, the y-interface between staged columns b+1 and b+2.  Both directions
+        // run through one copy of the interface code (a loop, not unrolled): two inlined
+        // copies of it stalled the kernel on instruction fetch.  After the first tile of
+        // the strip, x-interface row 0 is the previous tile's row TI.
+#pragma unroll 1
+        for (int dir = 0; dir < 2; ++dir) {
+            int r, c, q0, q1;  // staged cell of the interface's minus side; shared slots
+            bool valid;
+            if (dir == 0) {
+                q0 = tid / TJ;
+                q1 = tid - q0 * TJ;
+                valid = (kt == 0 || q0 > 0) && i0 + q0 - 1 <= p.Nx - 1 && j0 + q1 < p.Ny;
+                r = q0 + 1;
+                c = q1 + 2;
+            } else {
+                q0 = tid / (TJ + 1);
+                q1 = tid - q0 * (TJ + 1);
+                valid = tid < TI * (TJ + 1) && i0 + q0 < p.Nx && j0 + q1 - 1 <= p.Ny - 1;
+                r = q0 + 2;
+                c = q1 + 1;
+            }
+            if (!valid) continue;
+            double f[4];
+            interface_flux<RECON, RIEMANN, BATHY>(dir, t, r, c, p.g, p.half_g, f, &fail);
+            if (dir == 0) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) t.fx[q][q0][q1] = f[q];
+            } else {
+                t.fy[0][q0][q1] = f[0];
+                t.fy[1][q0][q1] = f[3];  // hu
+                t.fy[2][q0][q1] = f[1];  // hv of G^-
+                t.fy[3][q0][q1] = f[2];  // hv of G^+
+            }
+        }
+        __syncthreads();
+        const int r = tid / TJ, c = tid - (tid / TJ) * TJ;
+        const int i = i0 + r, j = j0 + c;
+        if (r < TI && i < p.Nx && j < p.Ny) {
+            // FiniteVolumeBathy / FiniteVolume::apply_spatial_operator: F^-(i) - F^+(i-1)
+            // products by -1/dx and 1/dy: exact exponent shifts when they are powers of two
+            auto mx = [&](double a) {
+                return p.kx != 127 ? x64::neg(x64::scale2(a, p.kx, x64::neg(p.nidx))) : p.nidx * a;
+            };
+            auto my = [&](double a) { return p.ky != 127 ? x64::scale2(a, p.ky, p.idy) : p.idy * a; };
+            double rhs[3];
+            rhs[0] = mx(t.fx[0][r + 1][c] - t.fx[0][r][c]) - my(t.fy[0][r][c + 1] - t.fy[0][r][c]);
+            rhs[1] = mx(t.fx[1][r + 1][c] - t.fx[2][r][c]) - my(t.fy[1][r][c + 1] - t.fy[1][r][c]);
+            rhs[2] = mx(t.fx[3][r + 1][c] - t.fx[3][r][c]) - my(t.fy[2][r][c + 1] - t.fy[3][r][c]);
+            const long long k = (long long)(i + NG) * p.P + (j + NG);
+            const double *src[3] = {p.hs, p.hus, p.hvs}, *un[3] = {p.hn, p.hun, p.hvn};
+            double o[3];
+#pragma unroll
+            for (int f = 0; f < 3; ++f) {
+                const double s = src[f][k];
+                // 1.0 * s == s and 1.0 / 4.0 * s is an exponent shift, both exact
+                if (p.stage == 1)
+                    o[f] = s + cu(p.dt, rhs[f]);                                       // compute_U1
+                else if (p.stage == 2)
+                    o[f] = cu(3.0 / 4.0, un[f][k]) + x64::scale2(s, -2, 0.25) + cu(p.c2, rhs[f]);  // compute_U2
+                else
+                    o[f] = cu(1.0 / 3.0, un[f][k]) + cu(2.0 / 3.0, s) + cu(p.c3, rhs[f]);  // compute_U_next
+            }
+            if (BATHY) {  // enforce_positivity (serial_solver.hpp:453-478)
+                if (x64::lt(o[0], H_FLOOR)) {
+                    o[0] = H_FLOOR;
+                    o[1] = 0.0;
+                    o[2] = 0.0;
+                }
+                auto finite = [](double x) { return (x64::bits(x) & x64::ABS) < x64::INF_BITS; };
+                bad = bad || !finite(o[0]) || !finite(o[1]) || !finite(o[2]);
+            }
+            p.ho[k] = o[0];
+            p.huo[k] = o[1];
+            p.hvo[k] = o[2];
+        }
+        if (kt + 1 < n_tiles) {
+            __syncthreads();  // every update has read the x-interface rows
+            for (int e = tid; e < 4 * TJ; e += NT) {
+                const int q = e / TJ, cc = e - q * TJ;
+                t.fx[q][0][cc] = t.fx[q][TI][cc];
+            }
+        }
     }
     if (bad) atomicOr(p.flags, FLAG_NONFINITE);
     if (fail) atomicOr(p.flags, FLAG_MODULAR_HLL);
@@ -415,7 +434,8 @@ static_assert(sizeof(Tile) <= 48 * 1024, "the tile fits the default shared-memor
 template <int RECON, int RIEMANN, bool BATHY>
 cudaError_t launch_one(const ModParams &p, cudaStream_t s) {
     const int smem = (int)sizeof(Tile);
-    const dim3 grid((p.Ny + TJ - 1) / TJ, (p.Nx + TI - 1) / TI);
+    const int tile_rows = (p.Nx + TI - 1) / TI;
+    const dim3 grid((p.Ny + TJ - 1) / TJ, (tile_rows + SWE_MOD_STRIP - 1) / SWE_MOD_STRIP);
     k_modular_stage<RECON, RIEMANN, BATHY><<<grid, NT, smem, s>>>(p);
     return cudaGetLastError();
 }
