@@ -530,11 +530,19 @@ constexpr int ens_min_blocks(int TI, int TJ) {
 
 // Tiles per CTA of the single-grid stage kernel: a CTA walks a strip of this many tiles
 // along x and carries each tile's last x-face row into the next, so that only one x-face
-// row in STRIP is computed twice: 2.05 interfaces per cell for 6 tiles, against 2.16 for
-// lone 8x32 tiles.  Measured at 8192^2 (GCUPS, the same bits for every length): lone
-// tiles 1.046, 3 tiles 1.050, 4 1.058, 5 1.057, 6 1.062, 7 1.054, 8 1.053, 16 1.052.
+// row in a strip is computed twice: 2.05 interfaces per cell for 6 tiles, against 2.16
+// for lone 8x32 tiles.  Fewer, longer CTAs fill the GPU less evenly, so the length is
+// chosen per grid (strip_tiles_f64): six tiles while they leave at least 16 waves of
+// resident CTAs, else four under the same rule, else lone tiles.  Measured (GCUPS, the
+// same bits for every length):
+//   8192^2: lone 1.043-1.046, 2 1.032, 3 1.050, 4 1.056-1.058, 5 1.057, 6 1.061-1.062,
+//           7 1.054, 8 1.053, 16 1.052;
+//   4096^2: lone 1.040, 2 1.029, 4 1.048, 6 1.050;
+//   2048^2: lone 1.029, 2 1.018, 4 1.025, 6 1.015;
+//   1024^2: lone 1.001, 2 0.962, 4 0.948, 6 0.864.
+// SWE_F64_STRIP > 0 fixes the length instead.
 #ifndef SWE_F64_STRIP
-#define SWE_F64_STRIP 6
+#define SWE_F64_STRIP 0
 #endif
 
 // Single grid: CTA (blockIdx.x, blockIdx.y) owns tile column blockIdx.x of the strip of
@@ -546,7 +554,8 @@ __global__ void __launch_bounds__((TI + 1) * TJ, min_blocks(TI, TJ))
     k_stage_f64(const StageParams p, const __grid_constant__ CUtensorMap tm_h,
                 const __grid_constant__ CUtensorMap tm_u,
                 const __grid_constant__ CUtensorMap tm_v,
-                const __grid_constant__ CUtensorMap tm_b, int use_tma, int tile_row1) {
+                const __grid_constant__ CUtensorMap tm_b, int use_tma, int tile_row1,
+                int strip) {
     TileF64<TI, TJ> &S = tile_smem<TI, TJ>();
     if (use_tma && threadIdx.x == 0) tma::mbar_init(&S.bar, 1);  // visible after stage_dt
     bool aborted;
@@ -554,8 +563,8 @@ __global__ void __launch_bounds__((TI + 1) * TJ, min_blocks(TI, TJ))
     if (aborted) return;  // an earlier wait of this call gave up
     const tma::TileMaps maps{&tm_h, &tm_u, &tm_v, &tm_b};
     tma::Pipe pipe{&S.bar, 0u};
-    const int tr0 = p.tile_row0 + (int)blockIdx.y * SWE_F64_STRIP;
-    const int n = min(SWE_F64_STRIP, tile_row1 - tr0);
+    const int tr0 = p.tile_row0 + (int)blockIdx.y * strip;
+    const int n = min(strip, tile_row1 - tr0);
     double speed = 0.0;
 #pragma unroll 1
     for (int k = 0; k < n; ++k) {
@@ -805,6 +814,24 @@ static cudaError_t smem_opt_in(K kernel, size_t bytes, bool (&done)[64]) {
     return cudaSuccess;
 }
 
+// The strip length for a grid of tiles_j x tile_rows tiles (see SWE_F64_STRIP): the
+// whole grid decides, so that the bands of swe_step_host use the length of the grid.
+static int strip_tiles_f64(int tiles_j, int tile_rows) {
+    if (SWE_F64_STRIP > 0) return SWE_F64_STRIP;
+    static int sms[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+    if (!sms[dev] && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) !=
+                         cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    const long long waves16 = 16LL * min_blocks(8, 32) * sms[dev];
+    for (int len : {6, 4})
+        if ((long long)tiles_j * ((tile_rows + len - 1) / len) >= waves16) return len;
+    return 1;
+}
+
 template <int TI, int TJ, int STAGE>
 static cudaError_t single_launch_f64(StageParams p, const StageMaps *maps, cudaStream_t s,
                                      int tr0, int tr1) {
@@ -817,10 +844,12 @@ static cudaError_t single_launch_f64(StageParams p, const StageMaps *maps, cudaS
     if (tr1 < 0 || tr1 > rows) tr1 = rows;
     if (tr0 < 0 || tr0 >= tr1) return tr0 == tr1 ? cudaSuccess : cudaErrorInvalidValue;
     p.tile_row0 = tr0;
-    const dim3 grid((p.Ny + TJ - 1) / TJ, (tr1 - tr0 + SWE_F64_STRIP - 1) / SWE_F64_STRIP);
+    const int strip = strip_tiles_f64((p.Ny + TJ - 1) / TJ, rows);
+    const dim3 grid((p.Ny + TJ - 1) / TJ, (tr1 - tr0 + strip - 1) / strip);
     static const StageMaps none{};  // unused when use_tma is 0
     const StageMaps &m = maps ? *maps : none;
-    k_stage_f64<TI, TJ, STAGE><<<grid, NT, smem, s>>>(p, m.e, m.u, m.v, m.b, maps ? 1 : 0, tr1);
+    k_stage_f64<TI, TJ, STAGE><<<grid, NT, smem, s>>>(p, m.e, m.u, m.v, m.b, maps ? 1 : 0, tr1,
+                                                      strip);
     return cudaGetLastError();
 }
 
