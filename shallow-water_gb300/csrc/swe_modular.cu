@@ -268,20 +268,23 @@ __device__ __forceinline__ int mirror(int i, int N, bool *flip) {
 #define SWE_MOD_MIN_BLOCKS 4
 #endif
 
-// Tiles per CTA: a CTA walks a strip of this many tiles along x and carries each tile's
-// last x-interface row into the next, so that one x-interface row in SWE_MOD_STRIP is
-// computed twice instead of one in TI.
+// Tiles per CTA: a CTA walks a strip of tiles along x and carries each tile's last
+// x-interface row into the next, so that one x-interface row per strip is computed twice
+// instead of one per tile.  The length is chosen per grid as for the fused kernel: six
+// tiles while that leaves at least 16 waves of resident CTAs, else lone tiles
+// (SWE_MOD_STRIP > 0 fixes it).
 #ifndef SWE_MOD_STRIP
-#define SWE_MOD_STRIP 6
+#define SWE_MOD_STRIP 0
 #endif
 
 template <int RECON, int RIEMANN, bool BATHY>
-__global__ void __launch_bounds__(NT, SWE_MOD_MIN_BLOCKS) k_modular_stage(const ModParams p) {
+__global__ void __launch_bounds__(NT, SWE_MOD_MIN_BLOCKS) k_modular_stage(const ModParams p,
+                                                                          int strip) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Tile &t = *reinterpret_cast<Tile *>(smem_raw);
     const int tid = threadIdx.x;
-    const int tr0 = blockIdx.y * SWE_MOD_STRIP, j0 = blockIdx.x * TJ;
-    const int n_tiles = min(SWE_MOD_STRIP, (p.Nx + TI - 1) / TI - tr0);
+    const int tr0 = blockIdx.y * strip, j0 = blockIdx.x * TJ;
+    const int n_tiles = min(strip, (p.Nx + TI - 1) / TI - tr0);
     bool fail = false, bad = false;
 #pragma unroll 1
     for (int kt = 0; kt < n_tiles; ++kt) {
@@ -431,12 +434,27 @@ __global__ void k_modular_stable_dt(const double *h, const double *hu, const dou
 
 static_assert(sizeof(Tile) <= 48 * 1024, "the tile fits the default shared-memory limit");
 
+static int strip_tiles_mod(int tiles_j, int tile_rows) {
+    if (SWE_MOD_STRIP > 0) return SWE_MOD_STRIP;
+    static int sms[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
+    if (!sms[dev] && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) !=
+                         cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    const long long waves16 = 16LL * SWE_MOD_MIN_BLOCKS * sms[dev];
+    return (long long)tiles_j * ((tile_rows + 5) / 6) >= waves16 ? 6 : 1;
+}
+
 template <int RECON, int RIEMANN, bool BATHY>
 cudaError_t launch_one(const ModParams &p, cudaStream_t s) {
     const int smem = (int)sizeof(Tile);
-    const int tile_rows = (p.Nx + TI - 1) / TI;
-    const dim3 grid((p.Ny + TJ - 1) / TJ, (tile_rows + SWE_MOD_STRIP - 1) / SWE_MOD_STRIP);
-    k_modular_stage<RECON, RIEMANN, BATHY><<<grid, NT, smem, s>>>(p);
+    const int tiles_j = (p.Ny + TJ - 1) / TJ, tile_rows = (p.Nx + TI - 1) / TI;
+    const int strip = strip_tiles_mod(tiles_j, tile_rows);
+    const dim3 grid(tiles_j, (tile_rows + strip - 1) / strip);
+    k_modular_stage<RECON, RIEMANN, BATHY><<<grid, NT, smem, s>>>(p, strip);
     return cudaGetLastError();
 }
 
