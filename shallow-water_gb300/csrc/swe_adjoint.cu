@@ -750,23 +750,27 @@ cudaError_t tape_and_reverse(Adj<T> &A, int l, int m, int base) {
 template <class T>
 cudaError_t taped(Adj<T> &A, int n) { return tape_and_reverse(A, 0, n, 0); }
 
-// Segmented schedule: a first sweep stores U^(s L) in snapshot slot s for the segments
-// of L steps, up to the last segment's start; each segment, last first, is then
-// recomputed once from its snapshot with its stage states taped (slots A.nseg + 1 + j),
-// and reversed.  Every step is advanced twice (the sweep and its segment's taped
-// recomputation), except the last segment's, which are advanced once; memory holds
-// ceil(n / L) + 1 snapshots and a tape of L steps.
+// Segmented schedule: the steps are cut into nseg segments of L steps, counted from the
+// end (the first segment takes the remainder), so that the last segment is a whole one.
+// A first sweep stores the start of segment s in snapshot slot s, up to the last
+// segment's start; each segment, last first, is then recomputed once from its snapshot
+// with its stage states taped (slots A.nseg + 1 + j), and reversed.  Every step is
+// advanced twice (the sweep and its segment's taped recomputation), except the last
+// segment's L, which are advanced once; memory holds ceil(n / L) + 1 snapshots and a tape
+// of L steps.
 template <class T>
 cudaError_t segmented(Adj<T> &A, int n) {
     const int L = A.seg_len;
     const int last = A.nseg - 1;
-    for (int k = 0; k < last * L; ++k) {
+    auto start = [&](int sg) { return sg == 0 ? 0 : n - (A.nseg - sg) * L; };
+    int next = 1;
+    for (int k = 0; k < start(last); ++k) {
         ACK(forward_step(A, A.W, A.W, false));
-        if ((k + 1) % L == 0) ACK(store_slot(A, (k + 1) / L));
+        if (k + 1 == start(next)) ACK(store_slot(A, next++));
     }
     const int base = A.nseg + 1;
     for (int sg = last; sg >= 0; --sg) {
-        const int l = sg * L, m = std::min(L, n - l);
+        const int l = start(sg), m = start(sg + 1) - l;
         T *src[3] = {slot_field(A, sg, 0), slot_field(A, sg, 1), slot_field(A, sg, 2)};
         T *dst[3] = {slot_field(A, base, 0), slot_field(A, base, 1), slot_field(A, base, 2)};
         ACK(copy_state(A, dst, src));
