@@ -276,9 +276,10 @@ int swe_last_step_ms(const swe_ctx *ctx, double *ms);
  * schedule.  n_snapshots = SWE_ADJ_TAPE_ALL instead keeps every state and every step's
  * stage states and clamp masks from one forward sweep (device memory about
  * (75 n_steps + 400) bytes per cell), so the reverse sweep recomputes nothing.
- * n_snapshots = SWE_ADJ_SEGMENTS stores the state every L = round(sqrt(n_steps)) steps in
- * one forward sweep, then recomputes each segment of L steps once, last first, keeping
- * its stage states, and reverses it: every step is advanced twice, in memory for
+ * n_snapshots = SWE_ADJ_SEGMENTS cuts the steps into segments of L = round(sqrt(n_steps))
+ * steps (counted from the end), stores each segment's start in one forward sweep, then
+ * recomputes each segment once, last first, keeping its stage states, and reverses it:
+ * every step but the last segment's is advanced twice, in memory for
  * ceil(n_steps / L) + 1 snapshots and a tape of L steps, about
  * (24 n_steps / L + 75 L + 450) bytes per cell.  All schedules give the same J and
  * gradients, bitwise.

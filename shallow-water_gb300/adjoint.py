@@ -26,7 +26,8 @@ def gauge_misfit_gradient(solver: Solver, steps: int, dt: float, gauges, h_obs,
     about sqrt(steps)); ``snapshots="tape"`` keeps every state and every step's stage
     states instead (no recomputation, about 75 bytes per cell and step);
     ``snapshots="segments"`` stores the state every sqrt(steps) steps and recomputes each
-    segment once with its stage states kept (every step advanced twice).  Returns a dict with J, grad_h, grad_hu, grad_hv, grad_B (ghosted
+    segment once with its stage states kept (every step but the last segment's advanced
+    twice).  Returns a dict with J, grad_h, grad_hu, grad_hv, grad_B (ghosted
     arrays, zero ghosts; grad_B holds the initial state fixed) and ms (device time)."""
     g = np.asarray(gauges, dtype=np.int32).reshape(-1, 2)
     gi = np.ascontiguousarray(g[:, 0])
